@@ -1,0 +1,235 @@
+/*
+ * tina3.h -- C ABI of the GB300 triangle rasteriser + deferred shading library
+ * (libtina3.so).  Plain C: device pointers, sizes, an explicit cudaStream_t
+ * (passed as void*), no torch types.  Every entry point returns 0 on success or
+ * a negative T3_E* code.  Nothing here allocates device memory: callers pass
+ * every output and the workspace (sized by t3_workspace_size).
+ *
+ * The structs below are the descriptors the Tina drop-in layer fills from its
+ * Python objects.  All matrices are row-major 4x4 float, M[i][j] = m[4*i + j],
+ * exactly as Tina's `Engine.W2V` / `Engine.V2W` fields (tina/core/engine.py:13-14).
+ *
+ * Image buffers use Tina's field indexing: pixel (x, y) lives at x*H + y
+ * (a Taichi field of shape (W, H) is x-major), rgb at 3*(x*H + y).
+ */
+#ifndef TINA3_H
+#define TINA3_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ------------------------------------------------------- */
+#define T3_OK 0
+#define T3_EINVAL (-1)       /* bad argument (null pointer, size, enum)        */
+#define T3_ECUDA (-2)        /* a CUDA launch or runtime call failed            */
+#define T3_EOVERFLOW (-3)    /* a bin / queue capacity was exceeded: retry with
+                                a larger capacity (t3_workspace_size)          */
+#define T3_ETIMEOUT (-4)     /* a bounded device-side wait gave up               */
+#define T3_ETOOBIG (-5)      /* a size exceeds a fixed maximum of this entry     */
+#define T3_EUNSUPPORTED (-6) /* a feature combination this build does not run    */
+
+/* ---- fixed maxima ---------------------------------------------------------- */
+#define T3_MAX_LIGHTS 16   /* Lighting(maxlights=16), tina/core/lighting.py:26 */
+#define T3_MAX_NODES 24    /* material expression nodes per object             */
+#define T3_MAX_OBJECTS 8   /* objects per frame                                 */
+#define T3_MAXDEPTH (1 << 30) /* Engine.maxdepth, tina/core/engine.py:11        */
+
+/* ---- frame ---------------------------------------------------------------- */
+/* flags */
+#define T3_CULLING 1    /* TriangleRaster(culling=True)  triangle.py:96-98 */
+#define T3_CLIPPING 2   /* TriangleRaster(clipping=True) triangle.py:100-104 */
+#define T3_SMOOTHING 4  /* interpolate vertex normals     triangle.py:36-38 */
+#define T3_TEXTURING 8  /* interpolate texcoords          triangle.py:44-46 */
+#define T3_TONEMAP 16   /* ACES after shading             scene/raster.py:202-203 */
+
+typedef struct t3_frame {
+  int32_t width, height; /* Engine.res                                      */
+  int32_t flags;         /* T3_CULLING | ...                                */
+  int32_t maxdepth;      /* 2**30                                           */
+  float W2V[16];         /* proj @ view, float32 (engine.py:72-76)          */
+  float V2W[16];         /* inv(proj @ view), float32                       */
+  float bias[2];         /* pixel-centre offset, (0.5, 0.5) by default      */
+  float bgcolor[3];      /* Scene(bgcolor=...) image.fill value             */
+  int32_t _pad;
+} t3_frame;
+
+/* ---- meshes (the mesh protocol of the tina.mesh package) ----------------------------- */
+#define T3_MESH_SOUP 0    /* SimpleMesh: verts [n,3,3], norms [n,3,3], coors [n,3,2]   */
+#define T3_MESH_GRID 1    /* MeshGrid:   pos [nx,ny,3], nrm [nx,ny,3], tex [nx,ny,2]   */
+#define T3_MESH_INDEXED 2 /* MeshModel / ConnectiveMesh: per-vertex arrays + face indices */
+
+/* mesh flags (mesh-edit nodes) */
+#define T3_MESH_TRANSFORM 1   /* MeshTransform        tina/mesh/trans.py:23-40 */
+#define T3_MESH_NOCULL 2      /* MeshNoCulling        tina/mesh/cull.py:31-58  */
+#define T3_MESH_FLIP_ORDER 4  /* MeshFlipCulling      tina/mesh/cull.py:5-28   */
+#define T3_MESH_FLIP_NORMAL 8 /* MeshFlipNormal       tina/mesh/cull.py:61-66  */
+#define T3_MESH_FLAT_NORMAL 16/* MeshFlatNormal       tina/mesh/norm.py:5-14   */
+
+typedef struct t3_mesh {
+  int32_t kind;        /* T3_MESH_*                                              */
+  int32_t flags;       /* T3_MESH_* edit flags                                   */
+  int64_t nfaces;      /* faces of the underlying mesh (before NOCULL doubling)  */
+  const float* verts;  /* positions (layout per kind)                            */
+  const float* norms;  /* normals, may be NULL unless T3_SMOOTHING               */
+  const float* coors;  /* texcoords, may be NULL unless T3_TEXTURING             */
+  const int32_t* faces;/* INDEXED: corner k of face f reads attribute slot s at
+                          faces[f*face_stride + k*corner_stride + s]             */
+  int32_t face_stride;   /* 3 (ConnectiveMesh [n,3]) or 9 (MeshModel [n,3,3])    */
+  int32_t corner_stride; /* 1 or 3                                              */
+  int32_t slot_vert, slot_coor, slot_norm; /* 0,0,0 or 0,1,2 (v, vt, vn)          */
+  int32_t grid_nx, grid_ny; /* GRID: vertex counts                               */
+  int32_t attr_stride;      /* floats per face in face_attr                      */
+  const float* face_attr;   /* per-face material attributes [n, attr_stride]     */
+  float trans[16];          /* MeshTransform.trans                                */
+  float trans_normal[9];    /* transpose(inv(trans))[:3,:3]                       */
+  int32_t _pad;
+} t3_mesh;
+
+/* ---- materials: an expression tree (tina/matr/material.py, nodes.py) -------- */
+/* value nodes */
+#define T3_OP_CONST 0    /* v[0..2], width in b (1 or 3)                 nodes.py:42-49 */
+#define T3_OP_ATTR 1     /* per-face attribute: a = channel, b = width   (FaceAttr)      */
+#define T3_OP_INPUT 2    /* a = 0 pos, 1 color, 2 normal, 3 texcoord     nodes.py:79-96  */
+#define T3_OP_FRESNEL 3  /* a = metallic, b = albedo, c = specular       material.py:69-83 */
+/* leaf materials */
+#define T3_OP_LAMBERT 16 /*                                              material.py:387-442 */
+#define T3_OP_PHONG 17   /* a = shineness                                material.py:445-472 */
+#define T3_OP_COOK 18    /* a = roughness, b = fresnel                   material.py:244-384 */
+#define T3_OP_EMISSION 19/*                                              material.py:659-681 */
+/* combinators */
+#define T3_OP_MIX 32     /* a = mat1, b = mat2, c = factor               material.py:86-145 */
+#define T3_OP_SCALE 33   /* a = mat, b = factor                          material.py:148-191 */
+#define T3_OP_ADD 34     /* a = mat1, b = mat2                           material.py:194-238 */
+
+typedef struct t3_node {
+  int32_t op, a, b, c;
+  float v[4];
+} t3_node;
+
+typedef struct t3_material {
+  int32_t nnodes; /* used entries of nodes[]                                 */
+  int32_t root;   /* index of the root material node                          */
+  t3_node nodes[T3_MAX_NODES];
+} t3_material;
+
+typedef struct t3_object {
+  t3_mesh mesh;
+  t3_material material;
+  int64_t face_base; /* first global face id of this object                  */
+  int64_t nfaces;    /* faces exposed to the raster (x2 for T3_MESH_NOCULL)    */
+} t3_object;
+
+/* ---- lighting (tina/core/lighting.py) -------------------------------------- */
+typedef struct t3_light {
+  float dir[4];   /* xyz, w: 0 directional (normalised dir), 1 point (position) */
+  float color[4]; /* rgb, pad                                                    */
+} t3_light;
+
+#define T3_LIGHT_LAMPS 0  /* Lighting: emission + ambient + sum of lamps     */
+#define T3_LIGHT_IBL 1    /* SkyboxLighting: sample_ibl + emission           */
+
+typedef struct t3_lighting {
+  int32_t mode;     /* T3_LIGHT_*                                             */
+  int32_t nlights;
+  float ambient[4];
+  t3_light lights[T3_MAX_LIGHTS];
+} t3_lighting;
+
+/* ---- whole-frame parameters --------------------------------------------- */
+typedef struct t3_scene {
+  t3_frame frame;
+  t3_lighting lighting;
+  int32_t nobjects;
+  int32_t _pad;
+  t3_object objects[T3_MAX_OBJECTS];
+} t3_scene;
+
+/* outputs of one frame (device pointers; any may be NULL except rgb)       */
+typedef struct t3_outputs {
+  float* rgb;        /* [W,H,3] scene.img (post tonemap when T3_TONEMAP)      */
+  int32_t* face_id;  /* [W,H] winning global face id, -1 where empty          */
+  int32_t* depth;    /* [W,H] Engine.depth (int32(depth_f * 2**30)), maxdepth  */
+  float* depth_f;    /* [W,H] the winning fragment's float depth, +inf empty    */
+} t3_outputs;
+
+/* raster modes */
+#define T3_RASTER_DIRECT 0 /* per-face threads, global packed u64 atomicMin     */
+#define T3_RASTER_BINNED 1 /* tile bins + per-tile queues in shared memory       */
+
+/* ---- entry points ------------------------------------------------------- */
+
+/* Version / build probe. */
+int t3_version(void);
+
+/* sizeof() of t3_frame, t3_mesh, t3_node, t3_material, t3_object, t3_light,
+ * t3_lighting, t3_scene, t3_outputs in that order, for binding-layer layout
+ * checks.  Returns the count; writes min(n, count) values when out != NULL. */
+int t3_struct_sizes(int64_t* out, int n);
+
+/* Workspace bytes needed by t3_render for this scene at raster mode `mode`
+ * with tile edge `tile` (8, 16 or 32) and `bin_capacity` entries per frame
+ * for the binned mode (0 = automatic).  Replaces the per-raster fields that
+ * TriangleRaster.__init__ allocates (tina/core/triangle.py:16-29). */
+int t3_workspace_size(const t3_scene* scene, int mode, int tile,
+                      int64_t bin_capacity, size_t* bytes);
+
+/* Engine.clear_depth (tina/core/engine.py:68-70) for the packed buffer:
+ * depth_id[W*H] = empty key. */
+int t3_clear(uint64_t* depth_id, int64_t npixels, void* stream);
+
+/* TriangleRaster.set_object + render_occup (tina/core/triangle.py:72-131)
+ * for one object: per-face transform, cull, clip, setup and depth test into
+ * the packed buffer key = (uint32(depth) ^ 0x80000000) << 32 | global face id,
+ * whose unsigned minimum equals the serial reference's winner (lowest depth,
+ * ties to the lowest face id).  `workspace` holds the large-triangle queue.
+ * `status` (device int32) receives T3_* codes of device-side overflows. */
+int t3_raster(const t3_frame* frame, const t3_object* object,
+              uint64_t* depth_id, void* workspace, size_t workspace_bytes,
+              int32_t* status, void* stream);
+
+/* TriangleRaster.render_color + Shader + Lighting + ToneMapping
+ * (tina/core/triangle.py:134-153, shader.py:119-131, lighting.py:84-98,
+ * postp/tonemap.py:10-12) for all objects of the scene.  The workspace (at
+ * least t3_workspace_size bytes) receives the device copy of the scene. */
+int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
+             size_t workspace_bytes, const t3_outputs* out, void* stream);
+
+/* Scene.render (tina/scene/raster.py:168-207) for one frame: clear, raster
+ * every object (mode T3_RASTER_*), shade, tonemap. */
+int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
+              void* workspace, size_t workspace_bytes, int32_t* status,
+              const t3_outputs* out, void* stream);
+
+/* MeshGrid.pre_compute (tina/mesh/grid.py:27-36): nrm[i,j] =
+ * normalize(cross(pos[i+1,j] - pos[i-1,j], pos[i,j+1] - pos[i,j-1])) with
+ * clamped neighbours, for a [nx, ny, 3] float grid. */
+int t3_grid_normals(const float* pos, float* nrm, int nx, int ny, void* stream);
+
+/* ToneMapping.apply (tina/postp/tonemap.py:10-12): in-place ACES on n floats. */
+int t3_tonemap(float* rgb, int64_t n, void* stream);
+
+/* t3_render with timing events: when stage_events is non-NULL, events [0..3]
+ * (cudaEvent_t handles, entries may be NULL) are recorded on `stream` at frame
+ * start, after the key clear, after the rasteriser and after shading. */
+int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
+                     void* workspace, size_t workspace_bytes, int32_t* status,
+                     const t3_outputs* out, void* stream, void* const* stage_events);
+
+/* Timing-event helpers for callers without their own CUDA runtime binding. */
+int t3_event_create(void** event);
+int t3_event_destroy(void* event);
+int t3_event_elapsed_ms(void* start, void* end, float* ms); /* waits for `end` */
+
+/* Reads back the device status word written by the last t3_raster/t3_render
+ * (synchronises `stream`). */
+int t3_read_status(const int32_t* status, int32_t* host_status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TINA3_H */

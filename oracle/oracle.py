@@ -1,0 +1,104 @@
+"""Test infrastructure only: ctypes binding of oracle/_build/libtina_oracle.so.
+
+`render(scene)` evaluates a taichi_three_gb300.Scene on the CPU with the
+restatement in oracle/tina_oracle.cpp, from the same t3_scene descriptor the
+CUDA library receives (its pointers placed on the host).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        lib = C.CDLL(path)
+        f = lib.oracle_render_f32
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 5
+        f = lib.oracle_render_f64
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 4
+        lib.oracle_grid_normals.restype = C.c_int
+        lib.oracle_grid_normals.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        lib.oracle_aces_f32.restype = C.c_int
+        lib.oracle_aces_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        lib.oracle_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def render_desc(sc, mode=0, nthreads=0, fp64=False, want_depth_f=True):
+    """Renders a t3_scene descriptor (host pointers).  mode 0 = serial face order
+    (the oracle), 1 = OpenMP packed-key minimum (the timed CPU baseline)."""
+    lib = load()
+    W, H = sc.frame.width, sc.frame.height
+    out = {
+        'rgb_pre': np.empty((W, H, 3), np.float32),
+        'face_id': np.empty((W, H), np.int32),
+        'depth': np.empty((W, H), np.int32),
+    }
+    if fp64:
+        out['rgb'] = np.empty((W, H, 3), np.float64)
+        rc = lib.oracle_render_f64(C.addressof(sc), mode, nthreads, _p(out['rgb']), _p(out['rgb_pre']),
+                                   _p(out['face_id']), _p(out['depth']))
+    else:
+        out['rgb'] = np.empty((W, H, 3), np.float32)
+        out['depth_f'] = np.empty((W, H), np.float32) if want_depth_f else None
+        rc = lib.oracle_render_f32(C.addressof(sc), mode, nthreads, _p(out['rgb']), _p(out['rgb_pre']),
+                                   _p(out['face_id']), _p(out['depth']), _p(out['depth_f']))
+    if rc != 0:
+        raise RuntimeError(f'oracle render failed ({rc})')
+    return out
+
+
+def render(scene, mode=0, nthreads=0, fp64=False, want_depth_f=True):
+    """Renders a taichi_three_gb300.Scene with the oracle (runs the scene's mesh
+    pre_compute on the host first, e.g. MeshGrid normals)."""
+    for obj in scene.objects:
+        pre_compute_host(obj)
+    sc, keep = scene.describe('cpu')
+    out = render_desc(sc, mode, nthreads, fp64, want_depth_f)
+    del keep
+    return out
+
+
+def grid_normals(pos):
+    lib = load()
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    nrm = np.empty_like(pos)
+    lib.oracle_grid_normals(_p(pos), _p(nrm), pos.shape[0], pos.shape[1])
+    return nrm
+
+
+def aces(x):
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    lib.oracle_aces_f32(_p(x), _p(y), x.size)
+    return y
+
+
+def pre_compute_host(obj):
+    """The mesh's pre_compute on the CPU (MeshGrid normals); the device copy of the
+    mesh is left untouched."""
+    base = obj
+    while hasattr(base, 'mesh') and not hasattr(base, 'res'):
+        base = base.mesh
+    if hasattr(base, 'auto_normals') and base.auto_normals and not base.pos.is_cuda:
+        import torch
+        base.nrm = torch.from_numpy(grid_normals(base.pos.numpy()))
+
+
+def max_threads():
+    return load().oracle_max_threads()

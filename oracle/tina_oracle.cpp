@@ -1,0 +1,731 @@
+// tina_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// A CPU restatement of Tina's triangle rasteriser and deferred shading pass
+// (taichi-dev/taichi_three, "Tina" v0.1.1), used by tests/ and by bench.py's
+// CPU-baseline leg as the checker.  It is never part of the product path.
+//
+// Parity status: the reference is Python on the Taichi JIT, Taichi is not
+// installable here, and the reference ships no golden vectors or tests with
+// assertions.  This restatement is pinned against the reference's own Python
+// source executed by tests/golden/make_golden.py (a pure-Python stand-in for the
+// subset of the Taichi DSL the path uses); where that pin does not reach, the
+// restatement is "parity unpinned".
+//
+// Semantics restated (file:line are within the reference project):
+//   * Engine              tina/core/engine.py:6-76   (W2V/V2W, bias, maxdepth 2**30)
+//   * mapply / mapply_pos tina/common.py:170-184     (op order below)
+//   * TriangleRaster      tina/core/triangle.py:89-153
+//   * interpolate         tina/core/triangle.py:32-49
+//   * calc_view_ray       tina/core/shader.py:82-93
+//   * Lighting            tina/core/lighting.py:84-98
+//   * materials           tina/matr/material.py:69-472, 659-706
+//   * nodes               tina/matr/nodes.py:42-96
+//   * ACES tonemap        tina/advans.py:32-34, tina/postp/tonemap.py:10-12
+//   * mesh getters        tina/mesh/simple.py:34-48, grid.py:27-70, trans.py:29-40,
+//                         cull.py:5-66, norm.py:5-14, model.py:50-73, conn.py:117-140
+//
+// Floating point: every expression is evaluated in the Real type (float for the
+// bit-exact oracle, double for the FP64 twin) left to right as the Taichi source
+// is written, with IEEE division and square root, and the file is compiled with
+// -ffp-contract=off so no multiply-add is fused.  Vector helpers follow Taichi's
+// Matrix methods: dot = ((x0*y0 + x1*y1) + x2*y2), norm = sqrt(dot(v, v)),
+// normalized = v * (1 / norm), 2-D cross = a.x*b.y - a.y*b.x, integer powers by
+// repeated squaring (x**2 = x*x, x**5 = x * ((x*x)*(x*x))).
+//
+// The serial mode walks faces in index order, which makes the reference's
+// `atomic_min(depth) > depth` (triangle.py:123) deterministic: the lowest depth
+// wins and ties keep the lowest face id.  The parallel mode (OpenMP) reaches the
+// same result through a 64-bit packed (depth, face id) compare-and-swap minimum;
+// it is the timed CPU baseline.
+
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/tina3.h"
+
+namespace {
+
+template <class R> struct v2 { R x, y; };
+template <class R> struct v3 { R x, y, z; };
+
+template <class R> inline v3<R> mk3(R a, R b, R c) { return v3<R>{a, b, c}; }
+template <class R> inline v3<R> add(v3<R> a, v3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R> inline v3<R> sub(v3<R> a, v3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R> inline v3<R> mul(v3<R> a, v3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class R> inline v3<R> muls(R s, v3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R> inline v3<R> mulv(v3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R> inline v3<R> divs(v3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class R> inline v3<R> neg(v3<R> a) { return {-a.x, -a.y, -a.z}; }
+template <class R> inline R dot(v3<R> a, v3<R> b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+template <class R> inline R norm(v3<R> a) { return std::sqrt(dot(a, a)); }
+template <class R> inline v3<R> normalized(v3<R> a) {
+  R inv = R(1) / norm(a);
+  return muls(inv, a);
+}
+template <class R> inline v3<R> cross(v3<R> a, v3<R> b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R> inline R cross2(v2<R> a, v2<R> b) { return a.x * b.y - a.y * b.x; }
+// reflect(I, N) = I - 2 * N.dot(I) * N   (tina/common.py:197-199)
+template <class R> inline v3<R> reflect(v3<R> I, v3<R> N) {
+  R d = R(2) * dot(N, I);
+  return sub(I, muls(d, N));
+}
+// A Taichi-source literal: an f32 constant in the FP32 oracle, the exact decimal in FP64.
+template <class R> inline R cst(double x) { return sizeof(R) == 4 ? (R)(float)x : (R)x; }
+template <class R> inline R pow2(R x) { return x * x; }
+template <class R> inline R ipow(R x, int n) {
+  R result = R(1), base = x;
+  bool first = true;
+  while (n > 0) {
+    if (n & 1) { result = first ? base : result * base; first = false; }
+    n >>= 1;
+    if (n) base = base * base;
+  }
+  return first ? R(1) : result;
+}
+template <class R> inline R pow5(R x) {
+  R x2 = x * x;
+  R x4 = x2 * x2;
+  return x * x4;
+}
+// Taichi `min`/`max` on floats keep the non-NaN operand (LLVM minnum/maxnum).
+template <class R> inline R fmin_(R a, R b) { return std::fmin(a, b); }
+template <class R> inline R fmax_(R a, R b) { return std::fmax(a, b); }
+
+// float -> int32 with truncation; out-of-range values saturate (the Taichi source
+// leaves them undefined) and NaN maps to INT32_MIN.
+template <class R> inline int32_t trunc_i32(R x) {
+  if (!(x >= R(-2147483648.0))) return INT32_MIN;
+  if (x >= R(2147483648.0)) return INT32_MAX;
+  return (int32_t)x;
+}
+
+// mapply(mat, pos, wei) (tina/common.py:170-177):
+//   res_i = M[i][3]*wei; res_i += M[i][0]*p0; res_i += M[i][1]*p1; res_i += M[i][2]*p2
+//   rew   = M[3][3]*wei; rew  += M[3][0]*p0; rew  += M[3][1]*p1; rew  += M[3][2]*p2
+template <class R> struct mat4 { R m[16]; };
+template <class R> inline void mapply(const mat4<R>& M, v3<R> p, R wei, v3<R>& res, R& rew) {
+  const R* m = M.m;
+  R r0 = m[3] * wei, r1 = m[7] * wei, r2 = m[11] * wei;
+  r0 = r0 + m[0] * p.x; r0 = r0 + m[1] * p.y; r0 = r0 + m[2] * p.z;
+  r1 = r1 + m[4] * p.x; r1 = r1 + m[5] * p.y; r1 = r1 + m[6] * p.z;
+  r2 = r2 + m[8] * p.x; r2 = r2 + m[9] * p.y; r2 = r2 + m[10] * p.z;
+  R w = m[15] * wei;
+  w = w + m[12] * p.x; w = w + m[13] * p.y; w = w + m[14] * p.z;
+  res = {r0, r1, r2};
+  rew = w;
+}
+template <class R> inline v3<R> mapply_pos(const mat4<R>& M, v3<R> p) {
+  v3<R> r; R w;
+  mapply(M, p, R(1), r, w);
+  return divs(r, w);
+}
+// 3x3 @ vec (Taichi Matrix.__matmul__: acc = M[i][0]*v0; acc += M[i][1]*v1; ...)
+template <class R> inline v3<R> matvec3(const R* m, v3<R> v) {
+  R a0 = m[0] * v.x; a0 = a0 + m[1] * v.y; a0 = a0 + m[2] * v.z;
+  R a1 = m[3] * v.x; a1 = a1 + m[4] * v.y; a1 = a1 + m[5] * v.z;
+  R a2 = m[6] * v.x; a2 = a2 + m[7] * v.y; a2 = a2 + m[8] * v.z;
+  return {a0, a1, a2};
+}
+
+template <class R> inline v3<R> ld3(const float* p) { return {(R)p[0], (R)p[1], (R)p[2]}; }
+template <class R> inline v3<R> ld2(const float* p) { return {(R)p[0], (R)p[1], R(0)}; }
+
+// ---------------------------------------------------------------------------
+// Mesh protocol (get_face_verts / get_face_norms / get_face_coors).
+// Mesh-edit flags are applied in one fixed nesting:
+//   MeshNoCulling(MeshFlipNormal(MeshFlipCulling(MeshFlatNormal(MeshTransform(base)))))
+// ---------------------------------------------------------------------------
+template <class R> struct Mesh {
+  const t3_mesh* d;
+  mat4<R> trans;
+  R tn[9];
+  explicit Mesh(const t3_mesh* desc) : d(desc) {
+    for (int i = 0; i < 16; i++) trans.m[i] = (R)desc->trans[i];
+    for (int i = 0; i < 9; i++) tn[i] = (R)desc->trans_normal[i];
+  }
+  // corner k, attribute 0 = vert, 1 = norm, 2 = coor, of a base-mesh face
+  const float* base_ptr(int64_t f, int k, int attr) const {
+    const float* arr = attr == 0 ? d->verts : attr == 1 ? d->norms : d->coors;
+    int width = attr == 2 ? 2 : 3;
+    if (d->kind == T3_MESH_SOUP) {
+      return arr + (f * 3 + k) * width;
+    } else if (d->kind == T3_MESH_GRID) {
+      // MeshGrid._get_face_props (tina/mesh/grid.py:46-58)
+      int64_t stride = d->grid_nx - 1;
+      int64_t m = f / 2;
+      int64_t i = m / stride, j = m % stride;
+      int64_t ii[4] = {i, i + 1, i + 1, i};
+      int64_t jj[4] = {j, j, j + 1, j + 1};
+      int sel[3] = {0, 1, 2};
+      if (f % 2 != 0) { sel[0] = 0; sel[1] = 2; sel[2] = 3; }
+      int c = sel[k];
+      return arr + (ii[c] * d->grid_ny + jj[c]) * width;
+    } else {
+      int slot = attr == 0 ? d->slot_vert : attr == 1 ? d->slot_norm : d->slot_coor;
+      int64_t idx = d->faces[f * d->face_stride + k * d->corner_stride + slot];
+      return arr + idx * width;
+    }
+  }
+  void verts(int64_t n, v3<R> v[3]) const {
+    int64_t f = n;
+    bool flip = (d->flags & T3_MESH_FLIP_ORDER) != 0;
+    if (d->flags & T3_MESH_NOCULL) { f = n / 2; if (n % 2 != 0) flip = !flip; }
+    v3<R> t[3];
+    for (int k = 0; k < 3; k++) {
+      t[k] = ld3<R>(base_ptr(f, k, 0));
+      if (d->flags & T3_MESH_TRANSFORM) t[k] = mapply_pos(trans, t[k]);
+    }
+    for (int k = 0; k < 3; k++) v[k] = flip ? t[2 - k] : t[k];
+  }
+  void norms(int64_t n, v3<R> v[3]) const {
+    int64_t f = n;
+    bool flip = (d->flags & T3_MESH_FLIP_ORDER) != 0;
+    bool negate = (d->flags & T3_MESH_FLIP_NORMAL) != 0;
+    if (d->flags & T3_MESH_NOCULL) {
+      f = n / 2;
+      if (n % 2 != 0) { flip = !flip; negate = !negate; }
+    }
+    v3<R> t[3];
+    if (d->flags & T3_MESH_FLAT_NORMAL) {
+      // MeshFlatNormal._calc_norm (tina/mesh/norm.py:7-9) on the transformed verts
+      v3<R> p[3];
+      for (int k = 0; k < 3; k++) {
+        p[k] = ld3<R>(base_ptr(f, k, 0));
+        if (d->flags & T3_MESH_TRANSFORM) p[k] = mapply_pos(trans, p[k]);
+      }
+      v3<R> nn = normalized(cross(sub(p[1], p[0]), sub(p[2], p[0])));
+      t[0] = t[1] = t[2] = nn;
+    } else {
+      for (int k = 0; k < 3; k++) {
+        t[k] = ld3<R>(base_ptr(f, k, 1));
+        if (d->flags & T3_MESH_TRANSFORM) t[k] = matvec3(tn, t[k]);
+      }
+    }
+    for (int k = 0; k < 3; k++) {
+      v[k] = flip ? t[2 - k] : t[k];
+      if (negate) v[k] = neg(v[k]);
+    }
+  }
+  void coors(int64_t n, v3<R> v[3]) const {
+    int64_t f = n;
+    bool flip = (d->flags & T3_MESH_FLIP_ORDER) != 0;
+    if (d->flags & T3_MESH_NOCULL) { f = n / 2; if (n % 2 != 0) flip = !flip; }
+    v3<R> t[3];
+    for (int k = 0; k < 3; k++) t[k] = ld2<R>(base_ptr(f, k, 2));
+    for (int k = 0; k < 3; k++) v[k] = flip ? t[2 - k] : t[k];
+  }
+  int64_t base_face(int64_t n) const { return (d->flags & T3_MESH_NOCULL) ? n / 2 : n; }
+};
+
+// ---------------------------------------------------------------------------
+// Per-face setup, shared by render_occup and render_color (triangle.py:93-113)
+// ---------------------------------------------------------------------------
+template <class R> struct Setup {
+  v3<R> Av, Bv, Cv;
+  v2<R> a, b, c;
+  v2<R> bcn, can;
+  v3<R> wscale;
+  int32_t botx, boty, topx, topy;
+  bool culled;
+};
+
+template <class R>
+inline v2<R> to_viewport(v3<R> p, int W, int H) {
+  // (p.xy * 0.5 + 0.5) * res   (tina/core/engine.py:59-61)
+  return {(p.x * R(0.5) + R(0.5)) * (R)W, (p.y * R(0.5) + R(0.5)) * (R)H};
+}
+
+template <class R> inline bool inside_clip(v3<R> p) {
+  return (R(-1) <= p.x && p.x <= R(1)) && (R(-1) <= p.y && p.y <= R(1)) &&
+         (R(-1) <= p.z && p.z <= R(1));
+}
+
+template <class R>
+void face_setup(const mat4<R>& W2V, const t3_frame& fr, const v3<R> v[3], Setup<R>& s) {
+  s.culled = false;
+  s.Av = mapply_pos(W2V, v[0]);
+  s.Bv = mapply_pos(W2V, v[1]);
+  s.Cv = mapply_pos(W2V, v[2]);
+  v2<R> e1 = {s.Bv.x - s.Av.x, s.Bv.y - s.Av.y};
+  v2<R> e2 = {s.Cv.x - s.Av.x, s.Cv.y - s.Av.y};
+  R facing = cross2(e1, e2);
+  if (facing <= R(0) && (fr.flags & T3_CULLING)) { s.culled = true; return; }
+  if (fr.flags & T3_CLIPPING) {
+    if (!inside_clip(s.Av) && !inside_clip(s.Bv) && !inside_clip(s.Cv)) { s.culled = true; return; }
+  }
+  s.a = to_viewport(s.Av, fr.width, fr.height);
+  s.b = to_viewport(s.Bv, fr.width, fr.height);
+  s.c = to_viewport(s.Cv, fr.width, fr.height);
+  R minx = fmin_(fmin_(s.a.x, s.b.x), s.c.x), miny = fmin_(fmin_(s.a.y, s.b.y), s.c.y);
+  R maxx = fmax_(fmax_(s.a.x, s.b.x), s.c.x), maxy = fmax_(fmax_(s.a.y, s.b.y), s.c.y);
+  int32_t bx = trunc_i32(std::floor(minx)), by = trunc_i32(std::floor(miny));
+  int32_t tx = trunc_i32(std::ceil(maxx)), ty = trunc_i32(std::ceil(maxy));
+  s.botx = bx > 0 ? bx : 0;
+  s.boty = by > 0 ? by : 0;
+  s.topx = tx < fr.width - 1 ? tx : fr.width - 1;
+  s.topy = ty < fr.height - 1 ? ty : fr.height - 1;
+  v2<R> ba = {s.b.x - s.a.x, s.b.y - s.a.y};
+  v2<R> ca = {s.c.x - s.a.x, s.c.y - s.a.y};
+  R n = cross2(ba, ca);
+  s.bcn = {(s.b.x - s.c.x) / n, (s.b.y - s.c.y) / n};
+  s.can = {(s.c.x - s.a.x) / n, (s.c.y - s.a.y) / n};
+  v3<R> r; R wa, wb, wc;
+  mapply(W2V, v[0], R(1), r, wa);
+  mapply(W2V, v[1], R(1), r, wb);
+  mapply(W2V, v[2], R(1), r, wc);
+  s.wscale = {R(1) / wa, R(1) / wb, R(1) / wc};
+}
+
+// barycentric weights at pixel (x, y) (triangle.py:115-119 and :147-151)
+template <class R>
+inline v3<R> face_weights(const Setup<R>& s, const t3_frame& fr, int32_t x, int32_t y) {
+  v2<R> pos = {(R)x + (R)fr.bias[0], (R)y + (R)fr.bias[1]};
+  R w_bc = cross2(v2<R>{pos.x - s.b.x, pos.y - s.b.y}, s.bcn);
+  R w_ca = cross2(v2<R>{pos.x - s.c.x, pos.y - s.c.y}, s.can);
+  v3<R> wei = {w_bc * s.wscale.x, w_ca * s.wscale.y, ((R(1) - w_bc) - w_ca) * s.wscale.z};
+  R sum = (wei.x + wei.y) + wei.z;
+  return divs(wei, sum);
+}
+
+template <class R> inline R face_depth(const Setup<R>& s, v3<R> wei) {
+  return (wei.x * s.Av.z + wei.y * s.Bv.z) + wei.z * s.Cv.z;
+}
+
+// ---------------------------------------------------------------------------
+// Materials (tina/matr/material.py, nodes.py).  Values are carried as 3-vectors
+// with a width tag; width-1 values broadcast like Taichi scalar * vector.
+// ---------------------------------------------------------------------------
+template <class R> struct Val { v3<R> v; int w; };
+template <class R> inline Val<R> sval(R s) { return {{s, s, s}, 1}; }
+template <class R> inline Val<R> vmul(Val<R> a, Val<R> b) { return {mul(a.v, b.v), a.w > b.w ? a.w : b.w}; }
+template <class R> inline Val<R> vadd(Val<R> a, Val<R> b) { return {add(a.v, b.v), a.w > b.w ? a.w : b.w}; }
+template <class R> inline Val<R> one_minus(Val<R> a) { return {{R(1) - a.v.x, R(1) - a.v.y, R(1) - a.v.z}, a.w}; }
+
+template <class R> struct Frag {
+  v3<R> pos, normal, texcoord;
+  const float* attr; // per-face attributes of this fragment's face
+};
+
+template <class R> struct MaterialEval {
+  const t3_material* m;
+  const Frag<R>* fr;
+
+  Val<R> value(int i) const {
+    const t3_node& n = m->nodes[i];
+    switch (n.op) {
+    case T3_OP_CONST:
+      return {{(R)n.v[0], (R)n.v[1], (R)n.v[2]}, n.b == 3 ? 3 : 1};
+    case T3_OP_ATTR: {
+      if (n.b == 1) return sval<R>((R)fr->attr[n.a]);
+      return {{(R)fr->attr[n.a], (R)fr->attr[n.a + 1], (R)fr->attr[n.a + 2]}, 3};
+    }
+    case T3_OP_INPUT:
+      if (n.a == 0) return {fr->pos, 3};
+      if (n.a == 1) return {{R(1), R(1), R(1)}, 3}; // color = V(1,1,1) triangle.py:48
+      if (n.a == 2) return {fr->normal, 3};
+      return {fr->texcoord, 2};
+    case T3_OP_FRESNEL: {
+      // f0 = metallic * albedo + (1 - metallic) * 0.16 * specular**2  material.py:69-71
+      Val<R> met = value(n.a), alb = value(n.b), spc = value(n.c);
+      Val<R> t1 = vmul(met, alb);
+      Val<R> om = one_minus(met);
+      Val<R> t2 = vmul(vmul(om, sval<R>(cst<R>(0.16))), vmul(spc, spc));
+      return vadd(t1, t2);
+    }
+    default:
+      return sval<R>(R(0));
+    }
+  }
+
+  // brdf(nrm, idir=L, odir=V)
+  Val<R> brdf(int i, v3<R> nrm, v3<R> idir, v3<R> odir) const {
+    const t3_node& n = m->nodes[i];
+    switch (n.op) {
+    case T3_OP_LAMBERT:
+      return sval<R>(inv_pi());
+    case T3_OP_PHONG: {
+      Val<R> mm = value(n.a);
+      R m_ = mm.v.x;
+      v3<R> rdir = reflect(neg(idir), nrm);
+      R VoR = fmax_(R(0), dot(odir, rdir));
+      // VoR**m: a Python-int shineness (node flag c == 1) is an integer power by
+      // repeated squaring, a float one is pow().
+      const t3_node& mn = m->nodes[n.a];
+      R p = (mn.op == T3_OP_CONST && mn.c == 1) ? ipow(VoR, (int)mn.v[0]) : std::pow(VoR, m_);
+      return sval<R>((p * (m_ + R(2))) / R(2));
+    }
+    case T3_OP_COOK:
+      return cook_brdf(n, nrm, idir, odir);
+    case T3_OP_EMISSION:
+      return sval<R>(R(0));
+    case T3_OP_MIX: {
+      Val<R> fac = value(n.c);
+      Val<R> w1 = brdf(n.a, nrm, idir, odir), w2 = brdf(n.b, nrm, idir, odir);
+      return vadd(vmul(one_minus(fac), w1), vmul(fac, w2));
+    }
+    case T3_OP_SCALE: {
+      Val<R> fac = value(n.b);
+      return vmul(fac, brdf(n.a, nrm, idir, odir));
+    }
+    case T3_OP_ADD:
+      return vadd(brdf(n.a, nrm, idir, odir), brdf(n.b, nrm, idir, odir));
+    default:
+      return sval<R>(R(0));
+    }
+  }
+
+  static R inv_pi() { return cst<R>(1.0 / M_PI); }        // 1 / ti.pi
+  static R c_eps_big() { return cst<R>(1.0 - 1e-10); }    // 1 - EPS
+  static R c_eps() { return cst<R>(1e-10); }              // EPS
+  static R c_eps6() { return cst<R>(1e-6); }              // advans.eps
+  static R c_4pi() { return cst<R>(4.0 * M_PI); }         // 4 * ti.pi
+
+  // CookTorrance.sub_brdf / brdf (material.py:322-362)
+  Val<R> cook_brdf(const t3_node& n, v3<R> nrm, v3<R> idir, v3<R> odir) const {
+    R roughness = value(n.a).v.x;
+    Val<R> f0 = value(n.b);
+    const R EPS = c_eps();
+    v3<R> half = normalized(add(idir, odir));
+    R NoH = fmax_(EPS, dot(half, nrm));
+    R NoL = fmax_(EPS, dot(idir, nrm));
+    R NoV = fmax_(EPS, dot(odir, nrm));
+    R VoH = fmin_(c_eps_big(), fmax_(EPS, dot(half, odir)));
+    R alpha2 = fmax_(c_eps6(), pow2(roughness));
+    R denom = R(1) - pow2(NoH) * (R(1) - alpha2);
+    R ndf = alpha2 / pow2(denom);
+    R k = alpha2 / R(2);
+    R vdf = R(1) / ((NoV * k + R(1)) - k);
+    vdf = vdf * (R(1) / ((NoL * k + R(1)) - k));
+    vdf = vdf / (R(1) * (R(1) - alpha2) + c_4pi() * alpha2);
+    R p5 = pow5(R(1) - VoH);
+    Val<R> fdf = {{f0.v.x + (R(1) - f0.v.x) * p5, f0.v.y + (R(1) - f0.v.y) * p5,
+                   f0.v.z + (R(1) - f0.v.z) * p5}, f0.w};
+    // fdf * vdf * ndf
+    return {{(fdf.v.x * vdf) * ndf, (fdf.v.y * vdf) * ndf, (fdf.v.z * vdf) * ndf}, fdf.w};
+  }
+
+  Val<R> ambient(int i) const {
+    const t3_node& n = m->nodes[i];
+    switch (n.op) {
+    case T3_OP_LAMBERT: case T3_OP_PHONG: case T3_OP_COOK:
+      return sval<R>(R(1));
+    case T3_OP_EMISSION:
+      return sval<R>(R(0));
+    case T3_OP_MIX: {
+      Val<R> fac = value(n.c);
+      return vadd(vmul(one_minus(fac), ambient(n.a)), vmul(fac, ambient(n.b)));
+    }
+    case T3_OP_SCALE:
+      return vmul(value(n.b), ambient(n.a));
+    case T3_OP_ADD:
+      return vadd(ambient(n.a), ambient(n.b));
+    default:
+      return sval<R>(R(0));
+    }
+  }
+
+  Val<R> emission(int i) const {
+    const t3_node& n = m->nodes[i];
+    switch (n.op) {
+    case T3_OP_EMISSION:
+      return sval<R>(R(1));
+    case T3_OP_MIX: {
+      Val<R> fac = value(n.c);
+      return vadd(vmul(one_minus(fac), emission(n.a)), vmul(fac, emission(n.b)));
+    }
+    case T3_OP_SCALE:
+      return vmul(value(n.b), emission(n.a));
+    case T3_OP_ADD:
+      return vadd(emission(n.a), emission(n.b));
+    default:
+      return sval<R>(R(0));
+    }
+  }
+};
+
+// ACES (tina/advans.py:32-34)
+template <class R> inline R aces1(R c) {
+  return (c * (cst<R>(2.51) * c + cst<R>(0.03))) / (c * (cst<R>(2.43) * c + cst<R>(0.59)) + cst<R>(0.14));
+}
+
+// Lighting.shade_color (tina/core/lighting.py:84-98)
+template <class R>
+v3<R> shade_lamps(const t3_lighting& L, const MaterialEval<R>& me, v3<R> pos, v3<R> normal,
+                  v3<R> viewdir) {
+  v3<R> res = {R(0), R(0), R(0)};
+  int root = me.m->root;
+  res = add(res, me.emission(root).v);
+  v3<R> amb = {(R)L.ambient[0], (R)L.ambient[1], (R)L.ambient[2]};
+  res = add(res, mul(amb, me.ambient(root).v));
+  for (int l = 0; l < L.nlights; l++) {
+    const t3_light& lt = L.lights[l];
+    v3<R> lxyz = {(R)lt.dir[0], (R)lt.dir[1], (R)lt.dir[2]};
+    R lw = (R)lt.dir[3];
+    v3<R> lcolor = {(R)lt.color[0], (R)lt.color[1], (R)lt.color[2]};
+    v3<R> light_dir = sub(lxyz, mulv(pos, lw));
+    R dist = norm(light_dir);
+    light_dir = divs(light_dir, dist);
+    R cos_i = dot(normal, light_dir);
+    if (cos_i > R(0)) {
+      lcolor = divs(lcolor, pow2(dist));
+      v3<R> mcolor = me.brdf(root, normal, light_dir, viewdir).v;
+      res = add(res, mul(muls(cos_i, lcolor), mcolor));
+    }
+  }
+  return res;
+}
+
+template <class R> struct Ctx {
+  const t3_scene* sc;
+  mat4<R> W2V, V2W;
+};
+
+// render_color for one pixel of one object (triangle.py:134-153 -> shader.py:119-131)
+template <class R>
+v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, int64_t f,
+                  int32_t x, int32_t y, R* depth_f_out) {
+  const t3_frame& fr = cx.sc->frame;
+  v3<R> v[3];
+  mesh.verts(f, v);
+  Setup<R> s;
+  face_setup(cx.W2V, fr, v, s);
+  v3<R> wei = face_weights(s, fr, x, y);
+  if (depth_f_out) *depth_f_out = face_depth(s, wei);
+  // interpolate (triangle.py:32-49)
+  v3<R> pos = add(add(muls(wei.x, v[0]), muls(wei.y, v[1])), muls(wei.z, v[2]));
+  v3<R> normal;
+  if (fr.flags & T3_SMOOTHING) {
+    v3<R> n[3];
+    mesh.norms(f, n);
+    normal = add(add(muls(wei.x, n[0]), muls(wei.y, n[1])), muls(wei.z, n[2]));
+  } else {
+    normal = cross(sub(v[1], v[0]), sub(v[2], v[0]));
+  }
+  normal = normalized(normal);
+  v3<R> tex = {R(0), R(0), R(0)};
+  if (fr.flags & T3_TEXTURING) {
+    v3<R> t[3];
+    mesh.coors(f, t);
+    tex = add(add(muls(wei.x, t[0]), muls(wei.y, t[1])), muls(wei.z, t[2]));
+    tex.z = R(0);
+  }
+  // calc_viewdir (shader.py:82-93)
+  R px = (R)x + (R)fr.bias[0], py = (R)y + (R)fr.bias[1];
+  R ux = (px / (R)fr.width) * R(2) - R(1);
+  R uy = (py / (R)fr.height) * R(2) - R(1);
+  v3<R> ro = mapply_pos(cx.V2W, v3<R>{ux, uy, R(-1)});
+  v3<R> ro1 = mapply_pos(cx.V2W, v3<R>{ux, uy, R(1)});
+  v3<R> rd = normalized(sub(ro1, ro));
+  v3<R> viewdir = neg(rd);
+
+  Frag<R> fg;
+  fg.pos = pos; fg.normal = normal; fg.texcoord = tex;
+  int64_t bf = mesh.base_face(f);
+  fg.attr = ob.mesh.face_attr ? ob.mesh.face_attr + bf * ob.mesh.attr_stride : nullptr;
+  MaterialEval<R> me{&ob.material, &fg};
+  return shade_lamps(cx.sc->lighting, me, pos, normal, viewdir);
+}
+
+inline uint64_t pack_key(int32_t depth, uint32_t id) {
+  return ((uint64_t)((uint32_t)depth ^ 0x80000000u) << 32) | (uint64_t)id;
+}
+
+template <class R>
+inline void raster_face(const Ctx<R>& cx, const Setup<R>& s, uint64_t id,
+                        std::atomic<uint64_t>* keys) {
+  const t3_frame& fr = cx.sc->frame;
+  const int H = fr.height;
+  for (int32_t x = s.botx; x <= s.topx; x++) {
+    for (int32_t y = s.boty; y <= s.topy; y++) {
+      v3<R> wei = face_weights(s, fr, x, y);
+      if (wei.x >= R(0) && wei.y >= R(0) && wei.z >= R(0)) {
+        R depth_f = face_depth(s, wei);
+        int32_t d = trunc_i32(depth_f * (R)fr.maxdepth);
+        if (d >= fr.maxdepth) continue; // can never pass `old > depth`
+        uint64_t key = pack_key(d, (uint32_t)id);
+        int64_t P_ = (int64_t)x * H + y;
+        uint64_t cur = keys[P_].load(std::memory_order_relaxed);
+        while (key < cur && !keys[P_].compare_exchange_weak(cur, key)) {
+        }
+      }
+    }
+  }
+}
+
+template <class R>
+int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb64,
+           int32_t* id_out, int32_t* depth_out, float* depth_f_out, int nthreads) {
+  const t3_frame& fr = sc->frame;
+  const int W = fr.width, H = fr.height;
+  const int64_t P = (int64_t)W * H;
+  Ctx<R> cx;
+  cx.sc = sc;
+  for (int i = 0; i < 16; i++) { cx.W2V.m[i] = (R)fr.W2V[i]; cx.V2W.m[i] = (R)fr.V2W[i]; }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  std::vector<int32_t> depth(P, fr.maxdepth);   // Engine.depth
+  std::vector<int64_t> gid(P, -1);               // global winner id
+  std::vector<v3<R>> img(P);                     // Scene.image
+  for (int64_t i = 0; i < P; i++) img[i] = {(R)fr.bgcolor[0], (R)fr.bgcolor[1], (R)fr.bgcolor[2]};
+
+  if (mode == 0) {
+    // Scene.render's per-object loop (tina/scene/raster.py:183-187), serial faces
+    std::vector<int64_t> occup(P);
+    for (int o = 0; o < sc->nobjects; o++) {
+      const t3_object& ob = sc->objects[o];
+      Mesh<R> mesh(&ob.mesh);
+      // render_occup (triangle.py:89-131)
+      std::fill(occup.begin(), occup.end(), -1);
+      for (int64_t f = 0; f < ob.nfaces; f++) {
+        v3<R> v[3];
+        mesh.verts(f, v);
+        Setup<R> s;
+        face_setup(cx.W2V, fr, v, s);
+        if (s.culled) continue;
+        for (int32_t x = s.botx; x <= s.topx; x++) {
+          for (int32_t y = s.boty; y <= s.topy; y++) {
+            v3<R> wei = face_weights(s, fr, x, y);
+            if (wei.x >= R(0) && wei.y >= R(0) && wei.z >= R(0)) {
+              R depth_f = face_depth(s, wei);
+              int32_t d = trunc_i32(depth_f * (R)fr.maxdepth);
+              int64_t P_ = (int64_t)x * H + y;
+              int32_t old = depth[P_];          // ti.atomic_min returns the old value
+              if (d < old) depth[P_] = d;
+              if (old > d) {
+                if (depth[P_] >= d) { occup[P_] = f; gid[P_] = ob.face_base + f; }
+              }
+            }
+          }
+        }
+      }
+      // render_color (triangle.py:134-153)
+      for (int64_t i = 0; i < P; i++) {
+        if (occup[i] == -1) continue;
+        img[i] = shade_pixel(cx, ob, mesh, occup[i], (int32_t)(i / H), (int32_t)(i % H), (R*)nullptr);
+      }
+    }
+  } else {
+    // all objects into one packed (depth, global id) minimum, then one shading
+    // pass with each pixel's winner: the same image as the per-object loop.
+    std::vector<std::atomic<uint64_t>> keys(P);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < P; i++) keys[i].store(~0ull, std::memory_order_relaxed);
+    for (int o = 0; o < sc->nobjects; o++) {
+      const t3_object& ob = sc->objects[o];
+      Mesh<R> mesh(&ob.mesh);
+#pragma omp parallel for schedule(dynamic, 2048)
+      for (int64_t f = 0; f < ob.nfaces; f++) {
+        v3<R> v[3];
+        mesh.verts(f, v);
+        Setup<R> s;
+        face_setup(cx.W2V, fr, v, s);
+        if (s.culled) continue;
+        raster_face(cx, s, (uint64_t)(ob.face_base + f), keys.data());
+      }
+    }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < P; i++) {
+      uint64_t k = keys[i].load(std::memory_order_relaxed);
+      if (k == ~0ull) continue;
+      depth[i] = (int32_t)((uint32_t)(k >> 32) ^ 0x80000000u);
+      gid[i] = (int64_t)(uint32_t)k;
+      for (int o = 0; o < sc->nobjects; o++) {
+        const t3_object& ob = sc->objects[o];
+        if (gid[i] >= ob.face_base && gid[i] < ob.face_base + ob.nfaces) {
+          Mesh<R> mesh(&ob.mesh);
+          img[i] = shade_pixel(cx, ob, mesh, gid[i] - ob.face_base, (int32_t)(i / H),
+                               (int32_t)(i % H), (R*)nullptr);
+        }
+      }
+    }
+  }
+
+  // ToneMapping.apply (postp/tonemap.py:10-12) and the outputs
+#pragma omp parallel for schedule(static) if (mode == 1)
+  for (int64_t i = 0; i < P; i++) {
+    v3<R> c = img[i];
+    if (rgb_pre) { rgb_pre[3 * i] = (float)c.x; rgb_pre[3 * i + 1] = (float)c.y; rgb_pre[3 * i + 2] = (float)c.z; }
+    if (fr.flags & T3_TONEMAP) c = {aces1(c.x), aces1(c.y), aces1(c.z)};
+    if (rgb) { rgb[3 * i] = (float)c.x; rgb[3 * i + 1] = (float)c.y; rgb[3 * i + 2] = (float)c.z; }
+    if (rgb64) { rgb64[3 * i] = (double)c.x; rgb64[3 * i + 1] = (double)c.y; rgb64[3 * i + 2] = (double)c.z; }
+    if (id_out) id_out[i] = (int32_t)gid[i];
+    if (depth_out) depth_out[i] = depth[i];
+    if (depth_f_out) {
+      float df = std::numeric_limits<float>::infinity();
+      for (int o = 0; o < sc->nobjects && gid[i] >= 0; o++) {
+        const t3_object& ob = sc->objects[o];
+        if (gid[i] >= ob.face_base && gid[i] < ob.face_base + ob.nfaces) {
+          // the winning fragment's float depth, recomputed as render_color does
+          Mesh<R> mesh(&ob.mesh);
+          v3<R> v[3];
+          mesh.verts(gid[i] - ob.face_base, v);
+          Setup<R> s;
+          face_setup(cx.W2V, fr, v, s);
+          df = (float)face_depth(s, face_weights(s, fr, (int32_t)(i / H), (int32_t)(i % H)));
+        }
+      }
+      depth_f_out[i] = df;
+    }
+  }
+  return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+// FP32 restatement (bit-exact target).  mode 0 = serial face order (the oracle),
+// mode 1 = OpenMP with packed-key minimum (the timed CPU baseline).
+int oracle_render_f32(const t3_scene* sc, int mode, int nthreads, float* rgb, float* rgb_pre,
+                      int32_t* face_id, int32_t* depth, float* depth_f) {
+  return render<float>(sc, mode, rgb, rgb_pre, nullptr, face_id, depth, depth_f, nthreads);
+}
+
+// FP64 twin: the same algorithm in double precision, for error statements.
+int oracle_render_f64(const t3_scene* sc, int mode, int nthreads, double* rgb, float* rgb_pre,
+                      int32_t* face_id, int32_t* depth) {
+  return render<double>(sc, mode, nullptr, rgb_pre, rgb, face_id, depth, nullptr, nthreads);
+}
+
+// MeshGrid.pre_compute (tina/mesh/grid.py:27-36)
+int oracle_grid_normals(const float* pos, float* nrm, int nx, int ny) {
+  for (int i = 0; i < nx; i++) {
+    for (int j = 0; j < ny; j++) {
+      int i2 = i - 1 > 0 ? i - 1 : 0, j2 = j - 1 > 0 ? j - 1 : 0;
+      int i1 = i + 1 < nx - 1 ? i + 1 : nx - 1, j1 = j + 1 < ny - 1 ? j + 1 : ny - 1;
+      auto at = [&](int a, int b) { return ld3<float>(pos + ((int64_t)a * ny + b) * 3); };
+      v3<float> dy = sub(at(i, j1), at(i, j2));
+      v3<float> dx = sub(at(i1, j), at(i2, j));
+      v3<float> n = normalized(cross(dx, dy));
+      float* o = nrm + ((int64_t)i * ny + j) * 3;
+      o[0] = n.x; o[1] = n.y; o[2] = n.z;
+    }
+  }
+  return 0;
+}
+
+int oracle_aces_f32(const float* in, float* out, int64_t n) {
+  for (int64_t i = 0; i < n; i++) out[i] = aces1<float>(in[i]);
+  return 0;
+}
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+} // extern "C"

@@ -1,0 +1,23 @@
+"""taichi_three_gb300 -- Tina's triangle rasteriser and deferred shading pass,
+rebuilt for one GB300 (sm_103a) GPU.
+
+Drop-in names follow Tina (taichi-dev/taichi_three): `import taichi_three_gb300
+as tina`, then tina.Scene, tina.SimpleMesh, tina.PBR, ... as in the reference's
+docs.  Rendering runs in hand-written CUDA kernels behind the C ABI of
+include/tina3.h; there is no CPU fallback.
+"""
+__version__ = (0, 1, 1)
+
+from .matrix import (affine, eularXYZ, frustum, identity, lookat, orbit_camera, ortho,
+                     orthogonal, perspective, quaternion, scale, translate)
+from .nodes import ChessboardTexture, Const, FaceAttr, Input, Node, Param, Texture
+from .materials import (AddMaterial, Classic, CookTorrance, Diffuse, Emission, FresnelFactor,
+                        IMaterial, Lambert, Lamp, MixMaterial, PBR, Phong, ScaleMaterial,
+                        compile_material)
+from .lighting import Lighting
+from .mesh import (MAX, ConnectiveMesh, MeshFlatNormal, MeshFlipCulling, MeshFlipNormal, MeshGrid,
+                   MeshModel, MeshNoCulling, MeshTransform, PrimitiveMesh, SimpleMesh)
+from .engine import Engine
+from .scene import Scene, Shader, TriangleRaster
+from .postp import ToneMapping, aces_tonemap
+from . import workloads

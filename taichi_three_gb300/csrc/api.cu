@@ -1,0 +1,336 @@
+// api.cu -- the extern "C" entry points of libtina3.so (declared in include/tina3.h).
+//
+// Host-side responsibilities: argument checks, flattening each material tree
+// into weighted lobes, the workspace layout, and the launch sequence of one
+// frame (Scene.render, tina/scene/raster.py:168-207):
+//   upload scene + zero counters -> clear keys -> per object: raster (+ big
+//   faces) -> shade (+ tonemap).
+// No entry point allocates device memory; every buffer is caller-owned.
+#include <cstring>
+
+#include "t3_internal.cuh"
+
+namespace t3 {
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t ws_scene_end() { return align256(T3_WS_SCENE + sizeof(DevScene)); }
+size_t ws_big_items() { return ws_scene_end(); }
+
+static int is_leaf(int op) {
+  return op == T3_OP_LAMBERT || op == T3_OP_PHONG || op == T3_OP_COOK || op == T3_OP_EMISSION;
+}
+static int is_value(int op) {
+  return op == T3_OP_CONST || op == T3_OP_ATTR || op == T3_OP_INPUT || op == T3_OP_FRESNEL;
+}
+
+// Walks the material tree from `node`, multiplying factors along the path.
+static int flatten_rec(const t3_material& in, int node, int* fac, int nfac, DevMaterial& out,
+                       int depth) {
+  if (depth > T3_MAX_NODES) return T3_EINVAL;
+  if (node < 0 || node >= in.nnodes) return T3_EINVAL;
+  const t3_node& nd = in.nodes[node];
+  if (is_leaf(nd.op)) {
+    if (out.nlobes >= T3_MAX_LOBES || nfac > T3_MAX_FACTORS) return T3_EUNSUPPORTED;
+    DevLobe& lb = out.lobes[out.nlobes++];
+    std::memset(&lb, 0, sizeof(lb));
+    lb.kind = nd.op;
+    lb.nfac = nfac;
+    for (int j = 0; j < nfac; j++) lb.fac[j] = fac[j];
+    lb.p0 = nd.a;
+    lb.p1 = nd.b;
+    if (nd.op == T3_OP_PHONG) {
+      if (nd.a < 0 || nd.a >= in.nnodes || !is_value(in.nodes[nd.a].op)) return T3_EINVAL;
+      const t3_node& mn = in.nodes[nd.a];
+      if (mn.op == T3_OP_CONST && mn.c == 1 && mn.v[0] >= 1.0f && mn.v[0] <= 65536.0f)
+        lb.int_pow = (int)mn.v[0];
+    }
+    if (nd.op == T3_OP_COOK) {
+      if (nd.a < 0 || nd.a >= in.nnodes || nd.b < 0 || nd.b >= in.nnodes) return T3_EINVAL;
+      if (!is_value(in.nodes[nd.a].op) || !is_value(in.nodes[nd.b].op)) return T3_EINVAL;
+    }
+    return T3_OK;
+  }
+  int f2[T3_MAX_FACTORS + 2];
+  for (int j = 0; j < nfac && j < T3_MAX_FACTORS; j++) f2[j] = fac[j];
+  switch (nd.op) {
+  case T3_OP_MIX: {
+    if (nd.c < 0 || nd.c >= in.nnodes || !is_value(in.nodes[nd.c].op)) return T3_EINVAL;
+    if (nfac + 1 > T3_MAX_FACTORS) return T3_EUNSUPPORTED;
+    f2[nfac] = nd.c | T3_FAC_ONE_MINUS;
+    int r = flatten_rec(in, nd.a, f2, nfac + 1, out, depth + 1);
+    if (r) return r;
+    f2[nfac] = nd.c;
+    return flatten_rec(in, nd.b, f2, nfac + 1, out, depth + 1);
+  }
+  case T3_OP_SCALE: {
+    if (nd.b < 0 || nd.b >= in.nnodes || !is_value(in.nodes[nd.b].op)) return T3_EINVAL;
+    if (nfac + 1 > T3_MAX_FACTORS) return T3_EUNSUPPORTED;
+    f2[nfac] = nd.b;
+    return flatten_rec(in, nd.a, f2, nfac + 1, out, depth + 1);
+  }
+  case T3_OP_ADD: {
+    int r = flatten_rec(in, nd.a, f2, nfac, out, depth + 1);
+    if (r) return r;
+    return flatten_rec(in, nd.b, f2, nfac, out, depth + 1);
+  }
+  default:
+    return T3_EINVAL;
+  }
+}
+
+int flatten_material(const t3_material& in, DevMaterial& out) {
+  std::memset(&out, 0, sizeof(out));
+  if (in.nnodes <= 0 || in.nnodes > T3_MAX_NODES) return T3_EINVAL;
+  // value nodes may only reference earlier value nodes (evaluated in order)
+  for (int i = 0; i < in.nnodes; i++) {
+    const t3_node& nd = in.nodes[i];
+    if (nd.op == T3_OP_FRESNEL) {
+      const int refs[3] = {nd.a, nd.b, nd.c};
+      for (int r : refs)
+        if (r < 0 || r >= i || !is_value(in.nodes[r].op)) return T3_EINVAL;
+    }
+    if (nd.op == T3_OP_ATTR && (nd.a < 0 || (nd.b != 1 && nd.b != 3))) return T3_EINVAL;
+    if (nd.op == T3_OP_INPUT && (nd.a < 0 || nd.a > 3)) return T3_EINVAL;
+  }
+  out.nnodes = in.nnodes;
+  for (int i = 0; i < in.nnodes; i++) out.nodes[i] = in.nodes[i];
+  int fac[T3_MAX_FACTORS];
+  return flatten_rec(in, in.root, fac, 0, out, 0);
+}
+
+static int check_mesh(const t3_mesh& m, int flags, int64_t nfaces) {
+  if (nfaces < 0) return T3_EINVAL;
+  if (nfaces == 0) return T3_OK;
+  if (!m.verts) return T3_EINVAL;
+  if ((flags & T3_SMOOTHING) && !(m.flags & T3_MESH_FLAT_NORMAL) && !m.norms) return T3_EINVAL;
+  if ((flags & T3_TEXTURING) && !m.coors) return T3_EINVAL;
+  if (m.kind == T3_MESH_GRID) {
+    if (m.grid_nx < 2 || m.grid_nx != m.grid_ny) return T3_EINVAL;
+  } else if (m.kind == T3_MESH_INDEXED) {
+    if (!m.faces || m.face_stride <= 0 || m.corner_stride <= 0) return T3_EINVAL;
+  } else if (m.kind != T3_MESH_SOUP) {
+    return T3_EINVAL;
+  }
+  return T3_OK;
+}
+
+static int check_frame(const t3_frame& fr) {
+  if (fr.width <= 0 || fr.height <= 0 || fr.width > 32768 || fr.height > 32768) return T3_EINVAL;
+  if (fr.maxdepth <= 0) return T3_EINVAL;
+  return T3_OK;
+}
+
+int make_dev_scene(const t3_scene& sc, DevScene& out) {
+  std::memset(&out, 0, sizeof(out));
+  int r = check_frame(sc.frame);
+  if (r) return r;
+  if (sc.nobjects < 0 || sc.nobjects > T3_MAX_OBJECTS) return T3_ETOOBIG;
+  if (sc.lighting.nlights < 0 || sc.lighting.nlights > T3_MAX_LIGHTS) return T3_ETOOBIG;
+  if (sc.lighting.mode != T3_LIGHT_LAMPS) return T3_EUNSUPPORTED;
+  out.frame = sc.frame;
+  out.lighting = sc.lighting;
+  out.nobjects = sc.nobjects;
+  int64_t total = 0;
+  for (int o = 0; o < sc.nobjects; o++) {
+    const t3_object& ob = sc.objects[o];
+    r = check_mesh(ob.mesh, sc.frame.flags, ob.nfaces);
+    if (r) return r;
+    if (ob.face_base != total) return T3_EINVAL;  // objects are numbered consecutively
+    total += ob.nfaces;
+    if (total >= (int64_t)0xFFFFFFFFll) return T3_ETOOBIG;  // ids are uint32 in the key
+    out.obj[o].mesh = ob.mesh;
+    out.obj[o].face_base = ob.face_base;
+    out.obj[o].nfaces = ob.nfaces;
+    r = flatten_material(ob.material, out.obj[o].mat);
+    if (r) return r;
+    // per-face attribute reads must stay inside the mesh's attribute rows
+    for (int i = 0; i < ob.material.nnodes; i++) {
+      const t3_node& nd = ob.material.nodes[i];
+      if (nd.op != T3_OP_ATTR) continue;
+      if (!ob.mesh.face_attr || nd.a + nd.b > ob.mesh.attr_stride) return T3_EINVAL;
+    }
+  }
+  return T3_OK;
+}
+
+static int64_t max_object_faces(const t3_scene& sc) {
+  int64_t m = 0;
+  for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
+    if (sc.objects[o].nfaces > m) m = sc.objects[o].nfaces;
+  return m;
+}
+
+struct Layout {
+  size_t counters, scene, big_items, keys, end;
+  uint32_t big_capacity;
+};
+
+static Layout layout_for(const t3_scene& sc) {
+  Layout L;
+  L.counters = T3_WS_COUNTERS;
+  L.scene = T3_WS_SCENE;
+  L.big_items = ws_big_items();
+  int64_t cap = max_object_faces(sc);
+  if (cap < 1) cap = 1;
+  L.big_capacity = (uint32_t)cap;
+  L.keys = align256(L.big_items + sizeof(uint32_t) * (size_t)cap);
+  L.end = align256(L.keys + sizeof(uint64_t) * (size_t)sc.frame.width * (size_t)sc.frame.height);
+  return L;
+}
+
+static int cuda_rc(cudaError_t e) { return e == cudaSuccess ? T3_OK : T3_ECUDA; }
+
+} // namespace t3
+
+using namespace t3;
+
+extern "C" {
+
+int t3_version(void) { return 8; }
+
+// sizeof of every ABI struct, for binding-layer layout checks.
+int t3_struct_sizes(int64_t* out, int n) {
+  const int64_t s[] = {(int64_t)sizeof(t3_frame),    (int64_t)sizeof(t3_mesh),
+                       (int64_t)sizeof(t3_node),     (int64_t)sizeof(t3_material),
+                       (int64_t)sizeof(t3_object),   (int64_t)sizeof(t3_light),
+                       (int64_t)sizeof(t3_lighting), (int64_t)sizeof(t3_scene),
+                       (int64_t)sizeof(t3_outputs)};
+  const int k = (int)(sizeof(s) / sizeof(s[0]));
+  if (!out) return k;
+  for (int i = 0; i < n && i < k; i++) out[i] = s[i];
+  return k;
+}
+
+int t3_workspace_size(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
+                      size_t* bytes) {
+  (void)tile;
+  (void)bin_capacity;
+  if (!scene || !bytes) return T3_EINVAL;
+  if (mode != T3_RASTER_DIRECT) return T3_EUNSUPPORTED;
+  int r = check_frame(scene->frame);
+  if (r) return r;
+  if (scene->nobjects < 0 || scene->nobjects > T3_MAX_OBJECTS) return T3_ETOOBIG;
+  *bytes = layout_for(*scene).end;
+  return T3_OK;
+}
+
+int t3_clear(uint64_t* depth_id, int64_t npixels, void* stream) {
+  if (!depth_id || npixels < 0) return T3_EINVAL;
+  return cuda_rc(launch_clear(reinterpret_cast<unsigned long long*>(depth_id), npixels,
+                              (cudaStream_t)stream));
+}
+
+int t3_raster(const t3_frame* frame, const t3_object* object, uint64_t* depth_id, void* workspace,
+              size_t workspace_bytes, int32_t* status, void* stream) {
+  if (!frame || !object || !depth_id || !workspace || !status) return T3_EINVAL;
+  int r = check_frame(*frame);
+  if (r) return r;
+  r = check_mesh(object->mesh, frame->flags, object->nfaces);
+  if (r) return r;
+  // workspace: one counter + the big-face queue of this object
+  const size_t need = 256 + sizeof(uint32_t) * (size_t)(object->nfaces > 0 ? object->nfaces : 1);
+  if (workspace_bytes < need) return T3_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
+  BigQueue big;
+  big.count = reinterpret_cast<uint32_t*>(ws);
+  big.items = reinterpret_cast<uint32_t*>(ws + 256);
+  big.capacity = (uint32_t)(object->nfaces > 0 ? object->nfaces : 1);
+  big.status = status;
+  cudaError_t e = cudaMemsetAsync(big.count, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return T3_ECUDA;
+  return cuda_rc(launch_raster_direct(*frame, *object, reinterpret_cast<unsigned long long*>(depth_id),
+                                      big, 128, st));
+}
+
+int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
+             size_t workspace_bytes, const t3_outputs* out, void* stream) {
+  if (!scene || !depth_id || !out || !out->rgb || !workspace) return T3_EINVAL;
+  if (workspace_bytes < ws_scene_end()) return T3_EINVAL;
+  static thread_local DevScene ds;
+  int r = make_dev_scene(*scene, ds);
+  if (r) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
+  DevScene* dsc = reinterpret_cast<DevScene*>(ws + T3_WS_SCENE);
+  cudaError_t e = launch_upload_scene(ds, dsc, reinterpret_cast<uint32_t*>(ws), 0, st);
+  if (e != cudaSuccess) return T3_ECUDA;
+  return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
+                              *out, st));
+}
+
+int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
+              size_t workspace_bytes, int32_t* status, const t3_outputs* out, void* stream) {
+  return t3_render_staged(scene, mode, tile, bin_capacity, workspace, workspace_bytes, status, out,
+                          stream, nullptr);
+}
+
+int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
+                     void* workspace, size_t workspace_bytes, int32_t* status,
+                     const t3_outputs* out, void* stream, void* const* stage_events) {
+  (void)tile;
+  (void)bin_capacity;
+  if (!scene || !workspace || !status || !out || !out->rgb) return T3_EINVAL;
+  if (mode != T3_RASTER_DIRECT) return T3_EUNSUPPORTED;
+  static thread_local DevScene ds;
+  int r = make_dev_scene(*scene, ds);
+  if (r) return r;
+  const Layout L = layout_for(*scene);
+  if (workspace_bytes < L.end) return T3_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
+  uint32_t* counters = reinterpret_cast<uint32_t*>(ws + L.counters);
+  DevScene* dsc = reinterpret_cast<DevScene*>(ws + L.scene);
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
+  const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
+  auto mark = [&](int k) -> cudaError_t {
+    if (!stage_events || !stage_events[k]) return cudaSuccess;
+    return cudaEventRecord((cudaEvent_t)stage_events[k], st);
+  };
+  cudaError_t e = mark(0);
+  if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, 64, st);
+  if (e == cudaSuccess) e = launch_clear(keys, npix, st);
+  if (e == cudaSuccess) e = mark(1);
+  for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
+    BigQueue big;
+    big.items = reinterpret_cast<uint32_t*>(ws + L.big_items);
+    big.capacity = L.big_capacity;
+    big.count = counters + o;
+    big.status = status;
+    e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 128, st);
+  }
+  if (e == cudaSuccess) e = mark(2);
+  if (e == cudaSuccess) e = launch_shade(dsc, scene->frame, keys, *out, st);
+  if (e == cudaSuccess) e = mark(3);
+  return cuda_rc(e);
+}
+
+int t3_event_create(void** event) {
+  if (!event) return T3_EINVAL;
+  cudaEvent_t ev;
+  if (cudaEventCreate(&ev) != cudaSuccess) return T3_ECUDA;
+  *event = (void*)ev;
+  return T3_OK;
+}
+
+int t3_event_destroy(void* event) {
+  if (!event) return T3_EINVAL;
+  return cuda_rc(cudaEventDestroy((cudaEvent_t)event));
+}
+
+int t3_event_elapsed_ms(void* start, void* end, float* ms) {
+  if (!start || !end || !ms) return T3_EINVAL;
+  if (cudaEventSynchronize((cudaEvent_t)end) != cudaSuccess) return T3_ECUDA;
+  return cuda_rc(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)end));
+}
+
+int t3_read_status(const int32_t* status, int32_t* host_status, void* stream) {
+  if (!status || !host_status) return T3_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(host_status, status, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return cuda_rc(e);
+}
+
+} // extern "C"

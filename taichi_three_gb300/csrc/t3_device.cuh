@@ -1,0 +1,265 @@
+// t3_device.cuh -- device-side building blocks shared by the raster and shade
+// kernels: exact-order FP32 arithmetic, the mesh protocol, per-face setup and
+// barycentric weights.
+//
+// Bit-exactness contract: face setup, weights and depth are evaluated with the
+// round-to-nearest intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn ...), which the
+// compiler never contracts into FMA, in the operation order of Tina's Taichi
+// source (tina/core/triangle.py:93-122, tina/common.py:170-184).  The triangle
+// id and depth buffers are therefore bit-identical to a serial FP32 evaluation
+// of that source.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/tina3.h"
+
+namespace t3 {
+
+#define T3_MAX_LOBES 4
+#define T3_MAX_FACTORS 4
+#define T3_EMPTY_KEY 0xFFFFFFFFFFFFFFFFull
+
+// ---- exact-order arithmetic -------------------------------------------------
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+struct f2 { float x, y; };
+struct f3 { float x, y, z; };
+
+__device__ __forceinline__ f3 mk3(float a, float b, float c) { return f3{a, b, c}; }
+
+// float -> int32 truncation; out-of-range saturates, NaN -> INT32_MIN
+__device__ __forceinline__ int32_t trunc_i32(float x) {
+  if (!(x >= -2147483648.0f)) return INT32_MIN;
+  if (x >= 2147483648.0f) return INT32_MAX;
+  return (int32_t)x;
+}
+
+// mapply (tina/common.py:170-177), exact order
+__device__ __forceinline__ void mapply_x(const float* m, f3 p, float wei, f3& r, float& w) {
+  float r0 = xmul(m[3], wei), r1 = xmul(m[7], wei), r2 = xmul(m[11], wei);
+  r0 = xadd(r0, xmul(m[0], p.x)); r0 = xadd(r0, xmul(m[1], p.y)); r0 = xadd(r0, xmul(m[2], p.z));
+  r1 = xadd(r1, xmul(m[4], p.x)); r1 = xadd(r1, xmul(m[5], p.y)); r1 = xadd(r1, xmul(m[6], p.z));
+  r2 = xadd(r2, xmul(m[8], p.x)); r2 = xadd(r2, xmul(m[9], p.y)); r2 = xadd(r2, xmul(m[10], p.z));
+  float ww = xmul(m[15], wei);
+  ww = xadd(ww, xmul(m[12], p.x)); ww = xadd(ww, xmul(m[13], p.y)); ww = xadd(ww, xmul(m[14], p.z));
+  r = f3{r0, r1, r2};
+  w = ww;
+}
+__device__ __forceinline__ f3 mapply_pos_x(const float* m, f3 p) {
+  f3 r; float w;
+  mapply_x(m, p, 1.0f, r, w);
+  return f3{xdiv(r.x, w), xdiv(r.y, w), xdiv(r.z, w)};
+}
+// 3x3 @ v (Taichi Matrix.__matmul__ order)
+__device__ __forceinline__ f3 matvec3_x(const float* m, f3 v) {
+  float a0 = xmul(m[0], v.x); a0 = xadd(a0, xmul(m[1], v.y)); a0 = xadd(a0, xmul(m[2], v.z));
+  float a1 = xmul(m[3], v.x); a1 = xadd(a1, xmul(m[4], v.y)); a1 = xadd(a1, xmul(m[5], v.z));
+  float a2 = xmul(m[6], v.x); a2 = xadd(a2, xmul(m[7], v.y)); a2 = xadd(a2, xmul(m[8], v.z));
+  return f3{a0, a1, a2};
+}
+__device__ __forceinline__ f3 sub_x(f3 a, f3 b) { return f3{xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)}; }
+__device__ __forceinline__ f3 cross_x(f3 a, f3 b) {
+  return f3{xsub(xmul(a.y, b.z), xmul(a.z, b.y)), xsub(xmul(a.z, b.x), xmul(a.x, b.z)),
+            xsub(xmul(a.x, b.y), xmul(a.y, b.x))};
+}
+__device__ __forceinline__ float dot_x(f3 a, f3 b) {
+  return xadd(xadd(xmul(a.x, b.x), xmul(a.y, b.y)), xmul(a.z, b.z));
+}
+__device__ __forceinline__ f3 normalized_x(f3 a) {
+  float inv = xdiv(1.0f, __fsqrt_rn(dot_x(a, a)));
+  return f3{xmul(inv, a.x), xmul(inv, a.y), xmul(inv, a.z)};
+}
+__device__ __forceinline__ float cross2_x(float ax, float ay, float bx, float by) {
+  return xsub(xmul(ax, by), xmul(ay, bx));
+}
+
+__device__ __forceinline__ f3 ld3(const float* p) { return f3{__ldg(p), __ldg(p + 1), __ldg(p + 2)}; }
+
+// ---- mesh protocol -----------------------------------------------------------
+// Mesh-edit flags apply in the fixed nesting
+//   MeshNoCulling(MeshFlipNormal(MeshFlipCulling(MeshFlatNormal(MeshTransform(base)))))
+
+// pointer to attribute `attr` (0 vert, 1 norm, 2 coor) of corner k of base face f
+__device__ __forceinline__ const float* base_ptr(const t3_mesh& d, int64_t f, int k, int attr) {
+  const float* arr = attr == 0 ? d.verts : attr == 1 ? d.norms : d.coors;
+  const int width = attr == 2 ? 2 : 3;
+  if (d.kind == T3_MESH_SOUP) {
+    return arr + (f * 3 + k) * width;
+  } else if (d.kind == T3_MESH_GRID) {
+    // MeshGrid._get_face_props (tina/mesh/grid.py:46-58); square grids
+    const uint32_t stride = (uint32_t)d.grid_nx - 1u;
+    const uint32_t m = (uint32_t)(f >> 1);
+    const uint32_t i = m / stride, j = m - i * stride;
+    // corners a=(i,j) b=(i+1,j) c=(i+1,j+1) d=(i,j+1); odd faces take (a, c, d)
+    int c = k;
+    if (f & 1) c = k == 0 ? 0 : k + 1;
+    const uint32_t ii = i + (c == 1 || c == 2 ? 1u : 0u);
+    const uint32_t jj = j + (c >= 2 ? 1u : 0u);
+    return arr + ((int64_t)ii * d.grid_ny + jj) * width;
+  } else {
+    const int slot = attr == 0 ? d.slot_vert : attr == 1 ? d.slot_norm : d.slot_coor;
+    const int32_t idx = __ldg(d.faces + f * d.face_stride + k * d.corner_stride + slot);
+    return arr + (int64_t)idx * width;
+  }
+}
+
+struct FaceRef {
+  int64_t f;   // base face
+  bool flip;   // corner order reversed
+  bool negate; // normals negated
+};
+
+__device__ __forceinline__ FaceRef face_ref(const t3_mesh& d, int64_t n) {
+  FaceRef r{n, (d.flags & T3_MESH_FLIP_ORDER) != 0, (d.flags & T3_MESH_FLIP_NORMAL) != 0};
+  if (d.flags & T3_MESH_NOCULL) {
+    r.f = n >> 1;
+    if (n & 1) { r.flip = !r.flip; r.negate = !r.negate; }
+  }
+  return r;
+}
+
+__device__ __forceinline__ void base_verts(const t3_mesh& d, int64_t f, f3 v[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    v[k] = ld3(base_ptr(d, f, k, 0));
+    if (d.flags & T3_MESH_TRANSFORM) v[k] = mapply_pos_x(d.trans, v[k]);
+  }
+}
+
+__device__ __forceinline__ void face_verts(const t3_mesh& d, const FaceRef& r, f3 v[3]) {
+  f3 t[3];
+  base_verts(d, r.f, t);
+  v[0] = r.flip ? t[2] : t[0];
+  v[1] = t[1];
+  v[2] = r.flip ? t[0] : t[2];
+}
+
+__device__ __forceinline__ void face_norms(const t3_mesh& d, const FaceRef& r, f3 v[3]) {
+  f3 t[3];
+  if (d.flags & T3_MESH_FLAT_NORMAL) {
+    f3 p[3];
+    base_verts(d, r.f, p);
+    f3 nn = normalized_x(cross_x(sub_x(p[1], p[0]), sub_x(p[2], p[0])));
+    t[0] = t[1] = t[2] = nn;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      t[k] = ld3(base_ptr(d, r.f, k, 1));
+      if (d.flags & T3_MESH_TRANSFORM) t[k] = matvec3_x(d.trans_normal, t[k]);
+    }
+  }
+  v[0] = r.flip ? t[2] : t[0];
+  v[1] = t[1];
+  v[2] = r.flip ? t[0] : t[2];
+  if (r.negate) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) v[k] = f3{-v[k].x, -v[k].y, -v[k].z};
+  }
+}
+
+__device__ __forceinline__ void face_coors(const t3_mesh& d, const FaceRef& r, f2 v[3]) {
+  f2 t[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float* p = base_ptr(d, r.f, k, 2);
+    t[k] = f2{__ldg(p), __ldg(p + 1)};
+  }
+  v[0] = r.flip ? t[2] : t[0];
+  v[1] = t[1];
+  v[2] = r.flip ? t[0] : t[2];
+}
+
+// ---- per-face setup (triangle.py:93-113) -------------------------------------
+struct Setup {
+  float Az, Bz, Cz;       // NDC depth of the corners
+  float bx, by, cx, cy;   // viewport corners b, c
+  float bcnx, bcny, canx, cany;
+  float wsa, wsb, wsc;    // 1 / clip w
+  int32_t botx, boty, topx, topy;
+};
+
+__device__ __forceinline__ bool inside_clip(f3 p) {
+  return (-1.0f <= p.x && p.x <= 1.0f) && (-1.0f <= p.y && p.y <= 1.0f) &&
+         (-1.0f <= p.z && p.z <= 1.0f);
+}
+
+// returns false when the face is culled or clipped
+__device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Setup& s) {
+  const float* W2V = fr.W2V;
+  f3 r; float wa, wb, wc;
+  mapply_x(W2V, v[0], 1.0f, r, wa);
+  const f3 Av = f3{xdiv(r.x, wa), xdiv(r.y, wa), xdiv(r.z, wa)};
+  mapply_x(W2V, v[1], 1.0f, r, wb);
+  const f3 Bv = f3{xdiv(r.x, wb), xdiv(r.y, wb), xdiv(r.z, wb)};
+  mapply_x(W2V, v[2], 1.0f, r, wc);
+  const f3 Cv = f3{xdiv(r.x, wc), xdiv(r.y, wc), xdiv(r.z, wc)};
+  const float facing = cross2_x(xsub(Bv.x, Av.x), xsub(Bv.y, Av.y), xsub(Cv.x, Av.x), xsub(Cv.y, Av.y));
+  if (facing <= 0.0f && (fr.flags & T3_CULLING)) return false;
+  if (fr.flags & T3_CLIPPING) {
+    if (!inside_clip(Av) && !inside_clip(Bv) && !inside_clip(Cv)) return false;
+  }
+  const float W = (float)fr.width, H = (float)fr.height;
+  const float ax = xmul(xadd(xmul(Av.x, 0.5f), 0.5f), W), ay = xmul(xadd(xmul(Av.y, 0.5f), 0.5f), H);
+  const float bx = xmul(xadd(xmul(Bv.x, 0.5f), 0.5f), W), by = xmul(xadd(xmul(Bv.y, 0.5f), 0.5f), H);
+  const float cx = xmul(xadd(xmul(Cv.x, 0.5f), 0.5f), W), cy = xmul(xadd(xmul(Cv.y, 0.5f), 0.5f), H);
+  const int32_t lox = trunc_i32(floorf(fminf(fminf(ax, bx), cx)));
+  const int32_t loy = trunc_i32(floorf(fminf(fminf(ay, by), cy)));
+  const int32_t hix = trunc_i32(ceilf(fmaxf(fmaxf(ax, bx), cx)));
+  const int32_t hiy = trunc_i32(ceilf(fmaxf(fmaxf(ay, by), cy)));
+  s.botx = lox > 0 ? lox : 0;
+  s.boty = loy > 0 ? loy : 0;
+  s.topx = hix < fr.width - 1 ? hix : fr.width - 1;
+  s.topy = hiy < fr.height - 1 ? hiy : fr.height - 1;
+  const float n = cross2_x(xsub(bx, ax), xsub(by, ay), xsub(cx, ax), xsub(cy, ay));
+  s.bcnx = xdiv(xsub(bx, cx), n);
+  s.bcny = xdiv(xsub(by, cy), n);
+  s.canx = xdiv(xsub(cx, ax), n);
+  s.cany = xdiv(xsub(cy, ay), n);
+  s.bx = bx; s.by = by; s.cx = cx; s.cy = cy;
+  s.wsa = xdiv(1.0f, wa);
+  s.wsb = xdiv(1.0f, wb);
+  s.wsc = xdiv(1.0f, wc);
+  s.Az = Av.z; s.Bz = Bv.z; s.Cz = Cv.z;
+  return true;
+}
+
+// Unnormalised weights at pixel centre (px, py) and their sum (triangle.py:115-119).
+__device__ __forceinline__ void face_raw_weights(const Setup& s, float px, float py, float& wx,
+                                                 float& wy, float& wz, float& sum) {
+  const float w_bc = cross2_x(xsub(px, s.bx), xsub(py, s.by), s.bcnx, s.bcny);
+  const float w_ca = cross2_x(xsub(px, s.cx), xsub(py, s.cy), s.canx, s.cany);
+  wx = xmul(w_bc, s.wsa);
+  wy = xmul(w_ca, s.wsb);
+  wz = xmul(xsub(xsub(1.0f, w_bc), w_ca), s.wsc);
+  sum = xadd(xadd(wx, wy), wz);
+}
+
+// Exact `all(wei / sum >= 0)`.  For 0 < sum < 1 a negative finite weight stays
+// negative after the division (|w| / sum > |w| >= 2^-149 never rounds to -0), so
+// those pixels are rejected without dividing; every other case divides.
+__device__ __forceinline__ bool face_inside(float wx, float wy, float wz, float sum, f3& wei) {
+  if (sum > 0.0f && sum < 1.0f && (wx < 0.0f || wy < 0.0f || wz < 0.0f)) return false;
+  wei = f3{xdiv(wx, sum), xdiv(wy, sum), xdiv(wz, sum)};
+  return wei.x >= 0.0f && wei.y >= 0.0f && wei.z >= 0.0f;
+}
+
+__device__ __forceinline__ f3 face_weights(const Setup& s, float px, float py) {
+  float wx, wy, wz, sum;
+  face_raw_weights(s, px, py, wx, wy, wz, sum);
+  return f3{xdiv(wx, sum), xdiv(wy, sum), xdiv(wz, sum)};
+}
+
+__device__ __forceinline__ float face_depth(const Setup& s, f3 wei) {
+  return xadd(xadd(xmul(wei.x, s.Az), xmul(wei.y, s.Bz)), xmul(wei.z, s.Cz));
+}
+
+__device__ __forceinline__ uint64_t pack_key(int32_t depth, uint32_t id) {
+  return ((uint64_t)((uint32_t)depth ^ 0x80000000u) << 32) | (uint64_t)id;
+}
+
+} // namespace t3

@@ -1,0 +1,76 @@
+// t3_internal.cuh -- library-internal types shared by the kernels and the C ABI
+// host code: the device copy of a scene (with materials flattened into lobes),
+// the workspace layout, status bits and the launchers.
+#pragma once
+
+#include "t3_device.cuh"
+
+namespace t3 {
+
+// device status word bits (OR-ed by kernels, read by t3_read_status)
+#define T3_STATUS_BIG_OVERFLOW 1
+#define T3_STATUS_BIN_OVERFLOW 2
+#define T3_STATUS_TIMEOUT 4
+
+// Large-face queue of the direct rasteriser.
+struct BigQueue {
+  uint32_t* items;
+  uint32_t capacity;
+  uint32_t* count;
+  int32_t* status;
+};
+
+// A material tree flattened into a sum of weighted leaf lobes:
+//   brdf = sum_k W_k * leaf_k.brdf,  ambient = sum_k W_k * leaf_k.ambient, ...
+// W_k is a product of factor nodes along the path from the root (Mix contributes
+// (1 - factor) to its first child and factor to its second, Scale its factor).
+// fac[j] = node index | T3_FAC_ONE_MINUS.
+#define T3_FAC_ONE_MINUS 0x10000
+struct DevLobe {
+  int32_t kind;    // T3_OP_LAMBERT / PHONG / COOK / EMISSION
+  int32_t nfac;
+  int32_t p0, p1;  // PHONG: shineness node; COOK: roughness, fresnel nodes
+  int32_t int_pow; // PHONG: integer exponent (>0) when shineness is a Python int
+  int32_t fac[T3_MAX_FACTORS];
+  int32_t _pad[3];
+};
+
+struct DevMaterial {
+  int32_t nnodes, nlobes;
+  int32_t _pad[2];
+  t3_node nodes[T3_MAX_NODES];
+  DevLobe lobes[T3_MAX_LOBES];
+};
+
+struct DevObject {
+  t3_mesh mesh;
+  DevMaterial mat;
+  int64_t face_base, nfaces;
+};
+
+struct DevScene {
+  t3_frame frame;
+  t3_lighting lighting;
+  int32_t nobjects;
+  int32_t _pad;
+  DevObject obj[T3_MAX_OBJECTS];
+};
+
+// workspace layout (byte offsets, 256-aligned)
+#define T3_WS_COUNTERS 0        // uint32[64]: per-object big-queue counts, misc
+#define T3_WS_SCENE 256         // DevScene
+size_t ws_scene_end();
+size_t ws_big_items();          // offset of the big-face queue
+
+int flatten_material(const t3_material& in, DevMaterial& out);
+int make_dev_scene(const t3_scene& sc, DevScene& out);
+
+cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st);
+cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
+                                int ncounters, cudaStream_t st);
+cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
+                                 const BigQueue& big, int32_t big_threshold, cudaStream_t st);
+cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
+                         const t3_outputs& out, cudaStream_t st);
+
+} // namespace t3

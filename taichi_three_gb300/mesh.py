@@ -1,0 +1,405 @@
+"""Mesh nodes: the mesh protocol of Tina's tina/mesh package.
+
+Every mesh fills a t3_mesh descriptor (`_t3_fill`) that the CUDA kernels read
+through the same getters the reference calls per face (get_face_verts /
+get_face_norms / get_face_coors).  Mesh-edit nodes become descriptor flags and
+apply in one fixed nesting,
+    MeshNoCulling(MeshFlipNormal(MeshFlipCulling(MeshFlatNormal(MeshTransform(base))))),
+any sub-sequence of which may be used; other nestings raise NotImplementedError.
+"""
+import numpy as np
+import torch
+
+from . import _native as N
+from ._device import as_f32, as_i32, default_device, ptr
+
+MAX = 2**20  # tina/common.py:7
+
+
+class MeshBase:
+    face_attr = None
+
+    def get_npolygon(self):
+        return 3
+
+    def pre_compute(self):
+        pass
+
+    def set_face_attrs(self, attrs):
+        """Extension: per-face material attributes [nfaces, C] read by FaceAttr."""
+        a = as_f32(attrs)
+        if a.dim() == 1:
+            a = a[:, None]
+        self.face_attr = a.contiguous()
+
+    def _fill_attr(self, m, device, keep):
+        if self.face_attr is not None:
+            m.face_attr = ptr(self.face_attr, device, keep)
+            m.attr_stride = int(self.face_attr.shape[1])
+
+    def attr_stride(self):
+        return 0 if self.face_attr is None else int(self.face_attr.shape[1])
+
+
+class SimpleMesh(MeshBase):
+    """A face soup (tina/mesh/simple.py): verts [n, 3, 3], norms [n, 3, 3],
+    coors [n, 3, 2]; nfaces = min(n, maxfaces)."""
+
+    def __init__(self, maxfaces=MAX, npolygon=3):
+        if npolygon != 3:
+            raise NotImplementedError('only triangle meshes (npolygon=3) are rasterised by this build')
+        self.maxfaces = maxfaces
+        self.npolygon = npolygon
+        self.nfaces = 0
+        dev = default_device()
+        self.verts = torch.zeros((0, 3, 3), dtype=torch.float32, device=dev)
+        self.norms = None
+        self.coors = None
+
+    def get_nfaces(self):
+        return min(self.nfaces, self.maxfaces)
+
+    def set_face_verts(self, verts):
+        v = as_f32(verts)
+        if v.dim() != 3 or v.shape[1] != 3 or v.shape[2] != 3:
+            raise ValueError('verts must have shape [nfaces, 3, 3]')
+        self.nfaces = min(v.shape[0], self.maxfaces)
+        self.verts = v[:self.nfaces].contiguous()
+
+    def set_face_norms(self, norms):
+        n = as_f32(norms)
+        if n.dim() != 3 or n.shape[0] < self.nfaces or n.shape[1:] != (3, 3):
+            raise ValueError('norms must have shape [>= nfaces, 3, 3]')
+        self.norms = n[:self.nfaces].contiguous()
+
+    def set_face_coors(self, coors):
+        c = as_f32(coors)
+        if c.dim() != 3 or c.shape[0] < self.nfaces or c.shape[1] != 3 or c.shape[2] < 2:
+            raise ValueError('coors must have shape [>= nfaces, 3, 2]')
+        self.coors = c[:self.nfaces, :, :2].contiguous()
+
+    def _t3_fill(self, m, device, keep):
+        m.kind = N.T3_MESH_SOUP
+        m.nfaces = self.get_nfaces()
+        m.verts = ptr(self.verts, device, keep)
+        m.norms = ptr(self.norms, device, keep)
+        m.coors = ptr(self.coors, device, keep)
+        self._fill_attr(m, device, keep)
+
+
+class PrimitiveMesh(SimpleMesh):
+    """SimpleMesh built from [n, 3, 3(vert, norm, coor), 3] faces
+    (tina/mesh/prim.py:6-26)."""
+
+    def __init__(self, faces):
+        faces = np.asarray(faces, dtype=np.float32)
+        super().__init__(maxfaces=len(faces), npolygon=faces.shape[1])
+        self.set_face_verts(faces[:, :, 0])
+        self.set_face_norms(faces[:, :, 1])
+        self.set_face_coors(faces[:, :, 2, :2])
+
+    @classmethod
+    def sphere(cls, lons=32, lats=24, rad=1):
+        """UV sphere (tina/mesh/prim.py:22-48): the pole rows drop one triangle
+        per quad, so lons=64, lats=32 gives 3,968 faces."""
+        def at(lat, lon):
+            lat /= lats
+            lon /= lons
+            coor = lon, lat, 0
+            lat = (lat - 0.5) * np.pi
+            lon = (lon * 2 - 1) * np.pi
+            x = np.cos(lat) * np.cos(lon)
+            y = np.cos(lat) * np.sin(lon)
+            z = np.sin(lat)
+            norm = x, y, z
+            vert = x * rad, y * rad, z * rad
+            return vert, norm, coor
+
+        faces = []
+        for lat in range(lats):
+            for lon in range(lons):
+                v1 = at(lat, lon)
+                v2 = at(lat, lon + 1)
+                v3 = at(lat + 1, lon + 1)
+                v4 = at(lat + 1, lon)
+                if lat != 0:
+                    faces.append([v1, v2, v3])
+                if lat != lats - 1:
+                    faces.append([v3, v4, v1])
+        return cls(faces)
+
+    @classmethod
+    def cylinder(cls, lons=32, lats=4, rad=1, hei=2):
+        """(tina/mesh/prim.py:50-88)"""
+        def at(lat, lon, rad=rad):
+            lat /= lats
+            lon /= lons
+            coor = lon, lat, 0
+            lat = lat - 0.5
+            lon = (lon * 2 - 1) * np.pi
+            x = np.cos(lon)
+            y = np.sin(lon)
+            z = lat
+            return (x * rad, y * rad, z * hei), (x, y, 0), coor
+
+        faces = []
+        for lat in range(lats):
+            for lon in range(lons):
+                v1, v2, v3, v4 = at(lat, lon), at(lat, lon + 1), at(lat + 1, lon + 1), at(lat + 1, lon)
+                faces.append([v1, v2, v3])
+                faces.append([v3, v4, v1])
+        for lon in range(lons):
+            norm, coor = (0, 0, -1), (0, 0, -1)
+            faces.append([(at(0, lon + 1)[0], norm, coor), (at(0, lon)[0], norm, coor),
+                          ((0, 0, -hei / 2), norm, coor)])
+        for lon in range(lons):
+            norm, coor = (0, 0, 1), (0, 0, 1)
+            faces.append([((0, 0, hei / 2), norm, coor), (at(lats, lon)[0], norm, coor),
+                          (at(lats, lon + 1)[0], norm, coor)])
+        return cls(faces)
+
+
+class MeshGrid(MeshBase):
+    """Parametric grid (tina/mesh/grid.py): pos/nrm/tex [n, n, 3|2]; two
+    triangles per quad; `pre_compute` (run by every render) recomputes the
+    smooth normals on the device."""
+
+    def __init__(self, res, as_quad=False):
+        if as_quad:
+            raise NotImplementedError('quad grids are not rasterised by this build')
+        if isinstance(res, int):
+            res = res, res
+        if res[0] != res[1]:
+            raise NotImplementedError("MeshGrid's face indexing (grid.py:46-58) covers square grids only")
+        self.res = tuple(int(r) for r in res)
+        dev = default_device()
+        nx, ny = self.res
+        # init_pos (tina/mesh/grid.py:15-20)
+        I = torch.stack(torch.meshgrid(torch.arange(nx, dtype=torch.float32),
+                                       torch.arange(ny, dtype=torch.float32), indexing='ij'), -1)
+        uv = I / torch.tensor([nx - 1, ny - 1], dtype=torch.float32)
+        self.tex = uv.to(dev).contiguous()
+        pos = torch.zeros((nx, ny, 3), dtype=torch.float32)
+        pos[..., 0] = uv[..., 0] * 2 - 1
+        pos[..., 1] = uv[..., 1] * 2 - 1
+        self.pos = pos.to(dev).contiguous()
+        self.nrm = torch.zeros((nx, ny, 3), dtype=torch.float32, device=dev)
+        self.auto_normals = True
+
+    def get_nfaces(self):
+        return (self.res[0] - 1) * (self.res[1] - 1) * 2
+
+    def pre_compute(self):
+        if not self.auto_normals:
+            return
+        if self.pos.is_cuda:
+            lib = N.load()
+            stream = torch.cuda.current_stream(self.pos.device).cuda_stream
+            N.check(lib.t3_grid_normals(self.pos.data_ptr(), self.nrm.data_ptr(), self.res[0],
+                                        self.res[1], stream), 't3_grid_normals')
+
+    def _t3_fill(self, m, device, keep):
+        m.kind = N.T3_MESH_GRID
+        m.nfaces = self.get_nfaces()
+        m.verts = ptr(self.pos, device, keep)
+        m.norms = ptr(self.nrm, device, keep)
+        m.coors = ptr(self.tex, device, keep)
+        m.grid_nx, m.grid_ny = self.res
+        self._fill_attr(m, device, keep)
+
+
+class ConnectiveMesh(MeshBase):
+    """Indexed mesh with shared vertex attributes (tina/mesh/conn.py)."""
+
+    def __init__(self, maxfaces=MAX, maxverts=MAX, npolygon=3):
+        if npolygon != 3:
+            raise NotImplementedError('only triangle meshes are rasterised by this build')
+        self.maxfaces, self.maxverts, self.npolygon = maxfaces, maxverts, npolygon
+        dev = default_device()
+        self.faces = torch.zeros((0, 3), dtype=torch.int32, device=dev)
+        self.verts = torch.zeros((0, 3), dtype=torch.float32, device=dev)
+        self.norms = None
+        self.coors = None
+        self.nfaces = 0
+
+    def get_max_vert_nindex(self):
+        return self.maxverts
+
+    def get_nfaces(self):
+        return self.nfaces
+
+    def set_vertices(self, verts):
+        self.verts = as_f32(verts)[:self.maxverts].contiguous()
+
+    def set_vert_norms(self, norms):
+        self.norms = as_f32(norms)[:self.maxverts].contiguous()
+
+    def set_vert_coors(self, coors):
+        self.coors = as_f32(coors)[:self.maxverts, :2].contiguous()
+
+    def set_faces(self, faces):
+        f = as_i32(faces)
+        if f.dim() != 2 or f.shape[1] != 3:
+            raise ValueError('faces must have shape [nfaces, 3]')
+        self.nfaces = min(f.shape[0], self.maxfaces)
+        self.faces = f[:self.nfaces].contiguous()
+
+    def _check_indices(self):
+        if self.nfaces == 0:
+            return
+        lo, hi = int(self.faces.min()), int(self.faces.max())
+        for name, arr in (('verts', self.verts), ('norms', self.norms), ('coors', self.coors)):
+            if arr is not None and (lo < 0 or hi >= arr.shape[0]):
+                raise ValueError(f'face indices [{lo}, {hi}] out of range for {name} ({arr.shape[0]})')
+
+    def _t3_fill(self, m, device, keep):
+        self._check_indices()
+        m.kind = N.T3_MESH_INDEXED
+        m.nfaces = self.nfaces
+        m.verts = ptr(self.verts, device, keep)
+        m.norms = ptr(self.norms, device, keep)
+        m.coors = ptr(self.coors, device, keep)
+        m.faces = ptr(self.faces, device, keep)
+        m.face_stride, m.corner_stride = 3, 1
+        m.slot_vert = m.slot_coor = m.slot_norm = 0
+        self._fill_attr(m, device, keep)
+
+
+class MeshModel(MeshBase):
+    """Indexed mesh with per-corner (v, vt, vn) indices (tina/mesh/model.py);
+    `obj` is a dict with 'v' [nv,3], 'vt' [nt,2], 'vn' [nn,3], 'f' [n,3,3] or [n,3]."""
+
+    def __init__(self, obj):
+        if isinstance(obj, str):
+            from .assimp import readobj
+            obj = readobj(obj)
+        f = np.asarray(obj['f'])
+        if f.ndim == 2:
+            f = np.stack([f, f, f], axis=2)
+        self.faces = as_i32(f.reshape(len(f), 9))
+        self.verts = as_f32(obj['v'])
+        self.coors = as_f32(np.asarray(obj['vt'])[:, :2]) if len(obj.get('vt', [])) else None
+        self.norms = as_f32(obj['vn']) if len(obj.get('vn', [])) else None
+        self.nfaces = len(f)
+
+    def get_nfaces(self):
+        return self.nfaces
+
+    def get_max_vert_nindex(self):
+        return int(self.verts.shape[0])
+
+    def _check_indices(self):
+        if self.nfaces == 0:
+            return
+        f = self.faces.view(-1, 3, 3)
+        for slot, arr, name in ((0, self.verts, 'v'), (1, self.coors, 'vt'), (2, self.norms, 'vn')):
+            if arr is None:
+                continue
+            lo, hi = int(f[:, :, slot].min()), int(f[:, :, slot].max())
+            if lo < 0 or hi >= arr.shape[0]:
+                raise ValueError(f'{name} indices [{lo}, {hi}] out of range ({arr.shape[0]})')
+
+    def _t3_fill(self, m, device, keep):
+        self._check_indices()
+        m.kind = N.T3_MESH_INDEXED
+        m.nfaces = self.nfaces
+        m.verts = ptr(self.verts, device, keep)
+        m.norms = ptr(self.norms, device, keep)
+        m.coors = ptr(self.coors, device, keep)
+        m.faces = ptr(self.faces, device, keep)
+        m.face_stride, m.corner_stride = 9, 3
+        m.slot_vert, m.slot_coor, m.slot_norm = 0, 1, 2
+        self._fill_attr(m, device, keep)
+
+
+class MeshEditBase:
+    """Wraps a mesh and forwards every other attribute (tina/mesh/base.py)."""
+    _flag = 0
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+
+    def __getattr__(self, attr):
+        return getattr(self.mesh, attr)
+
+    def get_nfaces(self):
+        return self.mesh.get_nfaces()
+
+    def pre_compute(self):
+        self.mesh.pre_compute()
+
+    def _check_inner(self, m, forbidden):
+        if m.flags & forbidden:
+            raise NotImplementedError(
+                f'{type(self).__name__} around this mesh-edit chain is not supported; nest edits as '
+                'MeshNoCulling(MeshFlipNormal(MeshFlipCulling(MeshFlatNormal(MeshTransform(mesh)))))')
+
+
+class MeshTransform(MeshEditBase):
+    """4x4 transform of the vertices and transpose(inv(trans))[:3, :3] of the
+    normals (tina/mesh/trans.py:5-40)."""
+
+    def __init__(self, mesh, trans=None):
+        super().__init__(mesh)
+        self.trans = np.eye(4, dtype=np.float32)
+        self.trans_normal = np.eye(3, dtype=np.float32)
+        if trans is not None:
+            self.set_transform(trans)
+
+    def set_transform(self, trans):
+        trans = np.asarray(trans, dtype=np.float64)
+        trans_normal = np.transpose(np.linalg.inv(trans))
+        self.trans = np.array(trans, dtype=np.float32)
+        self.trans_normal = np.array(trans_normal[:3, :3], dtype=np.float32)
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        self._check_inner(m, 0xFF)
+        m.flags |= N.T3_MESH_TRANSFORM
+        t = self.trans.reshape(-1)
+        tn = self.trans_normal.reshape(-1)
+        for k in range(16):
+            m.trans[k] = float(t[k])
+        for k in range(9):
+            m.trans_normal[k] = float(tn[k])
+
+
+class MeshFlatNormal(MeshEditBase):
+    """normals = normalize(cross(b - a, c - a)) per face (tina/mesh/norm.py:5-14)."""
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        self._check_inner(m, N.T3_MESH_FLAT_NORMAL | N.T3_MESH_FLIP_ORDER | N.T3_MESH_FLIP_NORMAL
+                          | N.T3_MESH_NOCULL)
+        m.flags |= N.T3_MESH_FLAT_NORMAL
+
+
+class MeshFlipCulling(MeshEditBase):
+    """Reversed corner order (tina/mesh/cull.py:5-28)."""
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        self._check_inner(m, N.T3_MESH_FLIP_NORMAL | N.T3_MESH_NOCULL)
+        m.flags ^= N.T3_MESH_FLIP_ORDER
+
+
+class MeshFlipNormal(MeshEditBase):
+    """Negated normals (tina/mesh/cull.py:61-66)."""
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        self._check_inner(m, N.T3_MESH_NOCULL)
+        m.flags ^= N.T3_MESH_FLIP_NORMAL
+
+
+class MeshNoCulling(MeshEditBase):
+    """Every face twice, odd copies flipped with negated normals
+    (tina/mesh/cull.py:31-58)."""
+
+    def get_nfaces(self):
+        return self.mesh.get_nfaces() * 2
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        self._check_inner(m, N.T3_MESH_NOCULL)
+        m.flags |= N.T3_MESH_NOCULL

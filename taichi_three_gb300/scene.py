@@ -1,0 +1,301 @@
+"""Scene and TriangleRaster: Tina's top-level API (tina/scene/raster.py,
+tina/core/triangle.py) over the CUDA library.
+
+`Scene.render()` issues one t3_render call per frame: scene upload, depth-key
+clear, the rasteriser over every object, then deferred shading with the ACES
+epilogue.  All buffers are torch tensors on the CUDA device; `scene.img` is a
+float32 tensor of shape (W, H, 3) indexed [x, y] like Tina's Taichi field.
+"""
+import ctypes as C
+
+import torch
+
+from . import _native as N
+from ._device import default_device, require_cuda
+from .engine import Engine
+from .lighting import Lighting
+from .materials import Diffuse, compile_material
+
+_UNSUPPORTED_OPTIONS = ('taa', 'ssr', 'ssao', 'fxaa', 'blooming')
+RASTER_MODES = {'direct': N.T3_RASTER_DIRECT, 'binned': N.T3_RASTER_BINNED}
+
+
+class _Obj:
+    def __init__(self, material, raster):
+        self.material = material
+        self.raster = raster
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+class TriangleRaster:
+    """The rasteriser protocol set_object / render_occup / render_color
+    (tina/core/triangle.py:5-153).  Options: maxfaces, smoothing, texturing,
+    culling (default True), clipping (default True)."""
+
+    def __init__(self, engine, maxfaces=None, smoothing=False, texturing=False, culling=True,
+                 clipping=True, **extra_options):
+        self.engine = engine
+        self.res = engine.res
+        self.maxfaces = maxfaces
+        self.smoothing = smoothing
+        self.texturing = texturing
+        self.culling = culling
+        self.clipping = clipping
+        self.mesh = None
+        self.keys = None
+        self._ws = None
+        self._status = None
+
+    def flags(self, tonemap=False):
+        f = 0
+        f |= N.T3_CULLING if self.culling else 0
+        f |= N.T3_CLIPPING if self.clipping else 0
+        f |= N.T3_SMOOTHING if self.smoothing else 0
+        f |= N.T3_TEXTURING if self.texturing else 0
+        f |= N.T3_TONEMAP if tonemap else 0
+        return f
+
+    def check_faces(self, mesh):
+        n = mesh.get_nfaces()
+        if self.maxfaces is not None and n > self.maxfaces:
+            raise ValueError(f'mesh has {n} faces, more than maxfaces={self.maxfaces}')
+        return n
+
+    # -- protocol ---------------------------------------------------------
+    def set_object(self, mesh):
+        mesh.pre_compute()
+        self.check_faces(mesh)
+        self.mesh = mesh
+
+    def render_occup(self):
+        """Clears this raster's key buffer and rasterises the current object into it."""
+        require_cuda('TriangleRaster.render_occup')
+        lib = N.load()
+        W, H = self.res
+        dev = default_device()
+        if self.keys is None or self.keys.numel() != W * H:
+            self.keys = torch.empty((W, H), dtype=torch.int64, device=dev)
+            self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        keep = []
+        ob = N.t3_object()
+        self.mesh._t3_fill(ob.mesh, dev, keep)
+        ob.nfaces = self.mesh.get_nfaces()
+        ob.face_base = 0
+        fr = N.t3_frame()
+        self.engine._t3_fill_frame(fr, self.flags(), 0.0)
+        need = 256 + 4 * max(1, ob.nfaces)
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        st = _stream()
+        N.check(lib.t3_clear(self.keys.data_ptr(), W * H, st), 't3_clear')
+        N.check(lib.t3_raster(C.byref(fr), C.byref(ob), self.keys.data_ptr(), self._ws.data_ptr(),
+                              self._ws.numel(), self._status.data_ptr(), st), 't3_raster')
+        self._keep = keep
+
+    @property
+    def occup(self):
+        """Winning face id per pixel, -1 where empty (TriangleRaster.occup)."""
+        k = self.keys
+        ids = (k & 0xFFFFFFFF).to(torch.int32)
+        return torch.where(k == -1, torch.full_like(ids, -1), ids)
+
+    def render_color(self, shader):
+        """Shades the pixels this raster won with `shader` (a Shader of the scene)."""
+        shader.shade_from_keys(self, self.keys)
+
+
+class Shader:
+    """Shader(img, lighting, material) (tina/core/shader.py:112-135): shades the
+    winning fragments of one raster into `img`."""
+
+    def __init__(self, img, lighting, material, scene=None):
+        self.img = img
+        self.lighting = lighting
+        self.material = material
+        self.scene = scene
+
+    def shade_from_keys(self, raster, keys):
+        require_cuda('Shader')
+        lib = N.load()
+        sc = N.t3_scene()
+        keep = []
+        dev = default_device()
+        raster.engine._t3_fill_frame(sc.frame, raster.flags(), 0.0)
+        self.lighting._t3_fill(sc.lighting)
+        sc.nobjects = 1
+        ob = sc.objects[0]
+        raster.mesh._t3_fill(ob.mesh, dev, keep)
+        ob.nfaces = raster.mesh.get_nfaces()
+        ob.face_base = 0
+        mat, _ = compile_material(self.material, raster.mesh.attr_stride())
+        ob.material = mat
+        size = C.c_size_t()
+        N.check(lib.t3_workspace_size(C.byref(sc), N.T3_RASTER_DIRECT, 16, 0, C.byref(size)),
+                't3_workspace_size')
+        ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+        # shade into a scratch image, then keep only the pixels this raster won
+        W, H = raster.res
+        tmp = torch.empty((W, H, 3), dtype=torch.float32, device=dev)
+        outs = N.t3_outputs()
+        outs.rgb = tmp.data_ptr()
+        N.check(lib.t3_shade(C.byref(sc), keys.data_ptr(), ws.data_ptr(), ws.numel(), C.byref(outs),
+                             _stream()), 't3_shade')
+        won = (keys != -1).unsqueeze(-1)
+        self.img.copy_(torch.where(won, tmp, self.img))
+
+
+class Scene:
+    """Tina's Scene(res, **options) (tina/scene/raster.py:5-258).
+
+    Options kept from the reference: smoothing, texturing, culling, clipping,
+    maxfaces, tonemap (default True), bgcolor (default 0).  Extension options:
+    raster ('direct' | 'binned'), tile (8 | 16 | 32), bin_capacity.  taa, ssr,
+    ssao, fxaa and blooming are outside this rasteriser build; ibl selects
+    SkyboxLighting.
+    """
+
+    def __init__(self, res_x=512, res_y=None, **options):
+        for opt in _UNSUPPORTED_OPTIONS:
+            if options.get(opt, False):
+                raise NotImplementedError(f'Scene({opt}=True) is not part of this rasteriser build')
+        self.engine = Engine(res_x, res_y)
+        self.res = self.engine.res
+        self.options = options
+        self.ibl = options.get('ibl', False)
+        self.tonemap = options.get('tonemap', True)
+        self.bgcolor = options.get('bgcolor', 0)
+        self.raster_mode = options.get('raster', 'direct')
+        if self.raster_mode not in RASTER_MODES:
+            raise ValueError(f"raster must be one of {list(RASTER_MODES)}")
+        self.tile = int(options.get('tile', 16))
+        self.bin_capacity = int(options.get('bin_capacity', 0))
+        if self.ibl:
+            from .skybox import SkyboxLighting
+            self.lighting = options.get('lighting') or SkyboxLighting()
+        else:
+            self.lighting = Lighting()
+            # add_default_lights (tina/scene/raster.py:89-93)
+            self.lighting.add_light(dir=[1, 2, 3], color=[0.9, 0.9, 0.9])
+            self.lighting.set_ambient_light([0.1, 0.1, 0.1])
+        self.default_material = Diffuse()
+        self.materials = []
+        self.objects = {}
+        self.raster_options = {k: options[k] for k in
+                               ('maxfaces', 'smoothing', 'texturing', 'culling', 'clipping')
+                               if k in options}
+        self.triangle_raster = None
+        self.image = None
+        self.face_id = None
+        self.depth_f = None
+        self._ws = None
+        self._status = None
+        self._keep = []
+        self._last_scene = None
+
+    def add_object(self, object, material=None, raster=None):
+        """(tina/scene/raster.py:112-146)"""
+        assert object not in self.objects
+        if material is None:
+            material = self.default_material
+        if raster is None:
+            if hasattr(object, 'get_nfaces'):
+                if hasattr(object, 'get_npolygon') and object.get_npolygon() == 2:
+                    raise NotImplementedError('wireframe rasterisation is not part of this build')
+                if self.triangle_raster is None:
+                    self.triangle_raster = TriangleRaster(self.engine, **self.raster_options)
+                raster = self.triangle_raster
+            elif hasattr(object, 'get_npars') or hasattr(object, 'sample_volume'):
+                raise NotImplementedError('particle / volume rasterisation is not part of this build')
+            else:
+                raise ValueError(f'cannot determine raster type of object: {object}')
+        if len(self.objects) >= N.T3_MAX_OBJECTS:
+            raise ValueError(f'at most {N.T3_MAX_OBJECTS} objects per scene')
+        if material not in self.materials:
+            self.materials.append(material)
+        self.objects[object] = _Obj(material, raster)
+
+    def _raster(self):
+        if self.triangle_raster is None:
+            self.triangle_raster = TriangleRaster(self.engine, **self.raster_options)
+        return self.triangle_raster
+
+    def describe(self, device=None):
+        """The t3_scene descriptor of the current state, with pointers on `device`
+        (default: the CUDA device).  Returns (descriptor, keep-alive list)."""
+        device = device or default_device()
+        sc = N.t3_scene()
+        keep = []
+        raster = self._raster()
+        self.engine._t3_fill_frame(sc.frame, raster.flags(self.tonemap), self.bgcolor)
+        self.lighting._t3_fill(sc.lighting)
+        if hasattr(self.lighting, '_t3_fill_device'):
+            self.lighting._t3_fill_device(sc.lighting, device, keep)
+        base = 0
+        sc.nobjects = len(self.objects)
+        for o, (obj, info) in enumerate(self.objects.items()):
+            ob = sc.objects[o]
+            obj._t3_fill(ob.mesh, device, keep)
+            n = info.raster.check_faces(obj)
+            ob.nfaces = n
+            ob.face_base = base
+            base += n
+            mat, uses_attr = compile_material(info.material, obj.attr_stride() if hasattr(obj, 'attr_stride') else 0)
+            if uses_attr and not ob.mesh.face_attr:
+                raise ValueError('material uses FaceAttr but the mesh has no face attributes '
+                                 '(mesh.set_face_attrs)')
+            ob.material = mat
+        return sc, keep
+
+    def _alloc_outputs(self, dev):
+        W, H = self.res
+        if self.image is None or tuple(self.image.shape[:2]) != (W, H):
+            self.image = torch.empty((W, H, 3), dtype=torch.float32, device=dev)
+            self.face_id = torch.empty((W, H), dtype=torch.int32, device=dev)
+            self.engine.depth = torch.empty((W, H), dtype=torch.int32, device=dev)
+            self.depth_f = torch.empty((W, H), dtype=torch.float32, device=dev)
+            self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def render(self):
+        """Renders one frame into self.img (tina/scene/raster.py:168-207)."""
+        require_cuda('Scene.render')
+        lib = N.load()
+        dev = default_device()
+        for obj in self.objects:
+            obj.pre_compute()
+        sc, keep = self.describe(dev)
+        self._alloc_outputs(dev)
+        mode = RASTER_MODES[self.raster_mode]
+        size = C.c_size_t()
+        N.check(lib.t3_workspace_size(C.byref(sc), mode, self.tile, self.bin_capacity, C.byref(size)),
+                't3_workspace_size')
+        if self._ws is None or self._ws.numel() < size.value:
+            self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+        outs = N.t3_outputs()
+        outs.rgb = self.image.data_ptr()
+        outs.face_id = self.face_id.data_ptr()
+        outs.depth = self.engine.depth.data_ptr()
+        outs.depth_f = self.depth_f.data_ptr()
+        N.check(lib.t3_render(C.byref(sc), mode, self.tile, self.bin_capacity, self._ws.data_ptr(),
+                              self._ws.numel(), self._status.data_ptr(), C.byref(outs), _stream()),
+                't3_render')
+        self._keep = keep
+        self._last_scene = sc
+
+    def status(self):
+        """Device status bits of the last render (synchronises)."""
+        lib = N.load()
+        out = C.c_int32()
+        N.check(lib.t3_read_status(self._status.data_ptr(), C.byref(out), _stream()), 't3_read_status')
+        return out.value
+
+    @property
+    def img(self):
+        """The final image (tina/scene/raster.py:209-214): float32 (W, H, 3)."""
+        return self.image
+
+    def input(self, gui):
+        raise NotImplementedError('GUI camera control is not part of this headless build; '
+                                  'call scene.engine.set_camera(view, proj)')
