@@ -1,0 +1,129 @@
+"""Golden scenes, written once against Tina's public API.
+
+Each recipe takes the `tina` module it should use -- the reference package
+(executed under the Taichi stand-in by make_golden.py) or taichi_three_gb300 --
+plus the scene's seeded input arrays, and builds the scene with identical calls.
+That the same code runs on both is the drop-in check; the saved outputs are the
+golden vectors.
+"""
+import numpy as np
+
+
+def _soup(n, seed, spread=0.9, sigma=0.3):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    centres = rng.uniform(-spread, spread, size=(n, 1, 3))
+    verts = (centres + rng.normal(0, sigma, size=(n, 3, 3))).astype(np.float32)
+    nrm = rng.normal(size=(n, 3, 3))
+    norms = (nrm / np.linalg.norm(nrm, axis=-1, keepdims=True)).astype(np.float32)
+    return verts, norms
+
+
+def inputs(name):
+    """Seeded input arrays of each golden scene."""
+    if name == 'tri_pair':
+        # two faces sharing an edge, given in NDC (default engine matrices)
+        v = np.array([[[-1, -1, -0.5], [1, -1, -0.5], [-1, 1, -0.5]],
+                      [[1, -1, -0.5], [1, 1, -0.5], [-1, 1, -0.5]],
+                      [[-0.6, -0.9, -0.2], [0.7, -0.2, -0.8], [-0.3, 0.8, -0.1]]], np.float32)
+        return {'verts': v}
+    if name in ('soup_pbr', 'soup_classic', 'soup_transform', 'two_objects'):
+        seed = {'soup_pbr': 1, 'soup_classic': 2, 'soup_transform': 3, 'two_objects': 4}[name]
+        verts, norms = _soup(240, seed)
+        out = {'verts': verts, 'norms': norms}
+        if name == 'two_objects':
+            v2, n2 = _soup(160, seed + 100)
+            out.update(verts2=v2, norms2=n2)
+        return out
+    if name == 'grid_pbr':
+        n = 9
+        u = np.linspace(0, 1, n)
+        x, y = np.meshgrid(u * 2 - 1, u * 2 - 1, indexing='ij')
+        pos = np.stack([x, y, 0.15 * np.sin(3 * x + 0.5) * np.cos(2 * y)], -1).astype(np.float32)
+        return {'pos': pos}
+    if name == 'sphere_lambert':
+        return {}
+    raise KeyError(name)
+
+
+NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
+         'two_objects']
+
+
+def build(tina, name, arrays, matrix):
+    """Builds scene `name` with module `tina`; `matrix` provides lookat/perspective
+    (tina.util.matrix in the reference).  Returns (scene, single_object)."""
+    if name == 'tri_pair':
+        scene = tina.Scene(16, 12)
+        mesh = tina.SimpleMesh()
+        scene.add_object(mesh)
+        mesh.set_face_verts(arrays['verts'])
+        return scene, True
+    if name == 'sphere_lambert':
+        scene = tina.Scene(64, 64, smoothing=True)
+        mesh = tina.PrimitiveMesh.sphere(lons=24, lats=12)
+        scene.add_object(mesh, tina.Diffuse(color=0.8))
+        scene.lighting.clear_lights()
+        scene.lighting.add_light(dir=[1, 1, -1])
+        scene.lighting.add_light(dir=[0.3, 0.5, 1.0], color=[0.6, 0.5, 0.4])
+        scene.lighting.set_ambient_light([0.0, 0.0, 0.0])
+        scene.engine.set_camera(matrix.lookat(back=(0, 0, 3)), matrix.perspective(60, 1))
+        return scene, True
+    if name == 'soup_pbr':
+        scene = tina.Scene(48, 36, smoothing=True)
+        mesh = tina.SimpleMesh()
+        scene.add_object(mesh, tina.PBR(basecolor=[0.8, 0.4, 0.2], metallic=0.3, roughness=0.35))
+        mesh.set_face_verts(arrays['verts'])
+        mesh.set_face_norms(arrays['norms'])
+        scene.lighting.clear_lights()
+        scene.lighting.add_light(pos=[1.5, 1.0, 2.0], color=[3.0, 3.0, 3.0])
+        scene.lighting.add_light(pos=[-2.0, 0.5, 1.0], color=[1.0, 2.0, 1.5])
+        scene.lighting.add_light(dir=[0.2, -0.4, 1.0], color=[0.3, 0.3, 0.3])
+        scene.lighting.set_ambient_light([0.05, 0.05, 0.05])
+        scene.engine.set_camera(matrix.lookat(back=(0.3, 0.2, 3)), matrix.perspective(60, 48 / 36))
+        return scene, True
+    if name == 'soup_classic':
+        scene = tina.Scene(48, 36, culling=False)
+        mesh = tina.SimpleMesh()
+        scene.add_object(mesh, tina.Classic())
+        mesh.set_face_verts(arrays['verts'])
+        scene.engine.set_camera(matrix.lookat(back=(-0.4, 0.3, 3)), matrix.perspective(55, 48 / 36))
+        return scene, True
+    if name == 'soup_transform':
+        scene = tina.Scene(40, 40, smoothing=True, tonemap=False, bgcolor=0.1)
+        mesh = tina.SimpleMesh()
+        mesh.set_face_verts(arrays['verts'])
+        mesh.set_face_norms(arrays['norms'])
+        trans = tina.MeshTransform(mesh)
+        trans.set_transform(matrix.translate([0.2, -0.1, 0.3]) @ matrix.scale([0.8, 1.2, 0.9]))
+        scene.add_object(tina.MeshNoCulling(trans), tina.Diffuse(color=[0.2, 0.7, 0.4]))
+        scene.engine.set_camera(matrix.lookat(back=(0, 0, 3)), matrix.perspective(60, 1))
+        return scene, True
+    if name == 'grid_pbr':
+        scene = tina.Scene(48, 36, smoothing=True)
+        grid = tina.MeshGrid(9)
+        _set_grid(grid, arrays['pos'])
+        scene.add_object(grid, tina.PBR(metallic=0.8, roughness=0.5))
+        scene.engine.set_camera(matrix.lookat(back=(0.3, -1.2, 2.2)), matrix.perspective(60, 48 / 36))
+        return scene, True
+    if name == 'two_objects':
+        scene = tina.Scene(48, 36, smoothing=True)
+        m1 = tina.SimpleMesh()
+        m1.set_face_verts(arrays['verts'])
+        m1.set_face_norms(arrays['norms'])
+        m2 = tina.SimpleMesh()
+        m2.set_face_verts(arrays['verts2'])
+        m2.set_face_norms(arrays['norms2'])
+        scene.add_object(m1, tina.Diffuse(color=[0.9, 0.6, 0.3]))
+        scene.add_object(m2, tina.Lamp(color=[0.2, 0.5, 1.0]))
+        scene.engine.set_camera(matrix.lookat(back=(0, 0, 3)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    raise KeyError(name)
+
+
+def _set_grid(grid, pos):
+    p = grid.pos
+    if hasattr(p, 'from_numpy'):       # a Taichi field (reference)
+        p.from_numpy(pos)
+    else:                              # a torch tensor
+        import torch
+        p.copy_(torch.from_numpy(pos).to(p.device))

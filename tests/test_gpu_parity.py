@@ -28,13 +28,18 @@ def gpu_render(scene):
     }
 
 
-def assert_parity(g, o, rgb_tol=RGB_TOL, o64=None):
+def assert_parity(g, o, rgb_tol=RGB_TOL, o64=None, hdr=False):
+    """hdr: the image is not tonemapped (values unbounded), so the bound is
+    relative: |gpu - oracle| <= rgb_tol * max(1, |oracle|)."""
     assert np.array_equal(g['face_id'], o['face_id']), \
         f"face id mismatch at {np.argwhere(g['face_id'] != o['face_id'])[:5].tolist()}"
     assert np.array_equal(g['depth'], o['depth'])
     assert np.array_equal(g['depth_f'].view(np.uint32), o['depth_f'].view(np.uint32))
-    err = np.abs(g['rgb'] - o['rgb']).max() if g['rgb'].size else 0.0
-    assert err <= rgb_tol, f'rgb max abs err {err}'
+    diff = np.abs(g['rgb'] - o['rgb'])
+    if hdr:
+        diff = diff / np.maximum(1.0, np.abs(o['rgb']))
+    err = diff.max() if g['rgb'].size else 0.0
+    assert err <= rgb_tol, f'rgb max {"rel" if hdr else "abs"} err {err}'
     if o64 is not None:
         same = g['face_id'] == o64['face_id']
         e64 = np.abs(g['rgb'][same] - o64['rgb'][same]).max() if same.any() else 0.0
@@ -84,7 +89,7 @@ def test_material_variants(cuda, oracle_mod, material):
                                   dict(smoothing=False), dict(bgcolor=(0.1, 0.2, 0.3))])
 def test_scene_options(cuda, oracle_mod, opts):
     scene, _ = random_soup_scene(6, ntri=2000, res=(128, 80), **opts)
-    assert_parity(gpu_render(scene), oracle_mod.render(scene))
+    assert_parity(gpu_render(scene), oracle_mod.render(scene), hdr=not scene.tonemap)
 
 
 def test_shared_edges_and_ties(cuda, oracle_mod):
