@@ -259,7 +259,12 @@ def main():
     with torch.cuda.graph(graph):
         frame(torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    kernels_per_frame = 2 + 2 * len(scene.objects) + 1  # upload, clear, (raster, big) x obj, shade
+    if args.raster == "direct":  # upload, clear, (raster, big) x objects, shade
+        kernels_per_frame = 2 + 2 * len(scene.objects) + 1
+        stage_names = ("clear", "raster", "shade")
+    else:                        # upload, bin x objects, tile (raster + shade)
+        kernels_per_frame = 1 + len(scene.objects) + 1
+        stage_names = ("upload", "bin", "tile")
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     for i in range(args.warmup):
@@ -303,7 +308,7 @@ def main():
     for e in evs:
         N.check(lib.t3_event_create(C.byref(e)), "t3_event_create")
     ev_arr = (C.c_void_p * 4)(*[e.value for e in evs])
-    stage = {"clear": [], "raster": [], "shade": []}
+    stage = {k: [] for k in stage_names}
     stream = torch.cuda.current_stream().cuda_stream
     for i in range(20):
         flush.fill_(float(i))
@@ -321,10 +326,14 @@ def main():
     fid = scene.face_id
     visible = int(torch.unique(fid[fid >= 0]).numel())
     attr_b = 4 * (mesh.face_attr.shape[1] if mesh.face_attr is not None else 0)
+    out_b = (12 + 4 + 4 + 4) * P  # rgb, face id, depth, depth_f written once
     alg = {
         "clear": 8 * P,
         "raster": 36 * faces,
-        "shade": 8 * P + (12 + 4 + 4 + 4) * P + visible * (36 + 36 + attr_b),
+        "shade": 8 * P + out_b + visible * (36 + 36 + attr_b),
+        "upload": 0,
+        "bin": 36 * faces,
+        "tile": out_b + visible * (36 + 36 + attr_b),
     }
     dominant = max(stage_ms, key=lambda k: stage_ms[k])
     peak, peak_kind = peaks()

@@ -177,6 +177,12 @@ int t3_struct_sizes(int64_t* out, int n);
 int t3_workspace_size(const t3_scene* scene, int mode, int tile,
                       int64_t bin_capacity, size_t* bytes);
 
+/* Effective per-tile bin capacity (entries) of the binned rasteriser for this
+ * scene at tile edge `tile`; `bin_capacity` 0 selects the automatic size
+ * (8 x faces / tiles + 64, rounded up to 32).  No counterpart in the
+ * reference, whose rasteriser has no bins. */
+int t3_bin_capacity(const t3_scene* scene, int tile, int64_t bin_capacity, int64_t* capacity);
+
 /* Engine.clear_depth (tina/core/engine.py:68-70) for the packed buffer:
  * depth_id[W*H] = empty key. */
 int t3_clear(uint64_t* depth_id, int64_t npixels, void* stream);

@@ -38,6 +38,7 @@ T3_OP_LAMBERT, T3_OP_PHONG, T3_OP_COOK, T3_OP_EMISSION = 16, 17, 18, 19
 T3_OP_MIX, T3_OP_SCALE, T3_OP_ADD = 32, 33, 34
 
 T3_LIGHT_LAMPS, T3_LIGHT_IBL = 0, 1
+T3_STATUS_BIG_OVERFLOW, T3_STATUS_BIN_OVERFLOW, T3_STATUS_TIMEOUT = 1, 2, 4
 T3_RASTER_DIRECT, T3_RASTER_BINNED = 0, 1
 
 
@@ -101,6 +102,7 @@ SIGNATURES = {
     "t3_workspace_size": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64,
                                     C.POINTER(C.c_size_t)]),
     "t3_clear": (C.c_int, [_VP, _I64, _VP]),
+    "t3_bin_capacity": (C.c_int, [C.POINTER(t3_scene), C.c_int, _I64, C.POINTER(C.c_int64)]),
     "t3_raster": (C.c_int, [C.POINTER(t3_frame), C.POINTER(t3_object), _VP, _VP, _SZ, _VP, _VP]),
     "t3_shade": (C.c_int, [C.POINTER(t3_scene), _VP, _VP, _SZ, C.POINTER(t3_outputs), _VP]),
     "t3_render": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,

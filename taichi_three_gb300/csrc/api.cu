@@ -14,9 +14,6 @@ namespace t3 {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-size_t ws_scene_end() { return align256(T3_WS_SCENE + sizeof(DevScene)); }
-size_t ws_big_items() { return ws_scene_end(); }
-
 static int is_leaf(int op) {
   return op == T3_OP_LAMBERT || op == T3_OP_PHONG || op == T3_OP_COOK || op == T3_OP_EMISSION;
 }
@@ -161,22 +158,66 @@ static int64_t max_object_faces(const t3_scene& sc) {
   return m;
 }
 
+static int64_t total_faces(const t3_scene& sc) {
+  int64_t t = 0;
+  for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++) t += sc.objects[o].nfaces;
+  return t;
+}
+
+// Workspace layout of one frame (byte offsets, 256-aligned):
+//   scene     DevScene (device copy of the descriptors)
+//   counters  uint32[64 + ntiles]: per-object big-face counts, big-list count,
+//             tile bin counts -- zeroed by the scene upload every frame
+//   big       uint32[big_capacity] big-face ids
+//   direct:   keys  uint64[W*H] packed (depth, id)
+//   binned:   rec   float4[4 * total_faces] setup records
+//             bins  uint32[ntiles * bin_capacity]
 struct Layout {
-  size_t counters, scene, big_items, keys, end;
-  uint32_t big_capacity;
+  size_t scene, counters, big, keys, rec, bins, end;
+  int ncounters;
+  uint32_t big_capacity, bin_capacity;
+  int tile, tiles_x, tiles_y;
 };
 
-static Layout layout_for(const t3_scene& sc) {
-  Layout L;
-  L.counters = T3_WS_COUNTERS;
-  L.scene = T3_WS_SCENE;
-  L.big_items = ws_big_items();
-  int64_t cap = max_object_faces(sc);
+static int64_t auto_bin_capacity(const t3_scene& sc, int tile) {
+  const int64_t tx = (sc.frame.width + tile - 1) / tile, ty = (sc.frame.height + tile - 1) / tile;
+  const int64_t per = 8 * total_faces(sc) / (tx * ty) + 64;
+  int64_t cap = per < 64 ? 64 : per > (1 << 16) ? (1 << 16) : per;
+  return (cap + 31) & ~(int64_t)31;
+}
+
+static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capacity, Layout& L) {
+  std::memset(&L, 0, sizeof(L));
+  L.scene = 0;
+  L.counters = align256(sizeof(DevScene));
+  L.tile = tile;
+  if (mode == T3_RASTER_BINNED) {
+    if (tile != 8 && tile != 16 && tile != 32) return T3_EINVAL;
+    L.tiles_x = (sc.frame.width + tile - 1) / tile;
+    L.tiles_y = (sc.frame.height + tile - 1) / tile;
+    int64_t cap = bin_capacity > 0 ? ((bin_capacity + 3) & ~(int64_t)3) : auto_bin_capacity(sc, tile);
+    if (cap > (1 << 20)) return T3_ETOOBIG;
+    L.bin_capacity = (uint32_t)cap;
+    L.ncounters = 64 + L.tiles_x * L.tiles_y;
+  } else if (mode == T3_RASTER_DIRECT) {
+    L.ncounters = 64;
+  } else {
+    return T3_EINVAL;
+  }
+  int64_t cap = mode == T3_RASTER_BINNED ? total_faces(sc) : max_object_faces(sc);
   if (cap < 1) cap = 1;
   L.big_capacity = (uint32_t)cap;
-  L.keys = align256(L.big_items + sizeof(uint32_t) * (size_t)cap);
-  L.end = align256(L.keys + sizeof(uint64_t) * (size_t)sc.frame.width * (size_t)sc.frame.height);
-  return L;
+  L.big = align256(L.counters + 4 * (size_t)L.ncounters);
+  const size_t after_big = align256(L.big + 4 * (size_t)cap);
+  if (mode == T3_RASTER_BINNED) {
+    L.rec = after_big;
+    L.bins = align256(L.rec + 64 * (size_t)(total_faces(sc) > 0 ? total_faces(sc) : 1));
+    L.end = align256(L.bins + 4 * (size_t)L.tiles_x * L.tiles_y * L.bin_capacity);
+  } else {
+    L.keys = after_big;
+    L.end = align256(L.keys + 8 * (size_t)sc.frame.width * (size_t)sc.frame.height);
+  }
+  return T3_OK;
 }
 
 static int cuda_rc(cudaError_t e) { return e == cudaSuccess ? T3_OK : T3_ECUDA; }
@@ -204,14 +245,23 @@ int t3_struct_sizes(int64_t* out, int n) {
 
 int t3_workspace_size(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
                       size_t* bytes) {
-  (void)tile;
-  (void)bin_capacity;
   if (!scene || !bytes) return T3_EINVAL;
-  if (mode != T3_RASTER_DIRECT) return T3_EUNSUPPORTED;
   int r = check_frame(scene->frame);
   if (r) return r;
   if (scene->nobjects < 0 || scene->nobjects > T3_MAX_OBJECTS) return T3_ETOOBIG;
-  *bytes = layout_for(*scene).end;
+  Layout L;
+  r = layout_for(*scene, mode, tile, bin_capacity, L);
+  if (r) return r;
+  *bytes = L.end;
+  return T3_OK;
+}
+
+int t3_bin_capacity(const t3_scene* scene, int tile, int64_t bin_capacity, int64_t* capacity) {
+  if (!scene || !capacity) return T3_EINVAL;
+  Layout L;
+  int r = layout_for(*scene, T3_RASTER_BINNED, tile, bin_capacity, L);
+  if (r) return r;
+  *capacity = L.bin_capacity;
   return T3_OK;
 }
 
@@ -247,14 +297,14 @@ int t3_raster(const t3_frame* frame, const t3_object* object, uint64_t* depth_id
 int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
              size_t workspace_bytes, const t3_outputs* out, void* stream) {
   if (!scene || !depth_id || !out || !out->rgb || !workspace) return T3_EINVAL;
-  if (workspace_bytes < ws_scene_end()) return T3_EINVAL;
+  if (workspace_bytes < align256(sizeof(DevScene))) return T3_EINVAL;
   static thread_local DevScene ds;
   int r = make_dev_scene(*scene, ds);
   if (r) return r;
   cudaStream_t st = (cudaStream_t)stream;
   uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
-  DevScene* dsc = reinterpret_cast<DevScene*>(ws + T3_WS_SCENE);
-  cudaError_t e = launch_upload_scene(ds, dsc, reinterpret_cast<uint32_t*>(ws), 0, st);
+  DevScene* dsc = reinterpret_cast<DevScene*>(ws);
+  cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
   return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
                               *out, st));
@@ -269,39 +319,59 @@ int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, v
 int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
                      void* workspace, size_t workspace_bytes, int32_t* status,
                      const t3_outputs* out, void* stream, void* const* stage_events) {
-  (void)tile;
-  (void)bin_capacity;
   if (!scene || !workspace || !status || !out || !out->rgb) return T3_EINVAL;
-  if (mode != T3_RASTER_DIRECT) return T3_EUNSUPPORTED;
   static thread_local DevScene ds;
   int r = make_dev_scene(*scene, ds);
   if (r) return r;
-  const Layout L = layout_for(*scene);
+  Layout L;
+  r = layout_for(*scene, mode, tile, bin_capacity, L);
+  if (r) return r;
   if (workspace_bytes < L.end) return T3_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
   uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
   uint32_t* counters = reinterpret_cast<uint32_t*>(ws + L.counters);
   DevScene* dsc = reinterpret_cast<DevScene*>(ws + L.scene);
-  unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
-  const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
   auto mark = [&](int k) -> cudaError_t {
     if (!stage_events || !stage_events[k]) return cudaSuccess;
     return cudaEventRecord((cudaEvent_t)stage_events[k], st);
   };
   cudaError_t e = mark(0);
-  if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, 64, st);
-  if (e == cudaSuccess) e = launch_clear(keys, npix, st);
-  if (e == cudaSuccess) e = mark(1);
-  for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
-    BigQueue big;
-    big.items = reinterpret_cast<uint32_t*>(ws + L.big_items);
-    big.capacity = L.big_capacity;
-    big.count = counters + o;
-    big.status = status;
-    e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 128, st);
+  if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
+  if (mode == T3_RASTER_DIRECT) {
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
+    const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
+    if (e == cudaSuccess) e = launch_clear(keys, npix, st);
+    if (e == cudaSuccess) e = mark(1);
+    for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
+      BigQueue big;
+      big.items = reinterpret_cast<uint32_t*>(ws + L.big);
+      big.capacity = L.big_capacity;
+      big.count = counters + o;
+      big.status = status;
+      e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
+    }
+    if (e == cudaSuccess) e = mark(2);
+    if (e == cudaSuccess) e = launch_shade(dsc, scene->frame, keys, *out, st);
+  } else {
+    BinArgs b;
+    b.rec = reinterpret_cast<float4*>(ws + L.rec);
+    b.bins = reinterpret_cast<uint32_t*>(ws + L.bins);
+    b.count = counters + 64;
+    b.big = reinterpret_cast<uint32_t*>(ws + L.big);
+    b.big_count = counters + 63;
+    b.status = status;
+    b.capacity = L.bin_capacity;
+    b.big_capacity = L.big_capacity;
+    b.tile = L.tile;
+    b.tiles_x = L.tiles_x;
+    b.tiles_y = L.tiles_y;
+    b.big_tiles = 16;
+    if (e == cudaSuccess) e = mark(1);
+    for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++)
+      e = launch_bin(scene->frame, scene->objects[o], b, st);
+    if (e == cudaSuccess) e = mark(2);
+    if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
   }
-  if (e == cudaSuccess) e = mark(2);
-  if (e == cudaSuccess) e = launch_shade(dsc, scene->frame, keys, *out, st);
   if (e == cudaSuccess) e = mark(3);
   return cuda_rc(e);
 }

@@ -1,19 +1,21 @@
-// raster.cu -- depth-buffer clear and the direct rasteriser.
+// raster.cu -- depth-key clear and the direct rasteriser.
 //
 // TriangleRaster.render_occup (tina/core/triangle.py:89-131) as a GB300 kernel:
 // one thread per face runs the vertex transform, back-face cull, trivial clip,
-// viewport map, bbox and edge setup, then walks the bbox and folds every covered
-// pixel into a packed 64-bit key (depth ^ sign bit) << 32 | face id with
-// atomicMin.  The unsigned minimum of that key is the serial reference's winner:
-// lowest int32 depth, ties to the lowest face id (the strict `>` at
-// triangle.py:123), so the result does not depend on thread order and the
-// reference's racy `occup[P] = f` store disappears.
+// viewport map, bbox and edge setup; the warp then rasterises its 32 faces
+// cooperatively (t3_raster.cuh) and folds every covered pixel into a packed
+// 64-bit key (depth ^ sign bit) << 32 | face id with atomicMin.  The unsigned
+// minimum of that key is the serial reference's winner: lowest int32 depth,
+// ties to the lowest face id (the strict `>` at triangle.py:123), so the result
+// does not depend on thread order and the reference's racy `occup[P] = f`
+// store disappears.
 //
 // Face-soup vertex positions (9 floats per face) are staged into shared memory
 // with 16-byte vector loads so a warp reads its 1152 contiguous bytes once.
-// Faces whose clamped bbox exceeds `big_threshold` pixels are pushed to a queue
-// and rasterised by k_raster_big, one CTA per face.
-#include "t3_internal.cuh"
+// Faces whose clamped bbox exceeds `big_threshold` pixels are queued and
+// rasterised by k_raster_big, where every CTA takes a slice of each queued
+// face's bbox.
+#include "t3_raster.cuh"
 
 namespace t3 {
 
@@ -30,104 +32,65 @@ __global__ void k_clear(unsigned long long* __restrict__ keys, int64_t n) {
   }
 }
 
-// Folds one face's covered pixels in [x0, x1] x [y0, y1] into the key buffer.
-__device__ __forceinline__ void raster_rect(const t3_frame& fr, const Setup& s, uint32_t id,
-                                            int32_t x0, int32_t x1, int32_t y0, int32_t y1,
-                                            unsigned long long* __restrict__ keys) {
-  const int64_t H = fr.height;
-  const float maxd = (float)fr.maxdepth;
-  for (int32_t x = x0; x <= x1; x++) {
-    const float px = xadd((float)x, fr.bias[0]);
-    for (int32_t y = y0; y <= y1; y++) {
-      const float py = xadd((float)y, fr.bias[1]);
-      float wx, wy, wz, sum;
-      face_raw_weights(s, px, py, wx, wy, wz, sum);
-      f3 wei;
-      if (!face_inside(wx, wy, wz, sum, wei)) continue;
-      const int32_t d = trunc_i32(xmul(face_depth(s, wei), maxd));
-      if (d >= fr.maxdepth) continue;  // can never pass `old > depth`
-      const unsigned long long key = pack_key(d, id);
-      unsigned long long* p = keys + (int64_t)x * H + y;
-      // keys only decrease: a stale read can only send us to the atomic
-      if (key < *reinterpret_cast<volatile unsigned long long*>(p)) atomicMin(p, key);
-    }
+struct GlobalKeySink {
+  unsigned long long* keys;
+  int64_t H;
+  __device__ __forceinline__ void operator()(int x, int y, unsigned long long key) const {
+    unsigned long long* p = keys + (int64_t)x * H + y;
+    // keys only decrease: a stale read can only send us to the atomic
+    if (key < *reinterpret_cast<volatile unsigned long long*>(p)) atomicMin(p, key);
   }
-}
+};
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
 k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t face_base,
                 unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold) {
   __shared__ __align__(16) float sv[BLOCK * 9];
+  __shared__ WarpFaces wfs[BLOCK / 32];
   const int64_t f0 = (int64_t)blockIdx.x * BLOCK;
-  const bool staged = mesh.kind == T3_MESH_SOUP && !(mesh.flags & T3_MESH_NOCULL);
-  if (staged) {
-    const int64_t rem = nfaces - f0;
-    const int nf = rem < BLOCK ? (int)rem : BLOCK;
-    const float* src = mesh.verts + f0 * 9;
-    const int nflt = nf * 9;
-    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-      const int n4 = nflt >> 2;
-      const float4* s4 = reinterpret_cast<const float4*>(src);
-      float4* d4 = reinterpret_cast<float4*>(sv);
-      for (int i = threadIdx.x; i < n4; i += BLOCK) d4[i] = __ldg(s4 + i);
-      for (int i = (n4 << 2) + threadIdx.x; i < nflt; i += BLOCK) sv[i] = __ldg(src + i);
-    } else {
-      for (int i = threadIdx.x; i < nflt; i += BLOCK) sv[i] = __ldg(src + i);
-    }
-    __syncthreads();
-  }
+  const bool staged = stage_soup<BLOCK>(mesh, nfaces, f0, sv);
   const int64_t n = f0 + threadIdx.x;
-  if (n >= nfaces) return;
-  f3 v[3];
-  if (staged) {
-    const float* p = sv + threadIdx.x * 9;
-    f3 t[3] = {f3{p[0], p[1], p[2]}, f3{p[3], p[4], p[5]}, f3{p[6], p[7], p[8]}};
-    if (mesh.flags & T3_MESH_TRANSFORM) {
-#pragma unroll
-      for (int k = 0; k < 3; k++) t[k] = mapply_pos_x(mesh.trans, t[k]);
-    }
-    const bool flip = (mesh.flags & T3_MESH_FLIP_ORDER) != 0;
-    v[0] = flip ? t[2] : t[0];
-    v[1] = t[1];
-    v[2] = flip ? t[0] : t[2];
-  } else {
-    face_verts(mesh, face_ref(mesh, n), v);
+  Setup s{};
+  bool vis = false;
+  if (n < nfaces) {
+    f3 v[3];
+    load_face(mesh, n, staged, sv, v);
+    vis = face_setup(fr, v, s) && s.botx <= s.topx && s.boty <= s.topy;
   }
-  Setup s;
-  if (!face_setup(fr, v, s)) return;
-  if (s.botx > s.topx || s.boty > s.topy) return;
-  const int64_t area = (int64_t)(s.topx - s.botx + 1) * (int64_t)(s.topy - s.boty + 1);
-  if (area > big_threshold) {
-    const uint32_t slot = atomicAdd(big.count, 1u);
-    if (slot < big.capacity) {
-      big.items[slot] = (uint32_t)n;
-    } else {
-      atomicOr(big.status, T3_STATUS_BIG_OVERFLOW);
+  if (vis) {
+    const int64_t area = (int64_t)(s.topx - s.botx + 1) * (int64_t)(s.topy - s.boty + 1);
+    if (area > big_threshold) {
+      const uint32_t slot = atomicAdd(big.count, 1u);
+      if (slot < big.capacity) big.items[slot] = (uint32_t)n;
+      else atomicOr(big.status, T3_STATUS_BIG_OVERFLOW);
+      vis = false;
     }
-    return;
   }
-  raster_rect(fr, s, face_base + (uint32_t)n, s.botx, s.topx, s.boty, s.topy, keys);
+  GlobalKeySink sink{keys, fr.height};
+  warp_raster(wfs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0, fr.width - 1, 0,
+              fr.height - 1, fr, sink);
 }
 
-// One CTA per queued large face: threads stride over the face's bbox pixels.
+// Large faces: every CTA walks a slice of every queued face's bbox.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
 k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
              unsigned long long* __restrict__ keys, BigQueue big) {
   const uint32_t count = min(*big.count, big.capacity);
-  const int64_t H = fr.height;
   const float maxd = (float)fr.maxdepth;
-  for (uint32_t e = blockIdx.x; e < count; e += gridDim.x) {
+  GlobalKeySink sink{keys, fr.height};
+  const int64_t stride = (int64_t)gridDim.x * BLOCK;
+  for (uint32_t e = 0; e < count; e++) {
     const uint32_t n = big.items[e];
     f3 v[3];
     face_verts(mesh, face_ref(mesh, n), v);
     Setup s;
     if (!face_setup(fr, v, s)) continue;
-    const int32_t w = s.topx - s.botx + 1, h = s.topy - s.boty + 1;
-    const int64_t area = (int64_t)w * h;
+    const int32_t h = s.topy - s.boty + 1;
+    const int64_t area = (int64_t)(s.topx - s.botx + 1) * h;
     const uint32_t id = face_base + n;
-    for (int64_t k = threadIdx.x; k < area; k += BLOCK) {
+    for (int64_t k = (int64_t)blockIdx.x * BLOCK + threadIdx.x; k < area; k += stride) {
       const int32_t x = s.botx + (int32_t)(k / h);
       const int32_t y = s.boty + (int32_t)(k - (k / h) * h);
       const float px = xadd((float)x, fr.bias[0]);
@@ -138,9 +101,7 @@ k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
       if (!face_inside(wx, wy, wz, sum, wei)) continue;
       const int32_t d = trunc_i32(xmul(face_depth(s, wei), maxd));
       if (d >= fr.maxdepth) continue;
-      const unsigned long long key = pack_key(d, id);
-      unsigned long long* p = keys + (int64_t)x * H + y;
-      if (key < *reinterpret_cast<volatile unsigned long long*>(p)) atomicMin(p, key);
+      sink(x, y, pack_key(d, id));
     }
   }
 }

@@ -20,6 +20,21 @@ struct BigQueue {
   int32_t* status;
 };
 
+// Binned rasteriser state (binned.cu).
+struct BinArgs {
+  float4* rec;           // setup records, 4 x float4 per global face id
+  uint32_t* bins;        // [ntiles, capacity] face ids
+  uint32_t* count;       // [ntiles] entries appended (may exceed capacity)
+  uint32_t* big;         // big-face ids
+  uint32_t* big_count;
+  int32_t* status;
+  uint32_t capacity;     // entries per tile bin (multiple of 4)
+  uint32_t big_capacity;
+  int32_t tile;          // tile edge in pixels (8, 16, 32)
+  int32_t tiles_x, tiles_y;
+  int32_t big_tiles;     // faces touching more tiles than this go to the big list
+};
+
 // A material tree flattened into a sum of weighted leaf lobes:
 //   brdf = sum_k W_k * leaf_k.brdf,  ambient = sum_k W_k * leaf_k.ambient, ...
 // W_k is a product of factor nodes along the path from the root (Mix contributes
@@ -56,21 +71,19 @@ struct DevScene {
   DevObject obj[T3_MAX_OBJECTS];
 };
 
-// workspace layout (byte offsets, 256-aligned)
-#define T3_WS_COUNTERS 0        // uint32[64]: per-object big-queue counts, misc
-#define T3_WS_SCENE 256         // DevScene
-size_t ws_scene_end();
-size_t ws_big_items();          // offset of the big-face queue
 
 int flatten_material(const t3_material& in, DevMaterial& out);
 int make_dev_scene(const t3_scene& sc, DevScene& out);
 
 cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st);
 cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
-                                int ncounters, cudaStream_t st);
+                                int ncounters, int32_t* status, cudaStream_t st);
 cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
                          const t3_outputs& out, cudaStream_t st);
+cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
+cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,
+                        cudaStream_t st);
 
 } // namespace t3

@@ -1,0 +1,128 @@
+// t3_raster.cuh -- warp-cooperative, load-balanced rasterisation of 32 faces.
+//
+// Face sizes in a soup are lognormal, so "one thread walks its face's bbox"
+// leaves a warp waiting on its largest face.  Here each lane contributes one
+// face (its clipped bbox), the warp prefix-sums the bbox areas, and the lanes
+// then walk the concatenated pixel list 32 pixels at a time: lane l takes
+// pixel base + l, finds its face by binary search over the prefix sums and runs
+// the exact inside / depth test of triangle.py:115-125 on it.  Setups live in
+// shared memory (structure of arrays, one slot per lane).
+#pragma once
+
+#include "t3_internal.cuh"
+
+namespace t3 {
+
+struct WarpFaces {
+  float bx[32], by[32], cx[32], cy[32], bcnx[32], bcny[32], canx[32], cany[32];
+  float wsa[32], wsb[32], wsc[32], Az[32], Bz[32], Cz[32];
+  int x0[32], y0[32], h[32], incl[32];
+  uint32_t id[32];
+};
+
+// Every lane of the warp must call this.  `active` lanes contribute the face
+// `s` clipped to [cx0, cx1] x [cy0, cy1]; sink(x, y, key) receives every
+// covered pixel with its packed (depth, id) key.
+template <class Sink>
+__device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool active, uint32_t id,
+                                            int cx0, int cx1, int cy0, int cy1,
+                                            const t3_frame& fr, Sink sink) {
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  const int x0 = max(s.botx, cx0), x1 = min(s.topx, cx1);
+  const int y0 = max(s.boty, cy0), y1 = min(s.topy, cy1);
+  const int area = (active && x0 <= x1 && y0 <= y1) ? (x1 - x0 + 1) * (y1 - y0 + 1) : 0;
+  if (area > 0) {
+    wf.bx[lane] = s.bx; wf.by[lane] = s.by; wf.cx[lane] = s.cx; wf.cy[lane] = s.cy;
+    wf.bcnx[lane] = s.bcnx; wf.bcny[lane] = s.bcny; wf.canx[lane] = s.canx; wf.cany[lane] = s.cany;
+    wf.wsa[lane] = s.wsa; wf.wsb[lane] = s.wsb; wf.wsc[lane] = s.wsc;
+    wf.Az[lane] = s.Az; wf.Bz[lane] = s.Bz; wf.Cz[lane] = s.Cz;
+    wf.x0[lane] = x0; wf.y0[lane] = y0; wf.h[lane] = y1 - y0 + 1; wf.id[lane] = id;
+  }
+  int incl = area;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  wf.incl[lane] = incl;
+  const int total = __shfl_sync(FULL, incl, 31);
+  __syncwarp();
+  const float maxd = (float)fr.maxdepth;
+  const float biasx = fr.bias[0], biasy = fr.bias[1];
+  for (int base = 0; base < total; base += 32) {
+    const int idx = base + lane;
+    if (idx < total) {
+      // first face j with incl[j] > idx
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (wf.incl[j + step - 1] <= idx) j += step;
+      const int off = idx - (j ? wf.incl[j - 1] : 0);
+      const int h = wf.h[j];
+      int q = __float2int_rz(__fdividef((float)off + 0.5f, (float)h));
+      int r = off - q * h;
+      if (r < 0) { q--; r += h; } else if (r >= h) { q++; r -= h; }
+      const int x = wf.x0[j] + q, y = wf.y0[j] + r;
+      Setup t;
+      t.bx = wf.bx[j]; t.by = wf.by[j]; t.cx = wf.cx[j]; t.cy = wf.cy[j];
+      t.bcnx = wf.bcnx[j]; t.bcny = wf.bcny[j]; t.canx = wf.canx[j]; t.cany = wf.cany[j];
+      t.wsa = wf.wsa[j]; t.wsb = wf.wsb[j]; t.wsc = wf.wsc[j];
+      const float px = xadd((float)x, biasx), py = xadd((float)y, biasy);
+      float wx, wy, wz, sum;
+      face_raw_weights(t, px, py, wx, wy, wz, sum);
+      f3 wei;
+      if (face_inside(wx, wy, wz, sum, wei)) {
+        t.Az = wf.Az[j]; t.Bz = wf.Bz[j]; t.Cz = wf.Cz[j];
+        const int32_t d = trunc_i32(xmul(face_depth(t, wei), maxd));
+        if (d < fr.maxdepth) sink(x, y, pack_key(d, wf.id[j]));
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Loads (and transforms) the corners of face n; soup positions come from the
+// block's shared-memory staging area when `staged`.
+__device__ __forceinline__ void load_face(const t3_mesh& mesh, int64_t n, bool staged,
+                                          const float* sv, f3 v[3]) {
+  if (staged) {
+    const float* p = sv + threadIdx.x * 9;
+    f3 t[3] = {f3{p[0], p[1], p[2]}, f3{p[3], p[4], p[5]}, f3{p[6], p[7], p[8]}};
+    if (mesh.flags & T3_MESH_TRANSFORM) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) t[k] = mapply_pos_x(mesh.trans, t[k]);
+    }
+    const bool flip = (mesh.flags & T3_MESH_FLIP_ORDER) != 0;
+    v[0] = flip ? t[2] : t[0];
+    v[1] = t[1];
+    v[2] = flip ? t[0] : t[2];
+  } else {
+    face_verts(mesh, face_ref(mesh, n), v);
+  }
+}
+
+// Cooperative 16-byte loads of the block's face-soup positions into shared memory.
+template <int BLOCK>
+__device__ __forceinline__ bool stage_soup(const t3_mesh& mesh, int64_t nfaces, int64_t f0, float* sv) {
+  const bool staged = mesh.kind == T3_MESH_SOUP && !(mesh.flags & T3_MESH_NOCULL);
+  if (staged) {
+    const int64_t rem = nfaces - f0;
+    const int nf = rem < BLOCK ? (int)(rem > 0 ? rem : 0) : BLOCK;
+    const float* src = mesh.verts + f0 * 9;
+    const int nflt = nf * 9;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+      const int n4 = nflt >> 2;
+      const float4* s4 = reinterpret_cast<const float4*>(src);
+      float4* d4 = reinterpret_cast<float4*>(sv);
+      for (int i = threadIdx.x; i < n4; i += BLOCK) d4[i] = __ldg(s4 + i);
+      for (int i = (n4 << 2) + threadIdx.x; i < nflt; i += BLOCK) sv[i] = __ldg(src + i);
+    } else {
+      for (int i = threadIdx.x; i < nflt; i += BLOCK) sv[i] = __ldg(src + i);
+    }
+  }
+  __syncthreads();
+  return staged;
+}
+
+} // namespace t3

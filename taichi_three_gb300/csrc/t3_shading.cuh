@@ -1,0 +1,280 @@
+// t3_shading.cuh -- per-pixel deferred shading shared by the direct shade kernel
+// and the binned tile kernel.
+//
+// Shader.shade_color (tina/core/shader.py:119-131) with calc_view_ray
+// (shader.py:82-93), Lighting.shade_color (tina/core/lighting.py:84-98), the
+// material BRDFs (tina/matr/material.py) and the ACES epilogue
+// (tina/advans.py:32-34).  Materials arrive flattened into weighted lobes; node
+// values are evaluated on the fly from the read-only node table (FRESNEL over
+// leaf nodes, everything else a leaf), so no per-thread node array is kept.
+#pragma once
+
+#include "t3_internal.cuh"
+
+namespace t3 {
+
+struct V3 { float x, y, z; };
+__device__ __forceinline__ V3 v3(float a, float b, float c) { return V3{a, b, c}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ V3 normalized(V3 a) { return rsqrtf(dot(a, a)) * a; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ V3 one_minus(V3 a) { return v3(1.0f - a.x, 1.0f - a.y, 1.0f - a.z); }
+__device__ __forceinline__ V3 tov(f3 a) { return v3(a.x, a.y, a.z); }
+
+__device__ __forceinline__ float aces(float c) {
+  return (c * (2.51f * c + 0.03f)) / (c * (2.43f * c + 0.59f) + 0.14f);
+}
+
+__device__ __forceinline__ float ipowf(float x, int n) {
+  float result = 1.0f, base = x;
+  bool first = true;
+  while (n > 0) {
+    if (n & 1) { result = first ? base : result * base; first = false; }
+    n >>= 1;
+    if (n) base = base * base;
+  }
+  return result;
+}
+
+struct Frag {
+  V3 pos, normal;
+  f2 tex;
+  const float* attr;
+};
+
+// CONST / ATTR / INPUT node value (scalars broadcast to all three lanes)
+__device__ __forceinline__ V3 eval_leaf(const t3_node& nd, const Frag& fg) {
+  switch (nd.op) {
+  case T3_OP_CONST:
+    return nd.b == 3 ? v3(nd.v[0], nd.v[1], nd.v[2]) : v3(nd.v[0], nd.v[0], nd.v[0]);
+  case T3_OP_ATTR:
+    if (nd.b == 1) {
+      const float a = __ldg(fg.attr + nd.a);
+      return v3(a, a, a);
+    }
+    return v3(__ldg(fg.attr + nd.a), __ldg(fg.attr + nd.a + 1), __ldg(fg.attr + nd.a + 2));
+  case T3_OP_INPUT:
+    return nd.a == 0 ? fg.pos : nd.a == 1 ? v3(1.f, 1.f, 1.f) : nd.a == 2 ? fg.normal
+                                                                        : v3(fg.tex.x, fg.tex.y, 0.f);
+  default:
+    return v3(0.f, 0.f, 0.f);
+  }
+}
+
+// value of node i; FRESNEL f0 = metallic * albedo + (1 - metallic) * 0.16 * specular**2
+__device__ __forceinline__ V3 eval_value(const DevMaterial& m, int i, const Frag& fg) {
+  const t3_node nd = m.nodes[i];
+  if (nd.op == T3_OP_FRESNEL) {
+    const V3 met = eval_leaf(m.nodes[nd.a], fg), alb = eval_leaf(m.nodes[nd.b], fg);
+    const V3 spc = eval_leaf(m.nodes[nd.c], fg);
+    return met * alb + (one_minus(met) * v3(0.16f, 0.16f, 0.16f)) * (spc * spc);
+  }
+  return eval_leaf(nd, fg);
+}
+
+struct LobeState {
+  int kind[T3_MAX_LOBES];
+  V3 w[T3_MAX_LOBES];   // lobe weight
+  V3 f0[T3_MAX_LOBES];  // COOK fresnel
+  float a2[T3_MAX_LOBES], k[T3_MAX_LOBES], gnorm[T3_MAX_LOBES];
+  float m[T3_MAX_LOBES];
+  int ipow[T3_MAX_LOBES];
+  int n;
+};
+
+__device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag& fg, V3 viewdir,
+                                              LobeState& L, V3& ambient, V3& emission) {
+  L.n = mat.nlobes;
+  ambient = v3(0.f, 0.f, 0.f);
+  emission = v3(0.f, 0.f, 0.f);
+  const float NoV = fmaxf(1e-10f, dot(viewdir, fg.normal));
+#pragma unroll
+  for (int k = 0; k < T3_MAX_LOBES; k++) {
+    L.kind[k] = -1;
+    if (k >= L.n) continue;
+    const DevLobe lb = mat.lobes[k];
+    V3 w = v3(1.f, 1.f, 1.f);
+    for (int j = 0; j < lb.nfac; j++) {
+      const V3 f = eval_value(mat, lb.fac[j] & 0xFFFF, fg);
+      w = w * ((lb.fac[j] & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
+    }
+    L.kind[k] = lb.kind;
+    if (lb.kind == T3_OP_EMISSION) emission = emission + w;
+    else ambient = ambient + w;
+    if (lb.kind == T3_OP_COOK) {
+      // per-pixel parts of CookTorrance.sub_brdf (material.py:323-357)
+      const float r = eval_value(mat, lb.p0, fg).x;
+      const float a2 = fmaxf(1e-6f, r * r);
+      const float kk = a2 * 0.5f;
+      L.a2[k] = a2;
+      L.k[k] = kk;
+      const float gv = 1.0f / ((NoV * kk + 1.0f) - kk);
+      L.gnorm[k] = gv / (1.0f * (1.0f - a2) + 12.566370614359172f * a2);
+      L.f0[k] = eval_value(mat, lb.p1, fg);
+    } else if (lb.kind == T3_OP_PHONG) {
+      L.m[k] = eval_value(mat, lb.p0, fg).x;
+      L.ipow[k] = lb.int_pow;
+    }
+    L.w[k] = w;
+  }
+}
+
+// sum_k W_k * brdf_k(n, L, V)
+__device__ __forceinline__ V3 eval_brdf(const LobeState& L, V3 n, V3 ldir, V3 vdir) {
+  V3 acc = v3(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < T3_MAX_LOBES; k++) {
+    if (L.kind[k] == T3_OP_LAMBERT) {
+      acc = acc + 0.31830988618379067f * L.w[k];
+    } else if (L.kind[k] == T3_OP_COOK) {
+      const V3 half = normalized(ldir + vdir);
+      const float NoH = fmaxf(1e-10f, dot(half, n));
+      const float NoL = fmaxf(1e-10f, dot(ldir, n));
+      const float VoH = fminf(1.0f, fmaxf(1e-10f, dot(half, vdir)));
+      const float a2 = L.a2[k];
+      const float denom = 1.0f - (NoH * NoH) * (1.0f - a2);
+      const float ndf = __fdividef(a2, denom * denom);
+      const float vdf = __fdividef(L.gnorm[k], (NoL * L.k[k] + 1.0f) - L.k[k]);
+      const float om = 1.0f - VoH;
+      const float om2 = om * om;
+      const float p5 = om * (om2 * om2);
+      const V3 f0 = L.f0[k];
+      const V3 fdf = f0 + p5 * one_minus(f0);
+      acc = acc + (vdf * ndf) * (L.w[k] * fdf);
+    } else if (L.kind[k] == T3_OP_PHONG) {
+      // reflect(-L, n) = -L - 2 (n . -L) n
+      const V3 I = v3(-ldir.x, -ldir.y, -ldir.z);
+      const V3 rdir = I - (2.0f * dot(n, I)) * n;
+      const float VoR = fmaxf(0.0f, dot(vdir, rdir));
+      const float m = L.m[k];
+      const float p = L.ipow[k] > 0 ? ipowf(VoR, L.ipow[k]) : powf(VoR, m);
+      acc = acc + ((p * (m + 2.0f)) * 0.5f) * L.w[k];
+    }
+  }
+  return acc;
+}
+
+// Shades pixel (x, y) from its packed (depth, id) key and writes every output.
+// `rec` (nullable) holds the rasteriser's setup records (64 bytes per face id);
+// without it the face setup is recomputed, bit-identically.
+__device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
+                                                     const float4* __restrict__ rec,
+                                                     unsigned long long key, int x, int y,
+                                                     const t3_outputs& out) {
+  const t3_frame& fr = sc->frame;
+  const int H = fr.height;
+  const int64_t i = (int64_t)x * H + y;
+  // the object owning this face id (-1: empty pixel, or an id no object owns)
+  int o = -1;
+  if (key != T3_EMPTY_KEY) {
+    const int64_t gid = (int64_t)(uint32_t)key;
+    const int nobj = sc->nobjects;
+    for (int j = 0; j < nobj; j++) {
+      if (gid >= sc->obj[j].face_base && gid < sc->obj[j].face_base + sc->obj[j].nfaces) o = j;
+    }
+  }
+  V3 color;
+  int32_t fid = -1, depth = fr.maxdepth;
+  float depth_f = __int_as_float(0x7f800000);
+  if (o < 0) {
+    color = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
+  } else {
+    const uint32_t gid = (uint32_t)key;
+    fid = (int32_t)gid;
+    depth = (int32_t)((uint32_t)(key >> 32) ^ 0x80000000u);
+    const DevObject& ob = sc->obj[o];
+    const t3_mesh& mesh = ob.mesh;
+    const int64_t n = (int64_t)gid - ob.face_base;
+    const FaceRef ref = face_ref(mesh, n);
+    f3 v[3];
+    face_verts(mesh, ref, v);
+    Setup s;
+    if (rec) {
+      const float4* r = rec + (size_t)gid * 4;
+      const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+      s.bx = a.x; s.by = a.y; s.cx = a.z; s.cy = a.w;
+      s.bcnx = b.x; s.bcny = b.y; s.canx = b.z; s.cany = b.w;
+      s.wsa = c.x; s.wsb = c.y; s.wsc = c.z; s.Az = c.w;
+      s.Bz = d.x; s.Cz = d.y;
+    } else {
+      face_setup(fr, v, s);
+    }
+    const float px = xadd((float)x, fr.bias[0]), py = xadd((float)y, fr.bias[1]);
+    const f3 wei = face_weights(s, px, py);
+    depth_f = face_depth(s, wei);
+
+    // interpolate (triangle.py:32-49)
+    Frag fg;
+    const V3 A = tov(v[0]), B = tov(v[1]), C = tov(v[2]);
+    fg.pos = (wei.x * A + wei.y * B) + wei.z * C;
+    V3 nrm;
+    if (fr.flags & T3_SMOOTHING) {
+      f3 nn[3];
+      face_norms(mesh, ref, nn);
+      nrm = (wei.x * tov(nn[0]) + wei.y * tov(nn[1])) + wei.z * tov(nn[2]);
+    } else {
+      nrm = cross(B - A, C - A);
+    }
+    fg.normal = normalized(nrm);
+    fg.tex = f2{0.f, 0.f};
+    if (fr.flags & T3_TEXTURING) {
+      f2 t[3];
+      face_coors(mesh, ref, t);
+      fg.tex = f2{(wei.x * t[0].x + wei.y * t[1].x) + wei.z * t[2].x,
+                  (wei.x * t[0].y + wei.y * t[1].y) + wei.z * t[2].y};
+    }
+    fg.attr = mesh.face_attr ? mesh.face_attr + ref.f * mesh.attr_stride : nullptr;
+    // calc_viewdir (shader.py:82-93)
+    const float ux = __fdividef(px, (float)fr.width) * 2.0f - 1.0f;
+    const float uy = __fdividef(py, (float)H) * 2.0f - 1.0f;
+    const float* M = fr.V2W;
+    // mapply_pos(V2W, (u, -1)) and (u, +1), then the difference of the two
+    const float bx = M[3] + M[0] * ux + M[1] * uy, by = M[7] + M[4] * ux + M[5] * uy;
+    const float bz = M[11] + M[8] * ux + M[9] * uy, bw = M[15] + M[12] * ux + M[13] * uy;
+    const float w0 = 1.0f / (bw - M[14]), w1 = 1.0f / (bw + M[14]);
+    const V3 ro = v3((bx - M[2]) * w0, (by - M[6]) * w0, (bz - M[10]) * w0);
+    const V3 ro1 = v3((bx + M[2]) * w1, (by + M[6]) * w1, (bz + M[10]) * w1);
+    const V3 rd = normalized(ro1 - ro);
+    const V3 vdir = v3(-rd.x, -rd.y, -rd.z);
+
+    LobeState L;
+    V3 amb, emi;
+    eval_material(ob.mat, fg, vdir, L, amb, emi);
+
+    // Lighting.shade_color (lighting.py:84-98)
+    const t3_lighting& lt = sc->lighting;
+    color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
+    const int nl = lt.nlights;
+    for (int l = 0; l < nl; l++) {
+      const float4 ld = *reinterpret_cast<const float4*>(lt.lights[l].dir);
+      V3 ldir = v3(ld.x - fg.pos.x * ld.w, ld.y - fg.pos.y * ld.w, ld.z - fg.pos.z * ld.w);
+      const float d2 = dot(ldir, ldir);
+      const float inv_d = rsqrtf(d2);
+      ldir = inv_d * ldir;
+      const float cos_i = dot(fg.normal, ldir);
+      if (cos_i > 0.0f) {
+        const float4 lc = *reinterpret_cast<const float4*>(lt.lights[l].color);
+        const float s = cos_i * (inv_d * inv_d);
+        const V3 mcol = eval_brdf(L, fg.normal, ldir, vdir);
+        color = color + v3(s * lc.x, s * lc.y, s * lc.z) * mcol;
+      }
+    }
+  }
+  if (fr.flags & T3_TONEMAP) color = v3(aces(color.x), aces(color.y), aces(color.z));
+  if (out.rgb) {
+    out.rgb[3 * i] = color.x;
+    out.rgb[3 * i + 1] = color.y;
+    out.rgb[3 * i + 2] = color.z;
+  }
+  if (out.face_id) out.face_id[i] = fid;
+  if (out.depth) out.depth[i] = depth;
+  if (out.depth_f) out.depth_f[i] = depth_f;
+}
+
+} // namespace t3

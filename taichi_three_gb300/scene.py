@@ -152,7 +152,9 @@ class Scene:
 
     Options kept from the reference: smoothing, texturing, culling, clipping,
     maxfaces, tonemap (default True), bgcolor (default 0).  Extension options:
-    raster ('direct' | 'binned'), tile (8 | 16 | 32), bin_capacity.  taa, ssr,
+    raster ('direct' | 'binned'), tile (8 | 16 | 32), bin_capacity (entries
+    per tile bin, 0 = automatic), check_bins (re-render with doubled bins when
+    a bin overflowed; default True).  taa, ssr,
     ssao, fxaa and blooming are outside this rasteriser build; ibl selects
     SkyboxLighting.
     """
@@ -172,6 +174,8 @@ class Scene:
             raise ValueError(f"raster must be one of {list(RASTER_MODES)}")
         self.tile = int(options.get('tile', 16))
         self.bin_capacity = int(options.get('bin_capacity', 0))
+        # read the device status after each binned frame and grow overflowing bins
+        self.check_bins = bool(options.get('check_bins', True))
         if self.ibl:
             from .skybox import SkyboxLighting
             self.lighting = options.get('lighting') or SkyboxLighting()
@@ -278,9 +282,23 @@ class Scene:
         outs.face_id = self.face_id.data_ptr()
         outs.depth = self.engine.depth.data_ptr()
         outs.depth_f = self.depth_f.data_ptr()
-        N.check(lib.t3_render(C.byref(sc), mode, self.tile, self.bin_capacity, self._ws.data_ptr(),
-                              self._ws.numel(), self._status.data_ptr(), C.byref(outs), _stream()),
-                't3_render')
+        for _attempt in range(8):
+            N.check(lib.t3_render(C.byref(sc), mode, self.tile, self.bin_capacity,
+                                  self._ws.data_ptr(), self._ws.numel(), self._status.data_ptr(),
+                                  C.byref(outs), _stream()), 't3_render')
+            if mode != N.T3_RASTER_BINNED or not self.check_bins:
+                break
+            # a bin that overflowed drops faces: retry with twice the capacity
+            if not (self.status() & N.T3_STATUS_BIN_OVERFLOW):
+                break
+            cap = C.c_int64()
+            N.check(lib.t3_bin_capacity(C.byref(sc), self.tile, self.bin_capacity, C.byref(cap)),
+                    't3_bin_capacity')
+            self.bin_capacity = 2 * cap.value
+            N.check(lib.t3_workspace_size(C.byref(sc), mode, self.tile, self.bin_capacity,
+                                          C.byref(size)), 't3_workspace_size')
+            if self._ws.numel() < size.value:
+                self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
         self._keep = keep
         self._last_scene = sc
 

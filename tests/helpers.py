@@ -33,6 +33,7 @@ def flat_scene(tris, W=8, H=8, z=None, material=None, **options):
 
 
 def random_soup_scene(seed, ntri=300, res=(64, 48), material='pbr', nlights=3, **options):
+    """Seeded PBR / Classic soup (moderately large faces) for parity tests."""
     verts, norms, attrs = tina.workloads.soup_arrays(ntri, seed, median_sigma=0.08, log_sd=0.6)
     scene, mesh = tina.workloads.soup_scene(ntri=ntri, res=res, seed=seed, material=material,
                                             nlights=nlights, arrays=(verts, norms, attrs), **options)

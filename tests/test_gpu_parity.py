@@ -63,9 +63,33 @@ def test_sphere_default_lights_and_ambient(cuda, oracle_mod):
     assert_parity(gpu_render(scene), oracle_mod.render(scene))
 
 
+RASTERS = [dict(raster='direct'), dict(raster='binned', tile=8), dict(raster='binned', tile=16),
+           dict(raster='binned', tile=32)]
+
+
 @pytest.mark.parametrize('seed,material', [(1, 'pbr'), (2, 'classic'), (3, 'pbr'), (4, 'classic')])
-def test_random_soups(cuda, oracle_mod, seed, material):
-    scene, _ = random_soup_scene(seed, ntri=3000, res=(160, 96), material=material, nlights=4)
+@pytest.mark.parametrize('rast', RASTERS, ids=lambda r: '-'.join(map(str, r.values())))
+def test_random_soups(cuda, oracle_mod, seed, material, rast):
+    scene, _ = random_soup_scene(seed, ntri=3000, res=(160, 96), material=material, nlights=4,
+                                 **rast)
+    assert_parity(gpu_render(scene), oracle_mod.render(scene))
+
+
+@pytest.mark.parametrize('rast', RASTERS[1:], ids=lambda r: 'tile%d' % r['tile'])
+def test_binned_bins_overflow_then_grow(cuda, oracle_mod, rast):
+    # 4-entry bins overflow; Scene.render sees the status bit and re-renders
+    scene, _ = random_soup_scene(12, ntri=4000, res=(128, 96), bin_capacity=4, **rast)
+    g = gpu_render(scene)
+    assert scene.bin_capacity > 4
+    assert_parity(g, oracle_mod.render(scene))
+    assert not (scene.status() & tina._native.T3_STATUS_BIN_OVERFLOW)
+
+
+@pytest.mark.parametrize('rast', RASTERS, ids=lambda r: '-'.join(map(str, r.values())))
+def test_big_faces_and_multi_object_per_mode(cuda, oracle_mod, rast):
+    scene, _ = flat_scene([[(-20, -20), (300, -20), (-20, 300)], [(5, 5), (200, 30), (40, 190)],
+                           [(100, 100), (104, 101), (101, 106)]],
+                          W=256, H=200, z=[0.6, 0.4, 0.3], clipping=False, **rast)
     assert_parity(gpu_render(scene), oracle_mod.render(scene))
 
 
@@ -116,9 +140,10 @@ def test_large_faces_take_the_queue_path(cuda, oracle_mod):
     assert_parity(gpu_render(scene), oracle_mod.render(scene))
 
 
-def test_mesh_edits_and_multi_object(cuda, oracle_mod):
+@pytest.mark.parametrize('rast', [RASTERS[0], RASTERS[2]], ids=['direct', 'binned16'])
+def test_mesh_edits_and_multi_object(cuda, oracle_mod, rast):
     verts, norms, attrs = tina.workloads.soup_arrays(1200, 9, median_sigma=0.1)
-    scene = tina.Scene(120, 90, smoothing=True)
+    scene = tina.Scene(120, 90, smoothing=True, **rast)
     base = tina.SimpleMesh()
     base.set_face_verts(verts)
     base.set_face_norms(norms)
@@ -194,10 +219,11 @@ def test_tonemap_kernel(cuda, oracle_mod):
     assert np.abs(y.cpu().numpy() - ref).max() < 1e-6
 
 
-def test_full_size_soup_1080p(cuda, oracle_mod):
+@pytest.mark.parametrize('rast', [RASTERS[0], RASTERS[2]], ids=['direct', 'binned16'])
+def test_full_size_soup_1080p(cuda, oracle_mod, rast):
     """1,000,000-face PBR soup at 1920x1080 with 8 point lamps: bit-exact id and
     depth against the oracle (its OpenMP mode, which equals the serial one)."""
-    scene, _ = tina.workloads.soup_scene()
+    scene, _ = tina.workloads.soup_scene(**rast)
     g = gpu_render(scene)
     o = oracle_mod.render(scene, mode=1)
     assert (o['face_id'] >= 0).mean() > 0.3
