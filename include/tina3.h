@@ -183,6 +183,12 @@ int t3_workspace_size(const t3_scene* scene, int mode, int tile,
  * reference, whose rasteriser has no bins. */
 int t3_bin_capacity(const t3_scene* scene, int tile, int64_t bin_capacity, int64_t* capacity);
 
+/* Largest per-tile bin count of the last binned frame rendered with this
+ * workspace (synchronises `stream`): the capacity a re-render needs after
+ * T3_STATUS_BIN_OVERFLOW.  No counterpart in the reference. */
+int t3_bin_counts_max(const t3_scene* scene, int tile, int64_t bin_capacity, const void* workspace,
+                      size_t workspace_bytes, int64_t* max_count, void* stream);
+
 /* Engine.clear_depth (tina/core/engine.py:68-70) for the packed buffer:
  * depth_id[W*H] = empty key. */
 int t3_clear(uint64_t* depth_id, int64_t npixels, void* stream);

@@ -103,6 +103,8 @@ SIGNATURES = {
                                     C.POINTER(C.c_size_t)]),
     "t3_clear": (C.c_int, [_VP, _I64, _VP]),
     "t3_bin_capacity": (C.c_int, [C.POINTER(t3_scene), C.c_int, _I64, C.POINTER(C.c_int64)]),
+    "t3_bin_counts_max": (C.c_int, [C.POINTER(t3_scene), C.c_int, _I64, _VP, _SZ,
+                                    C.POINTER(C.c_int64), _VP]),
     "t3_raster": (C.c_int, [C.POINTER(t3_frame), C.POINTER(t3_object), _VP, _VP, _SZ, _VP, _VP]),
     "t3_shade": (C.c_int, [C.POINTER(t3_scene), _VP, _VP, _SZ, C.POINTER(t3_outputs), _VP]),
     "t3_render": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,

@@ -6,6 +6,7 @@
 //   upload scene + zero counters -> clear keys -> per object: raster (+ big
 //   faces) -> shade (+ tonemap).
 // No entry point allocates device memory; every buffer is caller-owned.
+#include <cstdlib>
 #include <cstring>
 
 #include "t3_internal.cuh"
@@ -374,6 +375,29 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
   }
   if (e == cudaSuccess) e = mark(3);
   return cuda_rc(e);
+}
+
+int t3_bin_counts_max(const t3_scene* scene, int tile, int64_t bin_capacity, const void* workspace,
+                      size_t workspace_bytes, int64_t* max_count, void* stream) {
+  if (!scene || !workspace || !max_count) return T3_EINVAL;
+  Layout L;
+  int r = layout_for(*scene, T3_RASTER_BINNED, tile, bin_capacity, L);
+  if (r) return r;
+  if (workspace_bytes < L.end) return T3_EINVAL;
+  const int ntiles = L.tiles_x * L.tiles_y;
+  uint32_t* counts = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)ntiles);
+  if (!counts) return T3_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint8_t* ws = reinterpret_cast<const uint8_t*>(workspace);
+  cudaError_t e = cudaMemcpyAsync(counts, ws + L.counters + 64 * sizeof(uint32_t),
+                                  sizeof(uint32_t) * (size_t)ntiles, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  int64_t m = 0;
+  for (int i = 0; i < ntiles && e == cudaSuccess; i++) m = counts[i] > m ? counts[i] : m;
+  free(counts);
+  if (e != cudaSuccess) return T3_ECUDA;
+  *max_count = m;
+  return T3_OK;
 }
 
 int t3_event_create(void** event) {

@@ -282,19 +282,21 @@ class Scene:
         outs.face_id = self.face_id.data_ptr()
         outs.depth = self.engine.depth.data_ptr()
         outs.depth_f = self.depth_f.data_ptr()
-        for _attempt in range(8):
+        for _attempt in range(3):
             N.check(lib.t3_render(C.byref(sc), mode, self.tile, self.bin_capacity,
                                   self._ws.data_ptr(), self._ws.numel(), self._status.data_ptr(),
                                   C.byref(outs), _stream()), 't3_render')
             if mode != N.T3_RASTER_BINNED or not self.check_bins:
                 break
-            # a bin that overflowed drops faces: retry with twice the capacity
+            # a bin that overflowed dropped faces: re-render with bins sized from
+            # the counts this frame reached
             if not (self.status() & N.T3_STATUS_BIN_OVERFLOW):
                 break
-            cap = C.c_int64()
-            N.check(lib.t3_bin_capacity(C.byref(sc), self.tile, self.bin_capacity, C.byref(cap)),
-                    't3_bin_capacity')
-            self.bin_capacity = 2 * cap.value
+            need = C.c_int64()
+            N.check(lib.t3_bin_counts_max(C.byref(sc), self.tile, self.bin_capacity,
+                                          self._ws.data_ptr(), self._ws.numel(), C.byref(need),
+                                          _stream()), 't3_bin_counts_max')
+            self.bin_capacity = ((need.value * 5 // 4 + 32) + 31) // 32 * 32
             N.check(lib.t3_workspace_size(C.byref(sc), mode, self.tile, self.bin_capacity,
                                           C.byref(size)), 't3_workspace_size')
             if self._ws.numel() < size.value:
