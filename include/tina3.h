@@ -236,6 +236,29 @@ int t3_event_create(void** event);
 int t3_event_destroy(void* event);
 int t3_event_elapsed_ms(void* start, void* end, float* ms); /* waits for `end` */
 
+/* Limits of t3_render_noalloc's built-in scratch array. */
+#define T3_NOALLOC_MAX_PIXELS (1u << 21)      /* 2,097,152 px: covers 1920x1080 */
+#define T3_NOALLOC_MAX_BIG_FACES (1u << 16)   /* faces with bbox > 4096 px per frame */
+/* scene copy (16 KiB) + counters (256 B) + large-face queue + depth keys */
+#define T3_NOALLOC_SCRATCH_BYTES \
+  (16384u + 256u + 4u * T3_NOALLOC_MAX_BIG_FACES + 8u * T3_NOALLOC_MAX_PIXELS)
+
+/* t3_render (direct mode) for callers that cannot allocate device memory --
+ * code running inside a host application that owns the GPU's memory and hands
+ * the renderer only its buffers.  No counterpart in the reference, which has
+ * no allocation-free entry point.  The caller passes the scene, a device status
+ * word and the outputs; the scratch (depth keys, counters, large-face queue,
+ * scene copy) is a fixed device array inside the library,
+ * T3_NOALLOC_SCRATCH_BYTES (17,056,000 bytes, about 16.3 MiB),
+ * held by every GPU that loads the library until the process exits.  Limits:
+ * width * height <= T3_NOALLOC_MAX_PIXELS (else T3_ETOOBIG); at most
+ * T3_NOALLOC_MAX_BIG_FACES faces with a bbox above 4096 px per frame (more set
+ * T3_STATUS_BIG_OVERFLOW in *status and those faces are dropped).  The first
+ * call on each device looks the array's address up (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
+int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* out, void* stream);
+
 /* Reads back the device status word written by the last t3_raster/t3_render
  * (synchronises `stream`). */
 int t3_read_status(const int32_t* status, int32_t* host_status, void* stream);

@@ -27,6 +27,8 @@ T3_MAX_LIGHTS = 16
 T3_MAX_NODES = 24
 T3_MAX_OBJECTS = 8
 T3_MAXDEPTH = 1 << 30
+T3_NOALLOC_MAX_PIXELS = 1 << 21
+T3_NOALLOC_MAX_BIG_FACES = 1 << 16
 
 T3_CULLING, T3_CLIPPING, T3_SMOOTHING, T3_TEXTURING, T3_TONEMAP = 1, 2, 4, 8, 16
 T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED = 0, 1, 2
@@ -114,6 +116,7 @@ SIGNATURES = {
     "t3_tonemap": (C.c_int, [_VP, _I64, _VP]),
     "t3_render_staged": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,
                                    C.POINTER(t3_outputs), _VP, C.POINTER(C.c_void_p)]),
+    "t3_render_noalloc": (C.c_int, [C.POINTER(t3_scene), _VP, C.POINTER(t3_outputs), _VP]),
     "t3_event_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "t3_event_destroy": (C.c_int, [_VP]),
     "t3_event_elapsed_ms": (C.c_int, [_VP, _VP, C.POINTER(C.c_float)]),

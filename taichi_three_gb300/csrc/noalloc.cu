@@ -1,0 +1,88 @@
+// noalloc.cu -- t3_render_noalloc: one frame of the direct rasteriser whose
+// scratch memory is a fixed device array inside this library.
+//
+// Who needs it: code that renders inside a host application which owns the
+// GPU's memory and hands the renderer only its input and output buffers -- a
+// plug-in or frame callback that must not call cudaMalloc (the host forbids
+// allocations in its frame loop, or an allocation there could block or fail
+// at an unpredictable moment).  t3_render needs a caller-allocated workspace;
+// this entry point needs none.
+//
+// The scratch (scene copy, counters, large-face queue and the packed depth key
+// buffer) lives in `g_noalloc_scratch`, a file-scope __device__ array of
+// T3_NOALLOC_SCRATCH_BYTES (17,056,000 bytes, about 16.3 MiB).  Every GPU that loads the library
+// holds that array until the process exits.  In host code the array's name is
+// only a host-side stand-in, so the first call on each device (with that
+// device current) looks up its device address with cudaGetSymbolAddress and
+// caches it; make that first call before any stream capture.  Each call
+// clears what must start empty (counters, status word, key buffer).  All calls
+// share the one array: calls whose work overlaps on the GPU (other streams,
+// other host threads) race on it and must be serialised by the caller.
+#include <mutex>
+
+#include "t3_internal.cuh"
+
+namespace t3 {
+
+constexpr size_t kNoallocScene = 0;
+constexpr size_t kNoallocCounters = 16384;
+static_assert(sizeof(DevScene) <= kNoallocCounters, "scene copy outgrew its scratch region");
+constexpr size_t kNoallocBig = kNoallocCounters + 256;
+constexpr size_t kNoallocKeys = kNoallocBig + 4 * (size_t)T3_NOALLOC_MAX_BIG_FACES;
+constexpr size_t kNoallocBytes = kNoallocKeys + 8 * (size_t)T3_NOALLOC_MAX_PIXELS;
+static_assert(kNoallocBytes == T3_NOALLOC_SCRATCH_BYTES, "scratch size in tina3.h is stale");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[64];  // per device ordinal
+
+// device address of g_noalloc_scratch on the current device (looked up once)
+static int noalloc_scratch(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return T3_ECUDA;
+  if (dev < 0 || dev >= 64) return T3_EUNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return T3_ECUDA;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return T3_OK;
+}
+
+} // namespace t3
+
+using namespace t3;
+
+extern "C" int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* out,
+                                 void* stream) {
+  if (!scene || !status || !out || !out->rgb) return T3_EINVAL;
+  const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
+  if (scene->frame.width <= 0 || scene->frame.height <= 0) return T3_EINVAL;
+  if (npix > (int64_t)T3_NOALLOC_MAX_PIXELS) return T3_ETOOBIG;
+  static thread_local DevScene ds;
+  int r = make_dev_scene(*scene, ds);
+  if (r) return r;
+  void* base = nullptr;
+  r = noalloc_scratch(&base);
+  if (r) return r;
+  uint8_t* ws = reinterpret_cast<uint8_t*>(base);
+  cudaStream_t st = (cudaStream_t)stream;
+  DevScene* dsc = reinterpret_cast<DevScene*>(ws + kNoallocScene);
+  uint32_t* counters = reinterpret_cast<uint32_t*>(ws + kNoallocCounters);
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + kNoallocKeys);
+  cudaError_t e = launch_upload_scene(ds, dsc, counters, 64, status, st);
+  if (e == cudaSuccess) e = launch_clear(keys, npix, st);
+  for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
+    BigQueue big;
+    big.items = reinterpret_cast<uint32_t*>(ws + kNoallocBig);
+    big.capacity = T3_NOALLOC_MAX_BIG_FACES;
+    big.count = counters + o;
+    big.status = status;
+    e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
+  }
+  if (e == cudaSuccess) e = launch_shade(dsc, scene->frame, keys, *out, st);
+  return e == cudaSuccess ? T3_OK : T3_ECUDA;
+}
