@@ -152,6 +152,12 @@ int make_dev_scene(const t3_scene& sc, DevScene& out) {
   return T3_OK;
 }
 
+int max_lobes(const DevScene& sc) {
+  int m = 1;
+  for (int o = 0; o < sc.nobjects; o++) m = sc.obj[o].mat.nlobes > m ? sc.obj[o].mat.nlobes : m;
+  return m;
+}
+
 static int64_t max_object_faces(const t3_scene& sc) {
   int64_t m = 0;
   for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
@@ -170,9 +176,9 @@ static int64_t total_faces(const t3_scene& sc) {
 //   counters  uint32[64 + ntiles]: per-object big-face counts, big-list count,
 //             tile bin counts -- zeroed by the scene upload every frame
 //   big       uint32[big_capacity] big-face ids
+//   rec       float4[4 * total_faces] setup records of the visible faces
 //   direct:   keys  uint64[W*H] packed (depth, id)
-//   binned:   rec   float4[4 * total_faces] setup records
-//             bins  uint32[ntiles * bin_capacity]
+//   binned:   bins  uint32[ntiles * bin_capacity]
 struct Layout {
   size_t scene, counters, big, keys, rec, bins, end;
   int ncounters;
@@ -210,12 +216,13 @@ static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capaci
   L.big_capacity = (uint32_t)cap;
   L.big = align256(L.counters + 4 * (size_t)L.ncounters);
   const size_t after_big = align256(L.big + 4 * (size_t)cap);
+  L.rec = after_big;
+  const size_t after_rec = align256(L.rec + 64 * (size_t)(total_faces(sc) > 0 ? total_faces(sc) : 1));
   if (mode == T3_RASTER_BINNED) {
-    L.rec = after_big;
-    L.bins = align256(L.rec + 64 * (size_t)(total_faces(sc) > 0 ? total_faces(sc) : 1));
+    L.bins = after_rec;
     L.end = align256(L.bins + 4 * (size_t)L.tiles_x * L.tiles_y * L.bin_capacity);
   } else {
-    L.keys = after_big;
+    L.keys = after_rec;
     L.end = align256(L.keys + 8 * (size_t)sc.frame.width * (size_t)sc.frame.height);
   }
   return T3_OK;
@@ -289,6 +296,7 @@ int t3_raster(const t3_frame* frame, const t3_object* object, uint64_t* depth_id
   big.items = reinterpret_cast<uint32_t*>(ws + 256);
   big.capacity = (uint32_t)(object->nfaces > 0 ? object->nfaces : 1);
   big.status = status;
+  big.rec = nullptr;
   cudaError_t e = cudaMemsetAsync(big.count, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return T3_ECUDA;
   return cuda_rc(launch_raster_direct(*frame, *object, reinterpret_cast<unsigned long long*>(depth_id),
@@ -308,7 +316,7 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
   cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
   return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
-                              *out, st));
+                              nullptr, *out, max_lobes(ds), st));
 }
 
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
@@ -349,10 +357,13 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
       big.capacity = L.big_capacity;
       big.count = counters + o;
       big.status = status;
+      big.rec = reinterpret_cast<float4*>(ws + L.rec);
       e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
     }
     if (e == cudaSuccess) e = mark(2);
-    if (e == cudaSuccess) e = launch_shade(dsc, scene->frame, keys, *out, st);
+    if (e == cudaSuccess)
+      e = launch_shade(dsc, scene->frame, keys, reinterpret_cast<const float4*>(ws + L.rec), *out,
+                       max_lobes(ds), st);
   } else {
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -367,6 +378,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     b.tiles_x = L.tiles_x;
     b.tiles_y = L.tiles_y;
     b.big_tiles = 16;
+    b.max_lobes = max_lobes(ds);
     if (e == cudaSuccess) e = mark(1);
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++)
       e = launch_bin(scene->frame, scene->objects[o], b, st);

@@ -29,26 +29,6 @@
 
 namespace t3 {
 
-__device__ __forceinline__ void store_record(float4* __restrict__ rec, uint32_t gid, const Setup& s) {
-  float4* r = rec + (size_t)gid * 4;
-  r[0] = make_float4(s.bx, s.by, s.cx, s.cy);
-  r[1] = make_float4(s.bcnx, s.bcny, s.canx, s.cany);
-  r[2] = make_float4(s.wsa, s.wsb, s.wsc, s.Az);
-  r[3] = make_float4(s.Bz, s.Cz, __int_as_float(s.botx | (s.boty << 16)),
-                     __int_as_float(s.topx | (s.topy << 16)));
-}
-
-__device__ __forceinline__ void load_record(const float4* __restrict__ rec, uint32_t gid, Setup& s) {
-  const float4* r = rec + (size_t)gid * 4;
-  const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
-  s.bx = a.x; s.by = a.y; s.cx = a.z; s.cy = a.w;
-  s.bcnx = b.x; s.bcny = b.y; s.canx = b.z; s.cany = b.w;
-  s.wsa = c.x; s.wsb = c.y; s.wsc = c.z; s.Az = c.w;
-  s.Bz = d.x; s.Cz = d.y;
-  const int p0 = __float_as_int(d.z), p1 = __float_as_int(d.w);
-  s.botx = p0 & 0xFFFF; s.boty = p0 >> 16; s.topx = p1 & 0xFFFF; s.topy = p1 >> 16;
-}
-
 // ---- k_bin -------------------------------------------------------------------
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
@@ -136,8 +116,8 @@ struct SmemKeySink {
   int TS_DYN;
 };
 
-template <int TS, int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
+template <int TS, int BLOCK, int NL, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
 k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw);  // TS*TS
@@ -145,6 +125,8 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   __shared__ WarpFaces wfs[BLOCK / 32];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_ok;
+  __shared__ int s_list[TS * TS];
+  __shared__ int s_count;
 
   const t3_frame& fr = sc->frame;
   const int W = fr.width, H = fr.height;
@@ -158,6 +140,7 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
 
   if (threadIdx.x == 0) {
     s_ok = 1;
+    s_count = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar_a), "r"(1) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -220,11 +203,31 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   }
   __syncthreads();
 
-  // shade the tile: consecutive threads take consecutive y (contiguous memory)
-  for (int i = threadIdx.x; i < TS * TS; i += BLOCK) {
+  // shade the tile: empty pixels at once, covered ones compacted so full warps
+  // run the shading (consecutive threads take consecutive y: contiguous memory)
+  const V3 bg = background(fr);
+  const int lane = threadIdx.x & 31;
+  for (int i0 = 0; i0 < TS * TS; i0 += BLOCK) {
+    const int i = i0 + threadIdx.x;
     const int x = x0 + i / TS, y = y0 + i % TS;
-    if (x > x1 || y > y1) continue;
-    shade_pixel_from_key(sc, bins.rec, ok ? keys[i] : T3_EMPTY_KEY, x, y, out);
+    bool covered = false;
+    if (i < TS * TS && x <= x1 && y <= y1) {
+      if (!ok || keys[i] == T3_EMPTY_KEY) write_empty(fr, out, (int64_t)x * H + y, bg);
+      else covered = true;
+    }
+    const unsigned m = __ballot_sync(FULL, covered);
+    if (m) {
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
+      slot = __shfl_sync(FULL, slot, 0);
+      if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+  }
+  __syncthreads();
+  const int ncov = s_count;
+  for (int j = threadIdx.x; j < ncov; j += BLOCK) {
+    const int i = s_list[j];
+    shade_pixel_from_key<NL>(sc, bins.rec, keys[i], x0 + i / TS, y0 + i % TS, out);
   }
   if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(bar_a) : "memory");
 }
@@ -237,15 +240,31 @@ cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& b
   return cudaGetLastError();
 }
 
+template <int TS, int BLOCK, int NL, int MINB>
+static cudaError_t launch_tile_b(const DevScene* sc, const BinArgs& bins, int ntiles,
+                                 const t3_outputs& out, cudaStream_t st) {
+  const size_t smem = (size_t)TS * TS * 8 + (size_t)bins.capacity * 4;
+  cudaError_t e = cudaFuncSetAttribute(k_tile<TS, BLOCK, NL, MINB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_tile<TS, BLOCK, NL, MINB><<<ntiles, BLOCK, smem, st>>>(sc, bins, out);
+  return cudaGetLastError();
+}
+
+template <int TS, int BLOCK, int NL>
+static cudaError_t launch_tile_nl(const DevScene* sc, const BinArgs& bins, int ntiles,
+                                  const t3_outputs& out, cudaStream_t st) {
+  if (shade_min_blocks() == 3 && BLOCK == 256)
+    return launch_tile_b<TS, BLOCK, NL, 3>(sc, bins, ntiles, out, st);
+  return launch_tile_b<TS, BLOCK, NL, BLOCK == 256 ? 2 : 6>(sc, bins, ntiles, out, st);
+}
+
 template <int TS, int BLOCK>
 static cudaError_t launch_tile_t(const DevScene* sc, const BinArgs& bins, int ntiles,
                                  const t3_outputs& out, cudaStream_t st) {
-  const size_t smem = (size_t)TS * TS * 8 + (size_t)bins.capacity * 4;
-  cudaError_t e = cudaFuncSetAttribute(k_tile<TS, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  k_tile<TS, BLOCK><<<ntiles, BLOCK, smem, st>>>(sc, bins, out);
-  return cudaGetLastError();
+  if (bins.max_lobes <= 1) return launch_tile_nl<TS, BLOCK, 1>(sc, bins, ntiles, out, st);
+  if (bins.max_lobes == 2) return launch_tile_nl<TS, BLOCK, 2>(sc, bins, ntiles, out, st);
+  return launch_tile_nl<TS, BLOCK, 4>(sc, bins, ntiles, out, st);
 }
 
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,

@@ -59,6 +59,7 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
     vis = face_setup(fr, v, s) && s.botx <= s.topx && s.boty <= s.topy;
   }
   if (vis) {
+    if (big.rec) store_record(big.rec, face_base + (uint32_t)n, s);
     const int64_t area = (int64_t)(s.topx - s.botx + 1) * (int64_t)(s.topy - s.boty + 1);
     if (area > big_threshold) {
       const uint32_t slot = atomicAdd(big.count, 1u);

@@ -6,6 +6,8 @@
 // exactly as the rasteriser did (so depth_f is bit-exact), interpolates
 // position / normal / texcoord, evaluates the material once per pixel, then
 // sums the lamps and applies ACES.
+#include <cstdlib>
+
 #include "t3_shading.cuh"
 
 namespace t3 {
@@ -16,41 +18,102 @@ namespace t3 {
 __global__ void k_upload_scene(const DevScene sc, DevScene* __restrict__ dst,
                                uint32_t* __restrict__ counters, int ncounters,
                                int32_t* __restrict__ status) {
-  if (blockIdx.x == 0) {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(&sc);
-    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-    constexpr int nwords = (int)(sizeof(DevScene) / 4);
-    for (int i = threadIdx.x; i < nwords; i += blockDim.x) d[i] = src[i];
-    if (threadIdx.x == 0 && status) *status = 0;
-  }
+  // the descriptor is split across blocks: each block copies a 1 KB slice, so
+  // the constant-bank reads of the parameter run on many SMs at once
+  constexpr int nwords = (int)(sizeof(DevScene) / 4);
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(&sc);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  for (int i = blockIdx.x * 256 + threadIdx.x; i < nwords; i += gridDim.x * 256) d[i] = src[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && status) *status = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncounters; i += gridDim.x * blockDim.x)
     counters[i] = 0u;
 }
 
 cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
                                 int ncounters, int32_t* status, cudaStream_t st) {
+  constexpr int scene_blocks = (int)((sizeof(DevScene) / 4 + 255) / 256);
   int grid = (ncounters + 255) / 256;
-  grid = grid < 1 ? 1 : grid > 64 ? 64 : grid;
+  grid = grid < scene_blocks ? scene_blocks : grid > 64 ? 64 : grid;
   k_upload_scene<<<grid, 256, 0, st>>>(sc, dst, counters, ncounters, status);
   return cudaGetLastError();
 }
 
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
+// Each block owns PPT * BLOCK consecutive pixels.  Empty pixels are written as
+// background at once; covered ones are compacted into a shared list (warp
+// ballot + one shared atomic per warp) so that full warps run the shading.
+template <int BLOCK, int PPT, int NL, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
 k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
-        t3_outputs out, int64_t npix, int H) {
-  const int64_t i = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-  if (i >= npix) return;
-  const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
-  shade_pixel_from_key(sc, nullptr, keys[i], x, y, out);
+        const float4* __restrict__ rec, t3_outputs out, int64_t npix, int H) {
+  __shared__ int s_list[BLOCK * PPT];
+  __shared__ int s_count;
+  if (threadIdx.x == 0) s_count = 0;
+  __syncthreads();
+  const t3_frame& fr = sc->frame;
+  const int64_t base = (int64_t)blockIdx.x * BLOCK * PPT;
+  const V3 bg = background(fr);
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < PPT; k++) {
+    const int local = k * BLOCK + threadIdx.x;
+    const int64_t i = base + local;
+    bool covered = false;
+    if (i < npix) {
+      if (keys[i] == T3_EMPTY_KEY) write_empty(fr, out, i, bg);
+      else covered = true;
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
+    if (m) {
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
+      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+      if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = local;
+    }
+  }
+  __syncthreads();
+  const int n = s_count;
+  for (int j = threadIdx.x; j < n; j += BLOCK) {
+    const int64_t i = base + s_list[j];
+    const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
+    shade_pixel_from_key<NL>(sc, rec, keys[i], x, y, out);
+  }
+}
+
+// Resident blocks per SM the shade kernels are compiled for: 3 (default; more
+// warps to hide the gathers' latency, at the price of a few spills, measured
+// faster on the 1080p soup) or 2 (no spills; T3_SHADE_BLOCKS=2).  Read once.
+int shade_min_blocks() {
+  static int v = [] {
+    const char* e = getenv("T3_SHADE_BLOCKS");
+    return (e && e[0] == '2') ? 2 : 3;
+  }();
+  return v;
+}
+
+template <int NL, int MINB>
+static void launch_shade_t(const DevScene* sc_dev, const unsigned long long* keys,
+                           const float4* rec, const t3_outputs& out, int64_t npix, int H,
+                           cudaStream_t st) {
+  constexpr int BLOCK = 256, PPT = 4;
+  const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
+  k_shade<BLOCK, PPT, NL, MINB><<<(unsigned)grid, BLOCK, 0, st>>>(sc_dev, keys, rec, out, npix, H);
 }
 
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                         const t3_outputs& out, cudaStream_t st) {
-  constexpr int BLOCK = 256;
+                         const float4* rec, const t3_outputs& out, int max_lobes, cudaStream_t st) {
   const int64_t npix = (int64_t)fr.width * fr.height;
-  const int64_t grid = (npix + BLOCK - 1) / BLOCK;
-  k_shade<BLOCK><<<(unsigned)grid, BLOCK, 0, st>>>(sc_dev, keys, out, npix, fr.height);
+  const bool b3 = shade_min_blocks() == 3;
+  const int H = fr.height;
+  if (max_lobes <= 1) {
+    if (b3) launch_shade_t<1, 3>(sc_dev, keys, rec, out, npix, H, st);
+    else launch_shade_t<1, 2>(sc_dev, keys, rec, out, npix, H, st);
+  } else if (max_lobes == 2) {
+    if (b3) launch_shade_t<2, 3>(sc_dev, keys, rec, out, npix, H, st);
+    else launch_shade_t<2, 2>(sc_dev, keys, rec, out, npix, H, st);
+  } else {
+    if (b3) launch_shade_t<4, 3>(sc_dev, keys, rec, out, npix, H, st);
+    else launch_shade_t<4, 2>(sc_dev, keys, rec, out, npix, H, st);
+  }
   return cudaGetLastError();
 }
 

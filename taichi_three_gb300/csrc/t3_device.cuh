@@ -26,6 +26,8 @@ __device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+// 1 / b, correctly rounded: the same bits as xdiv(1.0f, b)
+__device__ __forceinline__ float xrcp(float b) { return __frcp_rn(b); }
 
 struct f2 { float x, y; };
 struct f3 { float x, y, z; };
@@ -71,7 +73,7 @@ __device__ __forceinline__ float dot_x(f3 a, f3 b) {
   return xadd(xadd(xmul(a.x, b.x), xmul(a.y, b.y)), xmul(a.z, b.z));
 }
 __device__ __forceinline__ f3 normalized_x(f3 a) {
-  float inv = xdiv(1.0f, __fsqrt_rn(dot_x(a, a)));
+  float inv = xrcp(__fsqrt_rn(dot_x(a, a)));
   return f3{xmul(inv, a.x), xmul(inv, a.y), xmul(inv, a.z)};
 }
 __device__ __forceinline__ float cross2_x(float ax, float ay, float bx, float by) {
@@ -188,6 +190,23 @@ __device__ __forceinline__ bool inside_clip(f3 p) {
          (-1.0f <= p.z && p.z <= 1.0f);
 }
 
+// The reference walks every pixel of [floor(min), ceil(max)] (triangle.py:108-114),
+// but a pixel whose centre c + 0.5 lies outside [min, max] by more than the
+// rounding error of the weights cannot pass the inside test: that error is a
+// few ulps of the viewport coordinates (|w| error <~ 2^-22 * (1 + |coord|)
+// in pixel units), far below the margin used here, 2^-16 * (2 + |coord| +
+// extent).  So only centres in [min - eps, max + eps] are tested, which halves
+// the pixel tests of small faces without changing which pixels are covered.
+__device__ __forceinline__ void tighten_to_centres(float lo, float hi, int32_t& bot, int32_t& top) {
+  const float mag = fmaxf(fabsf(lo), fabsf(hi));
+  if (!(mag < 16777216.0f)) return;  // also NaN / inf: keep the reference's range
+  const float eps = (2.0f + mag + (hi - lo)) * 1.52587890625e-05f;  // 2^-16
+  const int32_t b = (int32_t)ceilf(lo - 0.5f - eps);
+  const int32_t t = (int32_t)floorf(hi - 0.5f + eps);
+  bot = b > bot ? b : bot;
+  top = t < top ? t : top;
+}
+
 // returns false when the face is culled or clipped
 __device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Setup& s) {
   const float* W2V = fr.W2V;
@@ -215,15 +234,17 @@ __device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Se
   s.boty = loy > 0 ? loy : 0;
   s.topx = hix < fr.width - 1 ? hix : fr.width - 1;
   s.topy = hiy < fr.height - 1 ? hiy : fr.height - 1;
+  tighten_to_centres(fminf(fminf(ax, bx), cx), fmaxf(fmaxf(ax, bx), cx), s.botx, s.topx);
+  tighten_to_centres(fminf(fminf(ay, by), cy), fmaxf(fmaxf(ay, by), cy), s.boty, s.topy);
   const float n = cross2_x(xsub(bx, ax), xsub(by, ay), xsub(cx, ax), xsub(cy, ay));
   s.bcnx = xdiv(xsub(bx, cx), n);
   s.bcny = xdiv(xsub(by, cy), n);
   s.canx = xdiv(xsub(cx, ax), n);
   s.cany = xdiv(xsub(cy, ay), n);
   s.bx = bx; s.by = by; s.cx = cx; s.cy = cy;
-  s.wsa = xdiv(1.0f, wa);
-  s.wsb = xdiv(1.0f, wb);
-  s.wsc = xdiv(1.0f, wc);
+  s.wsa = xrcp(wa);
+  s.wsb = xrcp(wb);
+  s.wsc = xrcp(wc);
   s.Az = Av.z; s.Bz = Bv.z; s.Cz = Cv.z;
   return true;
 }

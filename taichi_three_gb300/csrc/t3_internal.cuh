@@ -12,12 +12,13 @@ namespace t3 {
 #define T3_STATUS_BIN_OVERFLOW 2
 #define T3_STATUS_TIMEOUT 4
 
-// Large-face queue of the direct rasteriser.
+// Large-face queue of the direct rasteriser (and its setup-record buffer).
 struct BigQueue {
   uint32_t* items;
   uint32_t capacity;
   uint32_t* count;
   int32_t* status;
+  float4* rec;  // setup records per global face id, or nullptr (shading recomputes)
 };
 
 // Binned rasteriser state (binned.cu).
@@ -33,6 +34,7 @@ struct BinArgs {
   int32_t tile;          // tile edge in pixels (8, 16, 32)
   int32_t tiles_x, tiles_y;
   int32_t big_tiles;     // faces touching more tiles than this go to the big list
+  int32_t max_lobes;     // largest flattened material of the scene
 };
 
 // A material tree flattened into a sum of weighted leaf lobes:
@@ -81,7 +83,9 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
 cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                         const t3_outputs& out, cudaStream_t st);
+                         const float4* rec, const t3_outputs& out, int max_lobes, cudaStream_t st);
+int max_lobes(const DevScene& sc);
+int shade_min_blocks();
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,
                         cudaStream_t st);

@@ -13,6 +13,28 @@
 
 namespace t3 {
 
+// Setup records: 4 x float4 per global face id, written by the rasteriser for
+// every visible face and read back by shading (no per-pixel setup recompute).
+__device__ __forceinline__ void store_record(float4* __restrict__ rec, uint32_t gid, const Setup& s) {
+  float4* r = rec + (size_t)gid * 4;
+  r[0] = make_float4(s.bx, s.by, s.cx, s.cy);
+  r[1] = make_float4(s.bcnx, s.bcny, s.canx, s.cany);
+  r[2] = make_float4(s.wsa, s.wsb, s.wsc, s.Az);
+  r[3] = make_float4(s.Bz, s.Cz, __int_as_float(s.botx | (s.boty << 16)),
+                     __int_as_float(s.topx | (s.topy << 16)));
+}
+
+__device__ __forceinline__ void load_record(const float4* __restrict__ rec, uint32_t gid, Setup& s) {
+  const float4* r = rec + (size_t)gid * 4;
+  const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+  s.bx = a.x; s.by = a.y; s.cx = a.z; s.cy = a.w;
+  s.bcnx = b.x; s.bcny = b.y; s.canx = b.z; s.cany = b.w;
+  s.wsa = c.x; s.wsb = c.y; s.wsc = c.z; s.Az = c.w;
+  s.Bz = d.x; s.Cz = d.y;
+  const int p0 = __float_as_int(d.z), p1 = __float_as_int(d.w);
+  s.botx = p0 & 0xFFFF; s.boty = p0 >> 16; s.topx = p1 & 0xFFFF; s.topy = p1 >> 16;
+}
+
 struct WarpFaces {
   float bx[32], by[32], cx[32], cy[32], bcnx[32], bcny[32], canx[32], cany[32];
   float wsa[32], wsb[32], wsc[32], Az[32], Bz[32], Cz[32];
@@ -20,18 +42,47 @@ struct WarpFaces {
   uint32_t id[32];
 };
 
+// One pixel's exact inside / depth test (triangle.py:115-125) against setup t.
+template <class Sink>
+__device__ __forceinline__ void test_pixel(const Setup& t, int x, int y, uint32_t id, float biasx,
+                                           float biasy, float maxd, int32_t maxdepth, Sink& sink) {
+  const float px = xadd((float)x, biasx), py = xadd((float)y, biasy);
+  float wx, wy, wz, sum;
+  face_raw_weights(t, px, py, wx, wy, wz, sum);
+  f3 wei;
+  if (face_inside(wx, wy, wz, sum, wei)) {
+    const int32_t d = trunc_i32(xmul(face_depth(t, wei), maxd));
+    if (d < maxdepth) sink(x, y, pack_key(d, id));
+  }
+}
+
 // Every lane of the warp must call this.  `active` lanes contribute the face
 // `s` clipped to [cx0, cx1] x [cy0, cy1]; sink(x, y, key) receives every
-// covered pixel with its packed (depth, id) key.
+// covered pixel with its packed (depth, id) key.  Faces of at most
+// kSmallArea pixels walk their own pixels (a short, nearly uniform loop);
+// larger ones go through the cooperative prefix-sum walk.
 template <class Sink>
 __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool active, uint32_t id,
                                             int cx0, int cx1, int cy0, int cy1,
                                             const t3_frame& fr, Sink sink) {
+  constexpr int kSmallArea = 4;
   const unsigned FULL = 0xFFFFFFFFu;
   const int lane = threadIdx.x & 31;
   const int x0 = max(s.botx, cx0), x1 = min(s.topx, cx1);
   const int y0 = max(s.boty, cy0), y1 = min(s.topy, cy1);
-  const int area = (active && x0 <= x1 && y0 <= y1) ? (x1 - x0 + 1) * (y1 - y0 + 1) : 0;
+  const int full_area = (active && x0 <= x1 && y0 <= y1) ? (x1 - x0 + 1) * (y1 - y0 + 1) : 0;
+  const float maxd = (float)fr.maxdepth;
+  const float biasx = fr.bias[0], biasy = fr.bias[1];
+  // small faces: per-lane walk
+  if (full_area > 0 && full_area <= kSmallArea) {
+    const int h = y1 - y0 + 1;
+    for (int k = 0; k < full_area; k++) {
+      const int q = k / h;  // h <= 4
+      test_pixel(s, x0 + q, y0 + (k - q * h), id, biasx, biasy, maxd, fr.maxdepth, sink);
+    }
+  }
+  const int area = full_area > kSmallArea ? full_area : 0;
+  if (!__any_sync(FULL, area > 0)) return;
   if (area > 0) {
     wf.bx[lane] = s.bx; wf.by[lane] = s.by; wf.cx[lane] = s.cx; wf.cy[lane] = s.cy;
     wf.bcnx[lane] = s.bcnx; wf.bcny[lane] = s.bcny; wf.canx[lane] = s.canx; wf.cany[lane] = s.cany;
@@ -48,8 +99,6 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
   wf.incl[lane] = incl;
   const int total = __shfl_sync(FULL, incl, 31);
   __syncwarp();
-  const float maxd = (float)fr.maxdepth;
-  const float biasx = fr.bias[0], biasy = fr.bias[1];
   for (int base = 0; base < total; base += 32) {
     const int idx = base + lane;
     if (idx < total) {
@@ -63,20 +112,12 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
       int q = __float2int_rz(__fdividef((float)off + 0.5f, (float)h));
       int r = off - q * h;
       if (r < 0) { q--; r += h; } else if (r >= h) { q++; r -= h; }
-      const int x = wf.x0[j] + q, y = wf.y0[j] + r;
       Setup t;
       t.bx = wf.bx[j]; t.by = wf.by[j]; t.cx = wf.cx[j]; t.cy = wf.cy[j];
       t.bcnx = wf.bcnx[j]; t.bcny = wf.bcny[j]; t.canx = wf.canx[j]; t.cany = wf.cany[j];
       t.wsa = wf.wsa[j]; t.wsb = wf.wsb[j]; t.wsc = wf.wsc[j];
-      const float px = xadd((float)x, biasx), py = xadd((float)y, biasy);
-      float wx, wy, wz, sum;
-      face_raw_weights(t, px, py, wx, wy, wz, sum);
-      f3 wei;
-      if (face_inside(wx, wy, wz, sum, wei)) {
-        t.Az = wf.Az[j]; t.Bz = wf.Bz[j]; t.Cz = wf.Cz[j];
-        const int32_t d = trunc_i32(xmul(face_depth(t, wei), maxd));
-        if (d < fr.maxdepth) sink(x, y, pack_key(d, wf.id[j]));
-      }
+      t.Az = wf.Az[j]; t.Bz = wf.Bz[j]; t.Cz = wf.Cz[j];
+      test_pixel(t, wf.x0[j] + q, wf.y0[j] + r, wf.id[j], biasx, biasy, maxd, fr.maxdepth, sink);
     }
   }
   __syncwarp();

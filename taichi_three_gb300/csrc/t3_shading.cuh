@@ -78,27 +78,30 @@ __device__ __forceinline__ V3 eval_value(const DevMaterial& m, int i, const Frag
   return eval_leaf(nd, fg);
 }
 
+// NL = lobe slots compiled in (the kernels are instantiated for 1, 2 and 4)
+template <int NL>
 struct LobeState {
-  int kind[T3_MAX_LOBES];
-  V3 w[T3_MAX_LOBES];   // lobe weight
-  V3 f0[T3_MAX_LOBES];  // COOK fresnel
-  float a2[T3_MAX_LOBES], k[T3_MAX_LOBES], gnorm[T3_MAX_LOBES];
-  float m[T3_MAX_LOBES];
-  int ipow[T3_MAX_LOBES];
+  int kind[NL];
+  V3 w[NL];   // lobe weight
+  V3 f0[NL];  // COOK fresnel
+  float a2[NL], k[NL], gnorm[NL];
+  float m[NL];
+  int ipow[NL];
   int n;
 };
 
+template <int NL>
 __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag& fg, V3 viewdir,
-                                              LobeState& L, V3& ambient, V3& emission) {
+                                              LobeState<NL>& L, V3& ambient, V3& emission) {
   L.n = mat.nlobes;
   ambient = v3(0.f, 0.f, 0.f);
   emission = v3(0.f, 0.f, 0.f);
   const float NoV = fmaxf(1e-10f, dot(viewdir, fg.normal));
 #pragma unroll
-  for (int k = 0; k < T3_MAX_LOBES; k++) {
+  for (int k = 0; k < NL; k++) {
     L.kind[k] = -1;
     if (k >= L.n) continue;
-    const DevLobe lb = mat.lobes[k];
+    const DevLobe& lb = mat.lobes[k];
     V3 w = v3(1.f, 1.f, 1.f);
     for (int j = 0; j < lb.nfac; j++) {
       const V3 f = eval_value(mat, lb.fac[j] & 0xFFFF, fg);
@@ -126,10 +129,11 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
 }
 
 // sum_k W_k * brdf_k(n, L, V)
-__device__ __forceinline__ V3 eval_brdf(const LobeState& L, V3 n, V3 ldir, V3 vdir) {
+template <int NL>
+__device__ __forceinline__ V3 eval_brdf(const LobeState<NL>& L, V3 n, V3 ldir, V3 vdir) {
   V3 acc = v3(0.f, 0.f, 0.f);
 #pragma unroll
-  for (int k = 0; k < T3_MAX_LOBES; k++) {
+  for (int k = 0; k < NL; k++) {
     if (L.kind[k] == T3_OP_LAMBERT) {
       acc = acc + 0.31830988618379067f * L.w[k];
     } else if (L.kind[k] == T3_OP_COOK) {
@@ -160,9 +164,29 @@ __device__ __forceinline__ V3 eval_brdf(const LobeState& L, V3 n, V3 ldir, V3 vd
   return acc;
 }
 
+__device__ __forceinline__ V3 background(const t3_frame& fr) {
+  V3 c = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
+  if (fr.flags & T3_TONEMAP) c = v3(aces(c.x), aces(c.y), aces(c.z));
+  return c;
+}
+
+// Writes an empty pixel: background colour, id -1, maxdepth, +inf.
+__device__ __forceinline__ void write_empty(const t3_frame& fr, const t3_outputs& out, int64_t i,
+                                            V3 bg) {
+  if (out.rgb) {
+    out.rgb[3 * i] = bg.x;
+    out.rgb[3 * i + 1] = bg.y;
+    out.rgb[3 * i + 2] = bg.z;
+  }
+  if (out.face_id) out.face_id[i] = -1;
+  if (out.depth) out.depth[i] = fr.maxdepth;
+  if (out.depth_f) out.depth_f[i] = __int_as_float(0x7f800000);
+}
+
 // Shades pixel (x, y) from its packed (depth, id) key and writes every output.
 // `rec` (nullable) holds the rasteriser's setup records (64 bytes per face id);
 // without it the face setup is recomputed, bit-identically.
+template <int NL>
 __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
                                                      const float4* __restrict__ rec,
                                                      unsigned long long key, int x, int y,
@@ -184,6 +208,9 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
   float depth_f = __int_as_float(0x7f800000);
   if (o < 0) {
     color = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
+    if (out.face_id) out.face_id[i] = fid;
+    if (out.depth) out.depth[i] = depth;
+    if (out.depth_f) out.depth_f[i] = depth_f;
   } else {
     const uint32_t gid = (uint32_t)key;
     fid = (int32_t)gid;
@@ -192,6 +219,15 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     const t3_mesh& mesh = ob.mesh;
     const int64_t n = (int64_t)gid - ob.face_base;
     const FaceRef ref = face_ref(mesh, n);
+    // start every gather of this face now: normals and material attributes are
+    // needed only after the weights, but their DRAM latency overlaps from here
+    if ((fr.flags & T3_SMOOTHING) && mesh.norms && !(mesh.flags & T3_MESH_FLAT_NORMAL)) {
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+        asm volatile("prefetch.global.L1 [%0];" :: "l"(base_ptr(mesh, ref.f, k, 1)));
+    }
+    if (mesh.face_attr)
+      asm volatile("prefetch.global.L1 [%0];" :: "l"(mesh.face_attr + ref.f * mesh.attr_stride));
     f3 v[3];
     face_verts(mesh, ref, v);
     Setup s;
@@ -208,6 +244,10 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     const float px = xadd((float)x, fr.bias[0]), py = xadd((float)y, fr.bias[1]);
     const f3 wei = face_weights(s, px, py);
     depth_f = face_depth(s, wei);
+    // the raster outputs are final: store them now (shorter live ranges)
+    if (out.face_id) out.face_id[i] = fid;
+    if (out.depth) out.depth[i] = depth;
+    if (out.depth_f) out.depth_f[i] = depth_f;
 
     // interpolate (triangle.py:32-49)
     Frag fg;
@@ -243,9 +283,9 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     const V3 rd = normalized(ro1 - ro);
     const V3 vdir = v3(-rd.x, -rd.y, -rd.z);
 
-    LobeState L;
+    LobeState<NL> L;
     V3 amb, emi;
-    eval_material(ob.mat, fg, vdir, L, amb, emi);
+    eval_material<NL>(ob.mat, fg, vdir, L, amb, emi);
 
     // Lighting.shade_color (lighting.py:84-98)
     const t3_lighting& lt = sc->lighting;
@@ -261,7 +301,7 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
       if (cos_i > 0.0f) {
         const float4 lc = *reinterpret_cast<const float4*>(lt.lights[l].color);
         const float s = cos_i * (inv_d * inv_d);
-        const V3 mcol = eval_brdf(L, fg.normal, ldir, vdir);
+        const V3 mcol = eval_brdf<NL>(L, fg.normal, ldir, vdir);
         color = color + v3(s * lc.x, s * lc.y, s * lc.z) * mcol;
       }
     }
@@ -272,9 +312,6 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     out.rgb[3 * i + 1] = color.y;
     out.rgb[3 * i + 2] = color.z;
   }
-  if (out.face_id) out.face_id[i] = fid;
-  if (out.depth) out.depth[i] = depth;
-  if (out.depth_f) out.depth_f[i] = depth_f;
 }
 
 } // namespace t3
