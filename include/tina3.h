@@ -129,14 +129,32 @@ typedef struct t3_light {
   float color[4]; /* rgb, pad                                                    */
 } t3_light;
 
-#define T3_LIGHT_LAMPS 0  /* Lighting: emission + ambient + sum of lamps     */
-#define T3_LIGHT_IBL 1    /* SkyboxLighting: sample_ibl + emission           */
+#define T3_LIGHT_LAMPS 0   /* Lighting: emission + ambient + sum of lamps              */
+#define T3_LIGHT_IBL_MC 1  /* SkyboxLighting by Monte Carlo over the materials' own
+                              importance samplers (material.sample, material.py:
+                              124-138, 365-405, 460-472): emission + mean of
+                              weight * env(dir) over `spp` samples (+ lamps if any)  */
+#define T3_LIGHT_IBL_MLP 2 /* SkyboxLighting by the learned IBL network             */
+
+/* MLP-IBL network (see t3_mlp_*): 400 -> 64 -> 64 -> 64 -> 16 (9 used),
+ * ReLU hidden layers, BF16 weights (inference) with FP32 biases. */
+#define T3_MLP_IN 400
+#define T3_MLP_HID 64
+#define T3_MLP_OUT 16
 
 typedef struct t3_lighting {
   int32_t mode;     /* T3_LIGHT_*                                             */
-  int32_t nlights;
+  int32_t nlights;  /* lamps; with an IBL mode they are added to the IBL term  */
   float ambient[4];
   t3_light lights[T3_MAX_LIGHTS];
+  /* environment map, Tina's equirect layout (tina/skybox.py:40-145): texel
+   * (i, j), i < env_w = 2*res, j < env_h = res, at (i*env_h + j)*3; FP16 when
+   * env_half, else FP32 */
+  const void* env;
+  int32_t env_w, env_h, env_half, spp;
+  uint32_t seed;    /* Monte Carlo stream seed                                 */
+  int32_t _pad;
+  const void* mlp;  /* T3_LIGHT_IBL_MLP: packed network (t3_mlp_pack)         */
 } t3_lighting;
 
 /* ---- whole-frame parameters --------------------------------------------- */
@@ -258,6 +276,42 @@ int t3_event_elapsed_ms(void* start, void* end, float* ms); /* waits for `end` *
  * stream capture).  All calls share the array: calls that overlap on the GPU
  * race and must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
 int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* out, void* stream);
+
+/* ---- MLP-IBL (learned image-based lighting) -------------------------------
+ * The network maps (normal, view direction, roughness, metallic) to log1p of
+ * the albedo-independent IBL integrals of the Lambert and CookTorrance lobes
+ * (E_d, S1, S2; RGB each) under the method's own Monte Carlo estimator; shading
+ * composes them with the pixel's albedo and f0.  No counterpart in the
+ * reference (its IBL is a prefiltered-map lookup, material.py:256-320). */
+int64_t t3_mlp_param_count(void);   /* FP32 parameters: W1 b1 W2 b2 W3 b3 W4 b4 */
+int64_t t3_mlp_packed_bytes(void);  /* bytes of the packed BF16 inference blob  */
+/* E_d on an equirect grid of normals (map [map_w, map_h, 3]), spp cosine samples */
+int t3_mlp_irradiance_map(const void* env, int env_w, int env_h, int env_half, int map_w, int map_h,
+                          int spp, uint32_t seed, float* map, void* stream);
+/* training targets [B, 9] = log1p(E_d from the map, S1, S2) at nv [B, 6] (n, v), rough [B] */
+int t3_mlp_targets(const void* env, int env_w, int env_h, int env_half, const float* irr_map,
+                   int map_w, int map_h, const float* nv, const float* rough, int64_t B, int spp,
+                   uint32_t seed, float* targets, void* stream);
+/* input features X [B, 400] of (n, v, roughness, metallic) */
+int t3_mlp_encode(const float* nv, const float* rough, const float* metal, int64_t B, float* X,
+                  void* stream);
+/* forward: hidden activations acts [B, 192], outputs Y [B, 16] */
+int t3_mlp_forward(const float* params, const float* X, int64_t B, float* acts, float* Y,
+                   void* stream);
+/* backward of the mean squared error over the 9 used outputs: grads (param
+ * layout), dbuf workspace [B, 144], loss (device float, accumulated) */
+int t3_mlp_backward(const float* params, const float* X, const float* acts, const float* Y,
+                    const float* targets, int64_t B, float* grads, float* dbuf, float* loss,
+                    void* stream);
+/* one Adam step (bias-corrected) over n parameters */
+int t3_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
+                float beta1, float beta2, float eps, int step, void* stream);
+/* BF16 inference blob (16-byte aligned, t3_mlp_packed_bytes) from FP32 params */
+int t3_mlp_pack(const float* params, void* blob, void* stream);
+/* inference on the tensor cores (tcgen05, FP32 accumulate): Y [B, 16] */
+int t3_mlp_infer(const void* blob, const float* X, int64_t B, float* Y, int32_t* status, void* stream);
+/* FP32 CUDA-core inference of the same network (reference path) */
+int t3_mlp_infer_f32(const float* params, const float* X, int64_t B, float* Y, void* stream);
 
 /* Reads back the device status word written by the last t3_raster/t3_render
  * (synchronises `stream`). */

@@ -30,6 +30,9 @@ def load():
         lib.oracle_aces_f32.restype = C.c_int
         lib.oracle_aces_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         lib.oracle_max_threads.restype = C.c_int
+        lib.oracle_pixels_f64.restype = C.c_int
+        lib.oracle_pixels_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_uint32,
+                                          C.c_int, C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -71,6 +74,25 @@ def render(scene, mode=0, nthreads=0, fp64=False, want_depth_f=True):
     out = render_desc(sc, mode, nthreads, fp64, want_depth_f)
     del keep
     return out
+
+
+def pixels_f64(scene, pixels, spp=0, seed=0, nthreads=0):
+    """FP64 colours (pre, post tonemap) of the given pixel indices x*H + y, shaded
+    over the FP32 raster's winners; spp > 0 overrides the IBL sample count and
+    seed (the converged reference for error statements)."""
+    lib = load()
+    for obj in scene.objects:
+        pre_compute_host(obj)
+    sc, keep = scene.describe('cpu')
+    px = np.ascontiguousarray(pixels, dtype=np.int64)
+    pre = np.empty((len(px), 3), np.float64)
+    post = np.empty((len(px), 3), np.float64)
+    rc = lib.oracle_pixels_f64(C.addressof(sc), _p(px), len(px), int(spp), int(seed) & 0xFFFFFFFF,
+                               int(nthreads), _p(pre), _p(post))
+    if rc != 0:
+        raise RuntimeError(f'oracle_pixels_f64 failed ({rc})')
+    del keep
+    return pre, post
 
 
 def grid_normals(pos):

@@ -458,6 +458,219 @@ template <class R> inline R aces1(R c) {
   return (c * (cst<R>(2.51) * c + cst<R>(0.03))) / (c * (cst<R>(2.43) * c + cst<R>(0.59)) + cst<R>(0.14));
 }
 
+// ---------------------------------------------------------------------------
+// Image-based lighting (SkyboxLighting, tina/core/lighting.py:5-21) by the
+// materials' own importance samplers (material.py sample(): Lambert :399-405,
+// CookTorrance :365-384, Phong :460-472, Mix :124-138, Scale :180-184), with
+// the sky-ray estimate of path/engine.py:243-266: emission + mean of
+// weight * env(dir).  The material tree is flattened into weighted lobes
+// (the product of Mix / Scale factors along the path); a lobe is drawn with
+// probability equal to the product of its Mix choices (smoothlerp(avg f, .12,
+// .88) or its complement), normalised over the lobes, and weighted by
+// lobe weight / probability.  Random numbers: pcg_hash (Jarzynski & Olano,
+// JCGT 2020) of (seed, pixel, sample, draw).
+// ---------------------------------------------------------------------------
+inline uint32_t pcg_hash(uint32_t v) {
+  const uint32_t state = v * 747796405u + 2891336453u;
+  const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+inline uint32_t rng_base(uint32_t seed, uint32_t pixel) { return pcg_hash(seed ^ pcg_hash(pixel)); }
+inline float rng_draw(uint32_t base, uint32_t sample, uint32_t draw) {
+  return (float)(pcg_hash(base ^ ((sample * 3u + draw) * 0x9E3779B9u)) >> 8) * 5.9604644775390625e-08f;
+}
+
+// IEEE binary16 -> float
+inline float half_to_float(uint16_t h) {
+  const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+  uint32_t exp = (h >> 10) & 0x1Fu, man = h & 0x3FFu, bits;
+  if (exp == 0) {
+    if (man == 0) {
+      bits = sign;
+    } else {  // subnormal: renormalise
+      int e = -1;
+      do { e++; man <<= 1; } while (!(man & 0x400u));
+      bits = sign | ((uint32_t)(127 - 15 - e) << 23) | ((man & 0x3FFu) << 13);
+    }
+  } else if (exp == 31) {
+    bits = sign | 0x7F800000u | (man << 13);
+  } else {
+    bits = sign | ((exp + 127 - 15) << 23) | (man << 13);
+  }
+  float f;
+  std::memcpy(&f, &bits, 4);
+  return f;
+}
+
+template <class R> struct EnvMap {
+  const t3_lighting* lt;
+  v3<R> texel(int64_t i, int64_t j) const {
+    i = i < 0 ? 0 : i >= lt->env_w ? lt->env_w - 1 : i;
+    j = j < 0 ? 0 : j >= lt->env_h ? lt->env_h - 1 : j;
+    const int64_t o = (i * lt->env_h + j) * 3;
+    if (lt->env_half) {
+      const uint16_t* t = reinterpret_cast<const uint16_t*>(lt->env) + o;
+      return {(R)half_to_float(t[0]), (R)half_to_float(t[1]), (R)half_to_float(t[2])};
+    }
+    const float* t = reinterpret_cast<const float*>(lt->env) + o;
+    return {(R)t[0], (R)t[1], (R)t[2]};
+  }
+  // Skybox.sample: spheremap (tina/skybox.py:23-28) + bilerp (tina/common.py:140-149),
+  // the +1 texel clamped to the map
+  v3<R> sample(v3<R> dir) const {
+    const R u = dir.y;
+    R p = std::atan2(-dir.z, dir.x) / R(2.0 * M_PI);
+    p = p - std::floor(p);
+    const R cx = p * (R)(lt->env_w - 1), cy = (u * R(0.5) + R(0.5)) * (R)(lt->env_h - 1);
+    const R fx = std::floor(cx), fy = std::floor(cy);
+    const int64_t ix = (int64_t)fx, iy = (int64_t)fy;
+    const R x1 = cx - fx, y1 = cy - fy, x0 = R(1) - x1, y0 = R(1) - y1;
+    v3<R> r = add(add(muls(x1 * y1, texel(ix + 1, iy + 1)), muls(x1 * y0, texel(ix + 1, iy))),
+                  add(muls(x0 * y0, texel(ix, iy)), muls(x0 * y1, texel(ix, iy + 1))));
+    return r;
+  }
+};
+
+// tangentspace(nrm) @ spherical(h, p)  (tina/advans.py:97-108)
+template <class R> inline v3<R> tangent_dir(v3<R> n, R h, R p) {
+  const v3<R> bitan = normalized(cross(n, v3<R>{R(233), R(666), R(512)}));
+  const v3<R> tan = cross(bitan, n);
+  const R r = std::sqrt(std::max(R(0), R(1) - h * h));
+  const R a = R(2.0 * M_PI) * p;
+  return add(add(muls(r * std::cos(a), tan), muls(r * std::sin(a), bitan)), muls(h, n));
+}
+
+template <class R> inline R mix_prob(R fac) {
+  if (fac != R(0) && fac != R(1)) {
+    const R t = std::min(R(1), std::max(R(0), fac));
+    const R s = t * t * (R(3) - R(2) * t);
+    return R(0.12) * (R(1) - s) + R(0.88) * s;
+  }
+  return fac;
+}
+
+struct FlatLobe {
+  int leaf;
+  int nfac;
+  int fac[8];     // node index
+  bool onem[8];
+  bool mix[8];
+};
+
+inline void flatten(const t3_material& m, int node, FlatLobe cur, std::vector<FlatLobe>& out) {
+  const t3_node& nd = m.nodes[node];
+  if (nd.op == T3_OP_LAMBERT || nd.op == T3_OP_PHONG || nd.op == T3_OP_COOK || nd.op == T3_OP_EMISSION) {
+    cur.leaf = node;
+    out.push_back(cur);
+    return;
+  }
+  if (nd.op == T3_OP_MIX) {
+    FlatLobe a = cur, b = cur;
+    a.fac[a.nfac] = nd.c; a.onem[a.nfac] = true; a.mix[a.nfac] = true; a.nfac++;
+    b.fac[b.nfac] = nd.c; b.onem[b.nfac] = false; b.mix[b.nfac] = true; b.nfac++;
+    flatten(m, nd.a, a, out);
+    flatten(m, nd.b, b, out);
+  } else if (nd.op == T3_OP_SCALE) {
+    cur.fac[cur.nfac] = nd.b; cur.onem[cur.nfac] = false; cur.mix[cur.nfac] = false; cur.nfac++;
+    flatten(m, nd.a, cur, out);
+  } else if (nd.op == T3_OP_ADD) {
+    flatten(m, nd.a, cur, out);
+    flatten(m, nd.b, cur, out);
+  }
+}
+
+template <class R>
+v3<R> shade_ibl_mc(const t3_lighting& L, const MaterialEval<R>& me, v3<R> normal, v3<R> viewdir,
+                   uint32_t pixel, int spp, uint32_t seed) {
+  std::vector<FlatLobe> lobes;
+  FlatLobe root{};
+  flatten(*me.m, me.m->root, root, lobes);
+  const int nl = (int)lobes.size();
+  std::vector<v3<R>> W(nl), f0(nl);
+  std::vector<R> prob(nl), cdf(nl), r2(nl);
+  v3<R> emission = {R(0), R(0), R(0)};
+  R c = 0;
+  for (int k = 0; k < nl; k++) {
+    v3<R> w = {R(1), R(1), R(1)};
+    R pr = 1;
+    for (int j = 0; j < lobes[k].nfac; j++) {
+      v3<R> f = me.value(lobes[k].fac[j]).v;
+      if (lobes[k].onem[j]) f = {R(1) - f.x, R(1) - f.y, R(1) - f.z};
+      w = mul(w, f);
+      if (lobes[k].mix[j]) {
+        v3<R> g = me.value(lobes[k].fac[j]).v;
+        const R q = mix_prob((g.x + g.y + g.z) * (R(1) / R(3)));
+        pr *= lobes[k].onem[j] ? R(1) - q : q;
+      }
+    }
+    const t3_node& leaf = me.m->nodes[lobes[k].leaf];
+    if (leaf.op == T3_OP_EMISSION) { emission = add(emission, w); pr = 0; }
+    W[k] = pr > 0 ? muls(R(1) / pr, w) : v3<R>{R(0), R(0), R(0)};
+    if (leaf.op == T3_OP_COOK) {
+      const R r = me.value(leaf.a).v.x;
+      r2[k] = r * r;
+      f0[k] = me.value(leaf.b).v;
+    } else if (leaf.op == T3_OP_PHONG) {
+      r2[k] = me.value(leaf.a).v.x;
+    }
+    c += pr;
+    cdf[k] = c;
+  }
+  for (int k = 0; k < nl; k++) W[k] = muls(c, W[k]);
+  v3<R> acc = {R(0), R(0), R(0)};
+  if (c > 0) {
+    EnvMap<R> env{&L};
+    const uint32_t base = rng_base(seed, pixel);
+    for (int s = 0; s < spp; s++) {
+      const R xs = (R)rng_draw(base, (uint32_t)s, 0u) * c;
+      const R xu = (R)rng_draw(base, (uint32_t)s, 1u), xv = (R)rng_draw(base, (uint32_t)s, 2u);
+      int k = 0;
+      for (int j = 0; j < nl - 1; j++)
+        if (xs >= cdf[j]) k = j + 1;
+      const t3_node& leaf = me.m->nodes[lobes[k].leaf];
+      v3<R> dir, w;
+      if (leaf.op == T3_OP_LAMBERT) {
+        dir = normalized(tangent_dir(normal, std::sqrt(xu), xv));
+        w = W[k];
+      } else if (leaf.op == T3_OP_COOK) {
+        const R a2s = std::max(R(0), r2[k]);
+        const R u = std::sqrt((R(1) - xu) / (R(1) - xu * (R(1) - a2s)));
+        const v3<R> rdir = reflect(neg(viewdir), normal);
+        v3<R> o = tangent_dir(rdir, u, xv);
+        const R a2 = std::max(MaterialEval<R>::c_eps6(), r2[k]);
+        const v3<R> half = normalized(add(viewdir, o));
+        const R NoL = std::max(MaterialEval<R>::c_eps(), dot(viewdir, normal));
+        const R NoV = std::max(MaterialEval<R>::c_eps(), dot(o, normal));
+        const R VoH = std::min(MaterialEval<R>::c_eps_big(), std::max(MaterialEval<R>::c_eps(), dot(half, o)));
+        const R kk = a2 / R(2);
+        R vdf = R(1) / ((NoV * kk + R(1)) - kk);
+        vdf = vdf * (R(1) / ((NoL * kk + R(1)) - kk));
+        vdf = vdf / (R(1) * (R(1) - a2) + MaterialEval<R>::c_4pi() * a2);
+        const R p5 = pow5(R(1) - VoH);
+        v3<R> fdf = {f0[k].x + (R(1) - f0[k].x) * p5, f0[k].y + (R(1) - f0[k].y) * p5,
+                     f0[k].z + (R(1) - f0[k].z) * p5};
+        if (dot(o, normal) < R(0)) { o = neg(o); fdf = {R(0), R(0), R(0)}; }
+        dir = o;
+        w = muls(vdf, mul(W[k], fdf));
+      } else if (leaf.op == T3_OP_PHONG) {
+        const R m = r2[k];
+        const R u = std::pow(xu, R(1) / (m + R(2) - R(1)));
+        const v3<R> rdir = reflect(neg(viewdir), normal);
+        v3<R> o = tangent_dir(rdir, u, xv);
+        R wt = 1;
+        if (dot(o, normal) < R(0)) { o = neg(o); wt = 0; }
+        dir = o;
+        w = muls(wt, W[k]);
+      } else {
+        continue;
+      }
+      if (w.x != R(0) || w.y != R(0) || w.z != R(0)) acc = add(acc, mul(w, env.sample(dir)));
+    }
+    acc = muls(R(1) / (R)spp, acc);
+  }
+  return add(emission, acc);
+}
+
 // Lighting.shade_color (tina/core/lighting.py:84-98)
 template <class R>
 v3<R> shade_lamps(const t3_lighting& L, const MaterialEval<R>& me, v3<R> pos, v3<R> normal,
@@ -488,6 +701,8 @@ v3<R> shade_lamps(const t3_lighting& L, const MaterialEval<R>& me, v3<R> pos, v3
 template <class R> struct Ctx {
   const t3_scene* sc;
   mat4<R> W2V, V2W;
+  int spp = 0;        // > 0: IBL sample count / seed override (ground-truth runs)
+  uint32_t seed = 0;
 };
 
 // render_color for one pixel of one object (triangle.py:134-153 -> shader.py:119-131)
@@ -533,7 +748,33 @@ v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, in
   int64_t bf = mesh.base_face(f);
   fg.attr = ob.mesh.face_attr ? ob.mesh.face_attr + bf * ob.mesh.attr_stride : nullptr;
   MaterialEval<R> me{&ob.material, &fg};
-  return shade_lamps(cx.sc->lighting, me, pos, normal, viewdir);
+  const t3_lighting& L = cx.sc->lighting;
+  if (L.mode == T3_LIGHT_IBL_MC) {
+    const uint32_t pixel = (uint32_t)((int64_t)x * fr.height + y);
+    const int spp = cx.spp > 0 ? cx.spp : L.spp;
+    const uint32_t seed = cx.spp > 0 ? cx.seed : L.seed;
+    v3<R> c = shade_ibl_mc(L, me, normal, viewdir, pixel, spp, seed);
+    if (L.nlights > 0) {
+      t3_lighting lamps = L;
+      lamps.ambient[0] = lamps.ambient[1] = lamps.ambient[2] = 0.0f;
+      v3<R> l = shade_lamps(lamps, me, pos, normal, viewdir);
+      c = add(c, sub(l, me.emission(me.m->root).v));  // lamps without a second emission
+    }
+    return c;
+  }
+  return shade_lamps(L, me, pos, normal, viewdir);
+}
+
+// Engine.render_background (tina/core/engine.py:42-49): the sky along the view ray
+template <class R> v3<R> background_pixel(const Ctx<R>& cx, int32_t x, int32_t y) {
+  const t3_frame& fr = cx.sc->frame;
+  R px = (R)x + (R)fr.bias[0], py = (R)y + (R)fr.bias[1];
+  R ux = (px / (R)fr.width) * R(2) - R(1);
+  R uy = (py / (R)fr.height) * R(2) - R(1);
+  v3<R> ro = mapply_pos(cx.V2W, v3<R>{ux, uy, R(-1)});
+  v3<R> ro1 = mapply_pos(cx.V2W, v3<R>{ux, uy, R(1)});
+  v3<R> rd = normalized(sub(ro1, ro));
+  return EnvMap<R>{&cx.sc->lighting}.sample(rd);
 }
 
 inline uint64_t pack_key(int32_t depth, uint32_t id) {
@@ -651,6 +892,12 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
     }
   }
 
+  if (sc->lighting.mode == T3_LIGHT_IBL_MC || sc->lighting.mode == T3_LIGHT_IBL_MLP) {
+#pragma omp parallel for schedule(static) if (mode == 1)
+    for (int64_t i = 0; i < P; i++)
+      if (gid[i] < 0) img[i] = background_pixel(cx, (int32_t)(i / H), (int32_t)(i % H));
+  }
+
   // ToneMapping.apply (postp/tonemap.py:10-12) and the outputs
 #pragma omp parallel for schedule(static) if (mode == 1)
   for (int64_t i = 0; i < P; i++) {
@@ -681,9 +928,83 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
   return 0;
 }
 
+// FP32 raster of every object (packed-key minimum, OpenMP): the winning
+// global face id per pixel, -1 where empty.
+inline std::vector<int64_t> raster_gids_f32(const t3_scene* sc) {
+  const t3_frame& fr = sc->frame;
+  const int64_t P = (int64_t)fr.width * fr.height;
+  Ctx<float> cx;
+  cx.sc = sc;
+  for (int i = 0; i < 16; i++) { cx.W2V.m[i] = fr.W2V[i]; cx.V2W.m[i] = fr.V2W[i]; }
+  std::vector<std::atomic<uint64_t>> keys(P);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < P; i++) keys[i].store(~0ull, std::memory_order_relaxed);
+  for (int o = 0; o < sc->nobjects; o++) {
+    const t3_object& ob = sc->objects[o];
+    Mesh<float> mesh(&ob.mesh);
+#pragma omp parallel for schedule(dynamic, 2048)
+    for (int64_t f = 0; f < ob.nfaces; f++) {
+      v3<float> v[3];
+      mesh.verts(f, v);
+      Setup<float> s;
+      face_setup(cx.W2V, fr, v, s);
+      if (s.culled) continue;
+      raster_face(cx, s, (uint64_t)(ob.face_base + f), keys.data());
+    }
+  }
+  std::vector<int64_t> gid(P);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < P; i++) {
+    const uint64_t k = keys[i].load(std::memory_order_relaxed);
+    gid[i] = k == ~0ull ? -1 : (int64_t)(uint32_t)k;
+  }
+  return gid;
+}
+
 } // namespace
 
 extern "C" {
+
+// FP64 shading of selected pixels over the FP32 raster's winners, with the IBL
+// sample count / seed overridden (spp > 0): the converged reference image for
+// error statements.  rgb_pre / rgb_post: [n, 3] before / after ACES.
+int oracle_pixels_f64(const t3_scene* sc, const int64_t* pixels, int64_t n, int spp, uint32_t seed,
+                      int nthreads, double* rgb_pre, double* rgb_post) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  const t3_frame& fr = sc->frame;
+  const int H = fr.height;
+  std::vector<int64_t> gid = raster_gids_f32(sc);
+  Ctx<double> cx;
+  cx.sc = sc;
+  cx.spp = spp;
+  cx.seed = seed;
+  for (int i = 0; i < 16; i++) { cx.W2V.m[i] = fr.W2V[i]; cx.V2W.m[i] = fr.V2W[i]; }
+  const bool ibl = sc->lighting.mode == T3_LIGHT_IBL_MC || sc->lighting.mode == T3_LIGHT_IBL_MLP;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t q = 0; q < n; q++) {
+    const int64_t i = pixels[q];
+    const int32_t x = (int32_t)(i / H), y = (int32_t)(i % H);
+    v3<double> c = {fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]};
+    if (gid[i] >= 0) {
+      for (int o = 0; o < sc->nobjects; o++) {
+        const t3_object& ob = sc->objects[o];
+        if (gid[i] >= ob.face_base && gid[i] < ob.face_base + ob.nfaces) {
+          Mesh<double> mesh(&ob.mesh);
+          c = shade_pixel(cx, ob, mesh, gid[i] - ob.face_base, x, y, (double*)nullptr);
+        }
+      }
+    } else if (ibl) {
+      c = background_pixel(cx, x, y);
+    }
+    if (rgb_pre) { rgb_pre[3 * q] = c.x; rgb_pre[3 * q + 1] = c.y; rgb_pre[3 * q + 2] = c.z; }
+    if (fr.flags & T3_TONEMAP) c = {aces1(c.x), aces1(c.y), aces1(c.z)};
+    if (rgb_post) { rgb_post[3 * q] = c.x; rgb_post[3 * q + 1] = c.y; rgb_post[3 * q + 2] = c.z; }
+  }
+  return 0;
+}
+
 
 // FP32 restatement (bit-exact target).  mode 0 = serial face order (the oracle),
 // mode 1 = OpenMP with packed-key minimum (the timed CPU baseline).

@@ -20,4 +20,5 @@ from .mesh import (MAX, ConnectiveMesh, MeshFlatNormal, MeshFlipCulling, MeshFli
 from .engine import Engine
 from .scene import Scene, Shader, TriangleRaster
 from .postp import ToneMapping, aces_tonemap
+from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from . import workloads

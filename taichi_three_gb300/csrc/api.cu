@@ -55,10 +55,10 @@ static int flatten_rec(const t3_material& in, int node, int* fac, int nfac, DevM
   case T3_OP_MIX: {
     if (nd.c < 0 || nd.c >= in.nnodes || !is_value(in.nodes[nd.c].op)) return T3_EINVAL;
     if (nfac + 1 > T3_MAX_FACTORS) return T3_EUNSUPPORTED;
-    f2[nfac] = nd.c | T3_FAC_ONE_MINUS;
+    f2[nfac] = nd.c | T3_FAC_ONE_MINUS | T3_FAC_MIX;
     int r = flatten_rec(in, nd.a, f2, nfac + 1, out, depth + 1);
     if (r) return r;
-    f2[nfac] = nd.c;
+    f2[nfac] = nd.c | T3_FAC_MIX;
     return flatten_rec(in, nd.b, f2, nfac + 1, out, depth + 1);
   }
   case T3_OP_SCALE: {
@@ -125,7 +125,14 @@ int make_dev_scene(const t3_scene& sc, DevScene& out) {
   if (r) return r;
   if (sc.nobjects < 0 || sc.nobjects > T3_MAX_OBJECTS) return T3_ETOOBIG;
   if (sc.lighting.nlights < 0 || sc.lighting.nlights > T3_MAX_LIGHTS) return T3_ETOOBIG;
-  if (sc.lighting.mode != T3_LIGHT_LAMPS) return T3_EUNSUPPORTED;
+  if (sc.lighting.mode == T3_LIGHT_IBL_MC || sc.lighting.mode == T3_LIGHT_IBL_MLP) {
+    if (!sc.lighting.env || sc.lighting.env_w < 2 || sc.lighting.env_h < 2) return T3_EINVAL;
+    if (sc.lighting.mode == T3_LIGHT_IBL_MC && (sc.lighting.spp < 1 || sc.lighting.spp > (1 << 20)))
+      return T3_EINVAL;
+    if (sc.lighting.mode == T3_LIGHT_IBL_MLP && !sc.lighting.mlp) return T3_EINVAL;
+  } else if (sc.lighting.mode != T3_LIGHT_LAMPS) {
+    return T3_EINVAL;
+  }
   out.frame = sc.frame;
   out.lighting = sc.lighting;
   out.nobjects = sc.nobjects;
@@ -316,7 +323,7 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
   cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
   return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
-                              nullptr, *out, max_lobes(ds), st));
+                              nullptr, *out, max_lobes(ds), ds.lighting.mode, st));
 }
 
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
@@ -363,7 +370,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
       e = launch_shade(dsc, scene->frame, keys, reinterpret_cast<const float4*>(ws + L.rec), *out,
-                       max_lobes(ds), st);
+                       max_lobes(ds), ds.lighting.mode, st);
   } else {
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -379,6 +386,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     b.tiles_y = L.tiles_y;
     b.big_tiles = 16;
     b.max_lobes = max_lobes(ds);
+    b.light_mode = ds.lighting.mode;
     if (e == cudaSuccess) e = mark(1);
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++)
       e = launch_bin(scene->frame, scene->objects[o], b, st);

@@ -116,8 +116,8 @@ struct SmemKeySink {
   int TS_DYN;
 };
 
-template <int TS, int BLOCK, int NL, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB)
+template <int TS, int BLOCK, int NL, int MODE>
+__global__ void __launch_bounds__(BLOCK, BLOCK == 256 ? 3 : 6)
 k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw);  // TS*TS
@@ -212,8 +212,10 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
     const int x = x0 + i / TS, y = y0 + i % TS;
     bool covered = false;
     if (i < TS * TS && x <= x1 && y <= y1) {
-      if (!ok || keys[i] == T3_EMPTY_KEY) write_empty(fr, out, (int64_t)x * H + y, bg);
-      else covered = true;
+      if (MODE == T3_LIGHT_LAMPS && (!ok || keys[i] == T3_EMPTY_KEY))
+        write_empty(fr, out, (int64_t)x * H + y, bg);
+      else
+        covered = true;
     }
     const unsigned m = __ballot_sync(FULL, covered);
     if (m) {
@@ -227,7 +229,8 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   const int ncov = s_count;
   for (int j = threadIdx.x; j < ncov; j += BLOCK) {
     const int i = s_list[j];
-    shade_pixel_from_key<NL>(sc, bins.rec, keys[i], x0 + i / TS, y0 + i % TS, out);
+    shade_pixel_from_key<NL, MODE>(sc, bins.rec, ok ? keys[i] : T3_EMPTY_KEY, x0 + i / TS,
+                                   y0 + i % TS, out);
   }
   if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(bar_a) : "memory");
 }
@@ -240,30 +243,31 @@ cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& b
   return cudaGetLastError();
 }
 
-template <int TS, int BLOCK, int NL, int MINB>
+template <int TS, int BLOCK, int NL, int MODE>
 static cudaError_t launch_tile_b(const DevScene* sc, const BinArgs& bins, int ntiles,
                                  const t3_outputs& out, cudaStream_t st) {
   const size_t smem = (size_t)TS * TS * 8 + (size_t)bins.capacity * 4;
-  cudaError_t e = cudaFuncSetAttribute(k_tile<TS, BLOCK, NL, MINB>,
+  cudaError_t e = cudaFuncSetAttribute(k_tile<TS, BLOCK, NL, MODE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_tile<TS, BLOCK, NL, MINB><<<ntiles, BLOCK, smem, st>>>(sc, bins, out);
+  k_tile<TS, BLOCK, NL, MODE><<<ntiles, BLOCK, smem, st>>>(sc, bins, out);
   return cudaGetLastError();
 }
 
 template <int TS, int BLOCK, int NL>
 static cudaError_t launch_tile_nl(const DevScene* sc, const BinArgs& bins, int ntiles,
                                   const t3_outputs& out, cudaStream_t st) {
-  if (shade_min_blocks() == 3 && BLOCK == 256)
-    return launch_tile_b<TS, BLOCK, NL, 3>(sc, bins, ntiles, out, st);
-  return launch_tile_b<TS, BLOCK, NL, BLOCK == 256 ? 2 : 6>(sc, bins, ntiles, out, st);
+  if (bins.light_mode == T3_LIGHT_LAMPS)
+    return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_LAMPS>(sc, bins, ntiles, out, st);
+  if (bins.light_mode == T3_LIGHT_IBL_MC)
+    return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_IBL_MC>(sc, bins, ntiles, out, st);
+  return cudaErrorInvalidValue;
 }
 
 template <int TS, int BLOCK>
 static cudaError_t launch_tile_t(const DevScene* sc, const BinArgs& bins, int ntiles,
                                  const t3_outputs& out, cudaStream_t st) {
-  if (bins.max_lobes <= 1) return launch_tile_nl<TS, BLOCK, 1>(sc, bins, ntiles, out, st);
-  if (bins.max_lobes == 2) return launch_tile_nl<TS, BLOCK, 2>(sc, bins, ntiles, out, st);
+  if (bins.max_lobes <= 2) return launch_tile_nl<TS, BLOCK, 2>(sc, bins, ntiles, out, st);
   return launch_tile_nl<TS, BLOCK, 4>(sc, bins, ntiles, out, st);
 }
 

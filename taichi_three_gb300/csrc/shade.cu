@@ -6,8 +6,6 @@
 // exactly as the rasteriser did (so depth_f is bit-exact), interpolates
 // position / normal / texcoord, evaluates the material once per pixel, then
 // sums the lamps and applies ACES.
-#include <cstdlib>
-
 #include "t3_shading.cuh"
 
 namespace t3 {
@@ -41,8 +39,8 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
 // Each block owns PPT * BLOCK consecutive pixels.  Empty pixels are written as
 // background at once; covered ones are compacted into a shared list (warp
 // ballot + one shared atomic per warp) so that full warps run the shading.
-template <int BLOCK, int PPT, int NL, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB)
+template <int BLOCK, int PPT, int NL, int MODE>
+__global__ void __launch_bounds__(BLOCK, 3)
 k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
         const float4* __restrict__ rec, t3_outputs out, int64_t npix, int H) {
   __shared__ int s_list[BLOCK * PPT];
@@ -59,7 +57,8 @@ k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ 
     const int64_t i = base + local;
     bool covered = false;
     if (i < npix) {
-      if (keys[i] == T3_EMPTY_KEY) write_empty(fr, out, i, bg);
+      // with IBL, empty pixels show the sky and go through the shading list too
+      if (MODE == T3_LIGHT_LAMPS && keys[i] == T3_EMPTY_KEY) write_empty(fr, out, i, bg);
       else covered = true;
     }
     const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
@@ -75,45 +74,38 @@ k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ 
   for (int j = threadIdx.x; j < n; j += BLOCK) {
     const int64_t i = base + s_list[j];
     const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
-    shade_pixel_from_key<NL>(sc, rec, keys[i], x, y, out);
+    shade_pixel_from_key<NL, MODE>(sc, rec, keys[i], x, y, out);
   }
 }
 
-// Resident blocks per SM the shade kernels are compiled for: 3 (default; more
-// warps to hide the gathers' latency, at the price of a few spills, measured
-// faster on the 1080p soup) or 2 (no spills; T3_SHADE_BLOCKS=2).  Read once.
-int shade_min_blocks() {
-  static int v = [] {
-    const char* e = getenv("T3_SHADE_BLOCKS");
-    return (e && e[0] == '2') ? 2 : 3;
-  }();
-  return v;
-}
-
-template <int NL, int MINB>
+template <int NL, int MODE>
 static void launch_shade_t(const DevScene* sc_dev, const unsigned long long* keys,
                            const float4* rec, const t3_outputs& out, int64_t npix, int H,
                            cudaStream_t st) {
   constexpr int BLOCK = 256, PPT = 4;
   const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
-  k_shade<BLOCK, PPT, NL, MINB><<<(unsigned)grid, BLOCK, 0, st>>>(sc_dev, keys, rec, out, npix, H);
+  k_shade<BLOCK, PPT, NL, MODE><<<(unsigned)grid, BLOCK, 0, st>>>(sc_dev, keys, rec, out, npix, H);
+}
+
+template <int MODE>
+static void launch_shade_m(const DevScene* sc_dev, const unsigned long long* keys,
+                           const float4* rec, const t3_outputs& out, int64_t npix, int H,
+                           int max_lobes, cudaStream_t st) {
+  if (max_lobes <= 1) launch_shade_t<1, MODE>(sc_dev, keys, rec, out, npix, H, st);
+  else if (max_lobes == 2) launch_shade_t<2, MODE>(sc_dev, keys, rec, out, npix, H, st);
+  else launch_shade_t<4, MODE>(sc_dev, keys, rec, out, npix, H, st);
 }
 
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                         const float4* rec, const t3_outputs& out, int max_lobes, cudaStream_t st) {
+                         const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
+                         cudaStream_t st) {
   const int64_t npix = (int64_t)fr.width * fr.height;
-  const bool b3 = shade_min_blocks() == 3;
-  const int H = fr.height;
-  if (max_lobes <= 1) {
-    if (b3) launch_shade_t<1, 3>(sc_dev, keys, rec, out, npix, H, st);
-    else launch_shade_t<1, 2>(sc_dev, keys, rec, out, npix, H, st);
-  } else if (max_lobes == 2) {
-    if (b3) launch_shade_t<2, 3>(sc_dev, keys, rec, out, npix, H, st);
-    else launch_shade_t<2, 2>(sc_dev, keys, rec, out, npix, H, st);
-  } else {
-    if (b3) launch_shade_t<4, 3>(sc_dev, keys, rec, out, npix, H, st);
-    else launch_shade_t<4, 2>(sc_dev, keys, rec, out, npix, H, st);
-  }
+  if (light_mode == T3_LIGHT_LAMPS)
+    launch_shade_m<T3_LIGHT_LAMPS>(sc_dev, keys, rec, out, npix, fr.height, max_lobes, st);
+  else if (light_mode == T3_LIGHT_IBL_MC)
+    launch_shade_m<T3_LIGHT_IBL_MC>(sc_dev, keys, rec, out, npix, fr.height, max_lobes, st);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

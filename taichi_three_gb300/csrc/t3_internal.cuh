@@ -35,6 +35,7 @@ struct BinArgs {
   int32_t tiles_x, tiles_y;
   int32_t big_tiles;     // faces touching more tiles than this go to the big list
   int32_t max_lobes;     // largest flattened material of the scene
+  int32_t light_mode;    // T3_LIGHT_*
 };
 
 // A material tree flattened into a sum of weighted leaf lobes:
@@ -43,6 +44,7 @@ struct BinArgs {
 // (1 - factor) to its first child and factor to its second, Scale its factor).
 // fac[j] = node index | T3_FAC_ONE_MINUS.
 #define T3_FAC_ONE_MINUS 0x10000
+#define T3_FAC_MIX 0x20000  // the factor comes from a Mix node (a sampling choice)
 struct DevLobe {
   int32_t kind;    // T3_OP_LAMBERT / PHONG / COOK / EMISSION
   int32_t nfac;
@@ -83,9 +85,9 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
 cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                         const float4* rec, const t3_outputs& out, int max_lobes, cudaStream_t st);
+                         const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
+                         cudaStream_t st);
 int max_lobes(const DevScene& sc);
-int shade_min_blocks();
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,
                         cudaStream_t st);

@@ -183,17 +183,48 @@ __device__ __forceinline__ void write_empty(const t3_frame& fr, const t3_outputs
   if (out.depth_f) out.depth_f[i] = __int_as_float(0x7f800000);
 }
 
-// Shades pixel (x, y) from its packed (depth, id) key and writes every output.
-// `rec` (nullable) holds the rasteriser's setup records (64 bytes per face id);
-// without it the face setup is recomputed, bit-identically.
-template <int NL>
-__device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
-                                                     const float4* __restrict__ rec,
-                                                     unsigned long long key, int x, int y,
-                                                     const t3_outputs& out) {
+} // namespace t3
+
+#include "t3_ibl.cuh"
+
+namespace t3 {
+
+// calc_view_ray (shader.py:82-87): the ray through pixel centre (px, py),
+// normalize(mapply_pos(V2W, (u, +1)) - mapply_pos(V2W, (u, -1)))
+__device__ __forceinline__ V3 view_ray(const t3_frame& fr, float px, float py) {
+  const float ux = __fdividef(px, (float)fr.width) * 2.0f - 1.0f;
+  const float uy = __fdividef(py, (float)fr.height) * 2.0f - 1.0f;
+  const float* M = fr.V2W;
+  const float bx = M[3] + M[0] * ux + M[1] * uy, by = M[7] + M[4] * ux + M[5] * uy;
+  const float bz = M[11] + M[8] * ux + M[9] * uy, bw = M[15] + M[12] * ux + M[13] * uy;
+  const float w0 = 1.0f / (bw - M[14]), w1 = 1.0f / (bw + M[14]);
+  const V3 ro = v3((bx - M[2]) * w0, (by - M[6]) * w0, (bz - M[10]) * w0);
+  const V3 ro1 = v3((bx + M[2]) * w1, (by + M[6]) * w1, (bz + M[10]) * w1);
+  return normalized(ro1 - ro);
+}
+
+// Everything shading needs about one covered pixel.
+struct PixelGeom {
+  int64_t i;          // pixel index x*H + y
+  const DevObject* ob;
+  Frag fg;
+  V3 vdir;            // calc_viewdir
+};
+
+// Decodes pixel (x, y)'s key, writes its raster outputs (face id, int depth,
+// float depth) and, when covered, fills `g` (interpolation of
+// triangle.py:32-49 and calc_viewdir of shader.py:82-93).  Returns false for
+// an empty pixel.  `rec` (nullable) holds the rasteriser's setup records
+// (64 bytes per face id); without it the face setup is recomputed,
+// bit-identically.
+__device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
+                                               const float4* __restrict__ rec,
+                                               unsigned long long key, int x, int y,
+                                               const t3_outputs& out, PixelGeom& g) {
   const t3_frame& fr = sc->frame;
   const int H = fr.height;
   const int64_t i = (int64_t)x * H + y;
+  g.i = i;
   // the object owning this face id (-1: empty pixel, or an id no object owns)
   int o = -1;
   if (key != T3_EMPTY_KEY) {
@@ -203,115 +234,148 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
       if (gid >= sc->obj[j].face_base && gid < sc->obj[j].face_base + sc->obj[j].nfaces) o = j;
     }
   }
-  V3 color;
-  int32_t fid = -1, depth = fr.maxdepth;
-  float depth_f = __int_as_float(0x7f800000);
   if (o < 0) {
-    color = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
-    if (out.face_id) out.face_id[i] = fid;
-    if (out.depth) out.depth[i] = depth;
-    if (out.depth_f) out.depth_f[i] = depth_f;
-  } else {
-    const uint32_t gid = (uint32_t)key;
-    fid = (int32_t)gid;
-    depth = (int32_t)((uint32_t)(key >> 32) ^ 0x80000000u);
-    const DevObject& ob = sc->obj[o];
-    const t3_mesh& mesh = ob.mesh;
-    const int64_t n = (int64_t)gid - ob.face_base;
-    const FaceRef ref = face_ref(mesh, n);
-    // start every gather of this face now: normals and material attributes are
-    // needed only after the weights, but their DRAM latency overlaps from here
-    if ((fr.flags & T3_SMOOTHING) && mesh.norms && !(mesh.flags & T3_MESH_FLAT_NORMAL)) {
+    if (out.face_id) out.face_id[i] = -1;
+    if (out.depth) out.depth[i] = fr.maxdepth;
+    if (out.depth_f) out.depth_f[i] = __int_as_float(0x7f800000);
+    return false;
+  }
+  const uint32_t gid = (uint32_t)key;
+  const DevObject& ob = sc->obj[o];
+  g.ob = &ob;
+  const t3_mesh& mesh = ob.mesh;
+  const int64_t n = (int64_t)gid - ob.face_base;
+  const FaceRef ref = face_ref(mesh, n);
+  // start every gather of this face now: normals and material attributes are
+  // needed only after the weights, but their DRAM latency overlaps from here
+  if ((fr.flags & T3_SMOOTHING) && mesh.norms && !(mesh.flags & T3_MESH_FLAT_NORMAL)) {
 #pragma unroll
-      for (int k = 0; k < 3; k++)
-        asm volatile("prefetch.global.L1 [%0];" :: "l"(base_ptr(mesh, ref.f, k, 1)));
-    }
-    if (mesh.face_attr)
-      asm volatile("prefetch.global.L1 [%0];" :: "l"(mesh.face_attr + ref.f * mesh.attr_stride));
-    f3 v[3];
-    face_verts(mesh, ref, v);
-    Setup s;
-    if (rec) {
-      const float4* r = rec + (size_t)gid * 4;
-      const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
-      s.bx = a.x; s.by = a.y; s.cx = a.z; s.cy = a.w;
-      s.bcnx = b.x; s.bcny = b.y; s.canx = b.z; s.cany = b.w;
-      s.wsa = c.x; s.wsb = c.y; s.wsc = c.z; s.Az = c.w;
-      s.Bz = d.x; s.Cz = d.y;
-    } else {
-      face_setup(fr, v, s);
-    }
-    const float px = xadd((float)x, fr.bias[0]), py = xadd((float)y, fr.bias[1]);
-    const f3 wei = face_weights(s, px, py);
-    depth_f = face_depth(s, wei);
-    // the raster outputs are final: store them now (shorter live ranges)
-    if (out.face_id) out.face_id[i] = fid;
-    if (out.depth) out.depth[i] = depth;
-    if (out.depth_f) out.depth_f[i] = depth_f;
+    for (int k = 0; k < 3; k++)
+      asm volatile("prefetch.global.L1 [%0];" :: "l"(base_ptr(mesh, ref.f, k, 1)));
+  }
+  if (mesh.face_attr)
+    asm volatile("prefetch.global.L1 [%0];" :: "l"(mesh.face_attr + ref.f * mesh.attr_stride));
+  f3 v[3];
+  face_verts(mesh, ref, v);
+  Setup s;
+  if (rec) {
+    const float4* r = rec + (size_t)gid * 4;
+    const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+    s.bx = a.x; s.by = a.y; s.cx = a.z; s.cy = a.w;
+    s.bcnx = b.x; s.bcny = b.y; s.canx = b.z; s.cany = b.w;
+    s.wsa = c.x; s.wsb = c.y; s.wsc = c.z; s.Az = c.w;
+    s.Bz = d.x; s.Cz = d.y;
+  } else {
+    face_setup(fr, v, s);
+  }
+  const float px = xadd((float)x, fr.bias[0]), py = xadd((float)y, fr.bias[1]);
+  const f3 wei = face_weights(s, px, py);
+  // the raster outputs are final: store them now (shorter live ranges)
+  if (out.face_id) out.face_id[i] = (int32_t)gid;
+  if (out.depth) out.depth[i] = (int32_t)((uint32_t)(key >> 32) ^ 0x80000000u);
+  if (out.depth_f) out.depth_f[i] = face_depth(s, wei);
 
-    // interpolate (triangle.py:32-49)
-    Frag fg;
-    const V3 A = tov(v[0]), B = tov(v[1]), C = tov(v[2]);
-    fg.pos = (wei.x * A + wei.y * B) + wei.z * C;
-    V3 nrm;
-    if (fr.flags & T3_SMOOTHING) {
-      f3 nn[3];
-      face_norms(mesh, ref, nn);
-      nrm = (wei.x * tov(nn[0]) + wei.y * tov(nn[1])) + wei.z * tov(nn[2]);
-    } else {
-      nrm = cross(B - A, C - A);
-    }
-    fg.normal = normalized(nrm);
-    fg.tex = f2{0.f, 0.f};
-    if (fr.flags & T3_TEXTURING) {
-      f2 t[3];
-      face_coors(mesh, ref, t);
-      fg.tex = f2{(wei.x * t[0].x + wei.y * t[1].x) + wei.z * t[2].x,
-                  (wei.x * t[0].y + wei.y * t[1].y) + wei.z * t[2].y};
-    }
-    fg.attr = mesh.face_attr ? mesh.face_attr + ref.f * mesh.attr_stride : nullptr;
-    // calc_viewdir (shader.py:82-93)
-    const float ux = __fdividef(px, (float)fr.width) * 2.0f - 1.0f;
-    const float uy = __fdividef(py, (float)H) * 2.0f - 1.0f;
-    const float* M = fr.V2W;
-    // mapply_pos(V2W, (u, -1)) and (u, +1), then the difference of the two
-    const float bx = M[3] + M[0] * ux + M[1] * uy, by = M[7] + M[4] * ux + M[5] * uy;
-    const float bz = M[11] + M[8] * ux + M[9] * uy, bw = M[15] + M[12] * ux + M[13] * uy;
-    const float w0 = 1.0f / (bw - M[14]), w1 = 1.0f / (bw + M[14]);
-    const V3 ro = v3((bx - M[2]) * w0, (by - M[6]) * w0, (bz - M[10]) * w0);
-    const V3 ro1 = v3((bx + M[2]) * w1, (by + M[6]) * w1, (bz + M[10]) * w1);
-    const V3 rd = normalized(ro1 - ro);
-    const V3 vdir = v3(-rd.x, -rd.y, -rd.z);
+  // interpolate (triangle.py:32-49)
+  Frag& fg = g.fg;
+  const V3 A = tov(v[0]), B = tov(v[1]), C = tov(v[2]);
+  fg.pos = (wei.x * A + wei.y * B) + wei.z * C;
+  V3 nrm;
+  if (fr.flags & T3_SMOOTHING) {
+    f3 nn[3];
+    face_norms(mesh, ref, nn);
+    nrm = (wei.x * tov(nn[0]) + wei.y * tov(nn[1])) + wei.z * tov(nn[2]);
+  } else {
+    nrm = cross(B - A, C - A);
+  }
+  fg.normal = normalized(nrm);
+  fg.tex = f2{0.f, 0.f};
+  if (fr.flags & T3_TEXTURING) {
+    f2 t[3];
+    face_coors(mesh, ref, t);
+    fg.tex = f2{(wei.x * t[0].x + wei.y * t[1].x) + wei.z * t[2].x,
+                (wei.x * t[0].y + wei.y * t[1].y) + wei.z * t[2].y};
+  }
+  fg.attr = mesh.face_attr ? mesh.face_attr + ref.f * mesh.attr_stride : nullptr;
+  const V3 rd = view_ray(fr, px, py);
+  g.vdir = v3(-rd.x, -rd.y, -rd.z);
+  return true;
+}
 
-    LobeState<NL> L;
-    V3 amb, emi;
-    eval_material<NL>(ob.mat, fg, vdir, L, amb, emi);
-
-    // Lighting.shade_color (lighting.py:84-98)
-    const t3_lighting& lt = sc->lighting;
-    color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
-    const int nl = lt.nlights;
-    for (int l = 0; l < nl; l++) {
-      const float4 ld = *reinterpret_cast<const float4*>(lt.lights[l].dir);
-      V3 ldir = v3(ld.x - fg.pos.x * ld.w, ld.y - fg.pos.y * ld.w, ld.z - fg.pos.z * ld.w);
-      const float d2 = dot(ldir, ldir);
-      const float inv_d = rsqrtf(d2);
-      ldir = inv_d * ldir;
-      const float cos_i = dot(fg.normal, ldir);
-      if (cos_i > 0.0f) {
-        const float4 lc = *reinterpret_cast<const float4*>(lt.lights[l].color);
-        const float s = cos_i * (inv_d * inv_d);
-        const V3 mcol = eval_brdf<NL>(L, fg.normal, ldir, vdir);
-        color = color + v3(s * lc.x, s * lc.y, s * lc.z) * mcol;
-      }
+// Lighting.shade_color's lamp loop (lighting.py:88-97) for the lobes in L
+template <int NL>
+__device__ __forceinline__ V3 lamps_term(const t3_lighting& lt, const LobeState<NL>& L,
+                                         const Frag& fg, V3 vdir) {
+  V3 color = v3(0.f, 0.f, 0.f);
+  const int nl = lt.nlights;
+  for (int l = 0; l < nl; l++) {
+    const float4 ld = *reinterpret_cast<const float4*>(lt.lights[l].dir);
+    V3 ldir = v3(ld.x - fg.pos.x * ld.w, ld.y - fg.pos.y * ld.w, ld.z - fg.pos.z * ld.w);
+    const float d2 = dot(ldir, ldir);
+    const float inv_d = rsqrtf(d2);
+    ldir = inv_d * ldir;
+    const float cos_i = dot(fg.normal, ldir);
+    if (cos_i > 0.0f) {
+      const float4 lc = *reinterpret_cast<const float4*>(lt.lights[l].color);
+      const float s = cos_i * (inv_d * inv_d);
+      const V3 mcol = eval_brdf<NL>(L, fg.normal, ldir, vdir);
+      color = color + v3(s * lc.x, s * lc.y, s * lc.z) * mcol;
     }
   }
+  return color;
+}
+
+__device__ __forceinline__ void store_rgb(const t3_frame& fr, const t3_outputs& out, int64_t i,
+                                          V3 color) {
   if (fr.flags & T3_TONEMAP) color = v3(aces(color.x), aces(color.y), aces(color.z));
   if (out.rgb) {
     out.rgb[3 * i] = color.x;
     out.rgb[3 * i + 1] = color.y;
     out.rgb[3 * i + 2] = color.z;
   }
+}
+
+// Shades pixel (x, y) from its packed (depth, id) key and writes every output.
+// MODE is the lighting (T3_LIGHT_LAMPS or T3_LIGHT_IBL_MC).
+template <int NL, int MODE>
+__device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
+                                                     const float4* __restrict__ rec,
+                                                     unsigned long long key, int x, int y,
+                                                     const t3_outputs& out) {
+  const t3_frame& fr = sc->frame;
+  PixelGeom g;
+  const t3_lighting& lt = sc->lighting;
+  if (!pixel_geometry(sc, rec, key, x, y, out, g)) {
+    V3 bg = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
+    if (MODE != T3_LIGHT_LAMPS) {
+      // Engine.render_background (engine.py:42-49): the sky along the view ray
+      const Env env{lt.env, lt.env_w, lt.env_h, lt.env_half};
+      bg = env_sample(env, view_ray(fr, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1])));
+    }
+    store_rgb(fr, out, (int64_t)x * fr.height + y, bg);
+    return;
+  }
+  V3 color;
+  if (MODE == T3_LIGHT_LAMPS) {
+    LobeState<NL> L;
+    V3 amb, emi;
+    eval_material<NL>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
+    color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
+    color = color + lamps_term<NL>(lt, L, g.fg, g.vdir);
+  } else {
+    // SkyboxLighting.shade_color (lighting.py:20-21): IBL + emission
+    IblLobes<NL> L;
+    V3 emi;
+    eval_ibl_lobes<NL>(g.ob->mat, g.fg, L, emi);
+    const Env env{lt.env, lt.env_w, lt.env_h, lt.env_half};
+    color = emi + ibl_mc<NL>(L, g.fg.normal, g.vdir, env, lt.spp, lt.seed, (uint32_t)g.i);
+    if (lt.nlights > 0) {
+      LobeState<NL> Ll;
+      V3 amb, e2;
+      eval_material<NL>(g.ob->mat, g.fg, g.vdir, Ll, amb, e2);
+      color = color + lamps_term<NL>(lt, Ll, g.fg, g.vdir);
+    }
+  }
+  store_rgb(fr, out, g.i, color);
 }
 
 } // namespace t3
