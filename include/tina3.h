@@ -224,7 +224,9 @@ int t3_raster(const t3_frame* frame, const t3_object* object,
 /* TriangleRaster.render_color + Shader + Lighting + ToneMapping
  * (tina/core/triangle.py:134-153, shader.py:119-131, lighting.py:84-98,
  * postp/tonemap.py:10-12) for all objects of the scene.  The workspace (at
- * least t3_workspace_size bytes) receives the device copy of the scene. */
+ * least t3_workspace_size bytes) receives the device copy of the scene.
+ * Lighting T3_LIGHT_LAMPS and T3_LIGHT_IBL_MC; T3_LIGHT_IBL_MLP returns
+ * T3_EUNSUPPORTED here (t3_render runs it and reports its device status). */
 int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
              size_t workspace_bytes, const t3_outputs* out, void* stream);
 

@@ -749,7 +749,8 @@ v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, in
   fg.attr = ob.mesh.face_attr ? ob.mesh.face_attr + bf * ob.mesh.attr_stride : nullptr;
   MaterialEval<R> me{&ob.material, &fg};
   const t3_lighting& L = cx.sc->lighting;
-  if (L.mode == T3_LIGHT_IBL_MC) {
+  // T3_LIGHT_IBL_MLP: the Monte Carlo estimator the network stands in for
+  if (L.mode == T3_LIGHT_IBL_MC || L.mode == T3_LIGHT_IBL_MLP) {
     const uint32_t pixel = (uint32_t)((int64_t)x * fr.height + y);
     const int spp = cx.spp > 0 ? cx.spp : L.spp;
     const uint32_t seed = cx.spp > 0 ? cx.seed : L.seed;

@@ -22,3 +22,5 @@ from .scene import Scene, Shader, TriangleRaster
 from .postp import ToneMapping, aces_tonemap
 from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from . import workloads
+from .mlp import IBLNet, train_for_skybox
+from . import colour

@@ -129,7 +129,9 @@ int make_dev_scene(const t3_scene& sc, DevScene& out) {
     if (!sc.lighting.env || sc.lighting.env_w < 2 || sc.lighting.env_h < 2) return T3_EINVAL;
     if (sc.lighting.mode == T3_LIGHT_IBL_MC && (sc.lighting.spp < 1 || sc.lighting.spp > (1 << 20)))
       return T3_EINVAL;
-    if (sc.lighting.mode == T3_LIGHT_IBL_MLP && !sc.lighting.mlp) return T3_EINVAL;
+    if (sc.lighting.mode == T3_LIGHT_IBL_MLP &&
+        (!sc.lighting.mlp || (reinterpret_cast<uintptr_t>(sc.lighting.mlp) & 15) != 0))
+      return T3_EINVAL;
   } else if (sc.lighting.mode != T3_LIGHT_LAMPS) {
     return T3_EINVAL;
   }
@@ -149,6 +151,16 @@ int make_dev_scene(const t3_scene& sc, DevScene& out) {
     out.obj[o].nfaces = ob.nfaces;
     r = flatten_material(ob.material, out.obj[o].mat);
     if (r) return r;
+    if (sc.lighting.mode == T3_LIGHT_IBL_MLP) {
+      // the network covers Lambert and one CookTorrance lobe (plus emission)
+      int cook = 0;
+      for (int k = 0; k < out.obj[o].mat.nlobes; k++) {
+        const int kind = out.obj[o].mat.lobes[k].kind;
+        if (kind == T3_OP_PHONG) return T3_EUNSUPPORTED;
+        cook += kind == T3_OP_COOK;
+      }
+      if (cook > 1) return T3_EUNSUPPORTED;
+    }
     // per-face attribute reads must stay inside the mesh's attribute rows
     for (int i = 0; i < ob.material.nnodes; i++) {
       const t3_node& nd = ob.material.nodes[i];
@@ -228,6 +240,11 @@ static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capaci
   if (mode == T3_RASTER_BINNED) {
     L.bins = after_rec;
     L.end = align256(L.bins + 4 * (size_t)L.tiles_x * L.tiles_y * L.bin_capacity);
+    if (sc.lighting.mode == T3_LIGHT_IBL_MLP) {
+      // the tiles hand their keys to the fused network shading pass
+      L.keys = L.end;
+      L.end = align256(L.keys + 8 * (size_t)sc.frame.width * (size_t)sc.frame.height);
+    }
   } else {
     L.keys = after_rec;
     L.end = align256(L.keys + 8 * (size_t)sc.frame.width * (size_t)sc.frame.height);
@@ -314,6 +331,8 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
              size_t workspace_bytes, const t3_outputs* out, void* stream) {
   if (!scene || !depth_id || !out || !out->rgb || !workspace) return T3_EINVAL;
   if (workspace_bytes < align256(sizeof(DevScene))) return T3_EINVAL;
+  // the network pass reports timeouts through a status word: t3_render has one
+  if (scene->lighting.mode == T3_LIGHT_IBL_MLP) return T3_EUNSUPPORTED;
   static thread_local DevScene ds;
   int r = make_dev_scene(*scene, ds);
   if (r) return r;
@@ -323,7 +342,7 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
   cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
   return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
-                              nullptr, *out, max_lobes(ds), ds.lighting.mode, st));
+                              nullptr, *out, max_lobes(ds), ds.lighting.mode, nullptr, st));
 }
 
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
@@ -370,7 +389,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
       e = launch_shade(dsc, scene->frame, keys, reinterpret_cast<const float4*>(ws + L.rec), *out,
-                       max_lobes(ds), ds.lighting.mode, st);
+                       max_lobes(ds), ds.lighting.mode, status, st);
   } else {
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -387,11 +406,15 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     b.big_tiles = 16;
     b.max_lobes = max_lobes(ds);
     b.light_mode = ds.lighting.mode;
+    b.keys = ds.lighting.mode == T3_LIGHT_IBL_MLP ? reinterpret_cast<unsigned long long*>(ws + L.keys)
+                                                  : nullptr;
     if (e == cudaSuccess) e = mark(1);
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++)
       e = launch_bin(scene->frame, scene->objects[o], b, st);
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
+    if (e == cudaSuccess && b.keys)
+      e = launch_shade(dsc, scene->frame, b.keys, b.rec, *out, b.max_lobes, ds.lighting.mode, status, st);
   }
   if (e == cudaSuccess) e = mark(3);
   return cuda_rc(e);

@@ -203,34 +203,42 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   }
   __syncthreads();
 
-  // shade the tile: empty pixels at once, covered ones compacted so full warps
-  // run the shading (consecutive threads take consecutive y: contiguous memory)
-  const V3 bg = background(fr);
-  const int lane = threadIdx.x & 31;
-  for (int i0 = 0; i0 < TS * TS; i0 += BLOCK) {
-    const int i = i0 + threadIdx.x;
-    const int x = x0 + i / TS, y = y0 + i % TS;
-    bool covered = false;
-    if (i < TS * TS && x <= x1 && y <= y1) {
-      if (MODE == T3_LIGHT_LAMPS && (!ok || keys[i] == T3_EMPTY_KEY))
-        write_empty(fr, out, (int64_t)x * H + y, bg);
-      else
-        covered = true;
+  if constexpr (MODE == T3_LIGHT_IBL_MLP) {
+    // the network runs in the fused shading pass: hand the keys to it
+    for (int i = threadIdx.x; i < TS * TS; i += BLOCK) {
+      const int x = x0 + i / TS, y = y0 + i % TS;
+      if (x <= x1 && y <= y1) bins.keys[(int64_t)x * H + y] = ok ? keys[i] : T3_EMPTY_KEY;
     }
-    const unsigned m = __ballot_sync(FULL, covered);
-    if (m) {
-      int slot = 0;
-      if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
-      slot = __shfl_sync(FULL, slot, 0);
-      if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = i;
+  } else {
+    // shade the tile: empty pixels at once, covered ones compacted so full warps
+    // run the shading (consecutive threads take consecutive y: contiguous memory)
+    const V3 bg = background(fr);
+    const int lane = threadIdx.x & 31;
+    for (int i0 = 0; i0 < TS * TS; i0 += BLOCK) {
+      const int i = i0 + threadIdx.x;
+      const int x = x0 + i / TS, y = y0 + i % TS;
+      bool covered = false;
+      if (i < TS * TS && x <= x1 && y <= y1) {
+        if (MODE == T3_LIGHT_LAMPS && (!ok || keys[i] == T3_EMPTY_KEY))
+          write_empty(fr, out, (int64_t)x * H + y, bg);
+        else
+          covered = true;
+      }
+      const unsigned m = __ballot_sync(FULL, covered);
+      if (m) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
+        slot = __shfl_sync(FULL, slot, 0);
+        if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = i;
+      }
     }
-  }
-  __syncthreads();
-  const int ncov = s_count;
-  for (int j = threadIdx.x; j < ncov; j += BLOCK) {
-    const int i = s_list[j];
-    shade_pixel_from_key<NL, MODE>(sc, bins.rec, ok ? keys[i] : T3_EMPTY_KEY, x0 + i / TS,
-                                   y0 + i % TS, out);
+    __syncthreads();
+    const int ncov = s_count;
+    for (int j = threadIdx.x; j < ncov; j += BLOCK) {
+      const int i = s_list[j];
+      shade_pixel_from_key<NL, MODE>(sc, bins.rec, ok ? keys[i] : T3_EMPTY_KEY, x0 + i / TS,
+                                     y0 + i % TS, out);
+    }
   }
   if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(bar_a) : "memory");
 }
@@ -261,6 +269,8 @@ static cudaError_t launch_tile_nl(const DevScene* sc, const BinArgs& bins, int n
     return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_LAMPS>(sc, bins, ntiles, out, st);
   if (bins.light_mode == T3_LIGHT_IBL_MC)
     return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_IBL_MC>(sc, bins, ntiles, out, st);
+  if (bins.light_mode == T3_LIGHT_IBL_MLP)  // visibility only: one instance serves every NL
+    return launch_tile_b<TS, BLOCK, 2, T3_LIGHT_IBL_MLP>(sc, bins, ntiles, out, st);
   return cudaErrorInvalidValue;
 }
 

@@ -16,8 +16,10 @@
 // shading composes them with the pixel's albedo, f0 and lobe weights, so one
 // network serves every albedo.
 //
-// Input encoding (400 floats): for each of the six coordinates of n and v,
-// sin and cos of pi * c * 2^(o + j/4), o = 0..7, j = 0..3 (32 frequencies),
+// Input encoding (400 floats): for each of the six coordinates of n and of the
+// mirrored view direction r = 2 (n . v) n - v (v's information in the frame of
+// the specular lobes), sin and cos of pi * c * 2^(o + j/4), o = 0..7, j = 0..3
+// (32 frequencies),
 // evaluated as one sincos per base phase j followed by double-angle steps;
 // then roughness, metallic, and zeros up to 400.
 #include "t3_shading.cuh"
@@ -89,22 +91,16 @@ __global__ void k_targets(Env env, Env irr, const float* __restrict__ nv, const 
 
 // ---- encoding --------------------------------------------------------------
 __device__ __forceinline__ void encode_features(const float nv[6], float rough, float metal, float* x) {
-#pragma unroll
+  float in[6];
+  mirror_inputs(nv, in);
+#pragma unroll 1
   for (int c = 0; c < 6; c++) {
+    float s[32], co[32];
+    encode_coord(in[c], s, co);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      float s, co;
-      // base phase pi * c * 2^(j/4)
-      sincospif(nv[c] * exp2f(0.25f * (float)j), &s, &co);
-#pragma unroll
-      for (int o = 0; o < 8; o++) {
-        const int f = o * 4 + j;
-        x[c * 64 + f] = s;
-        x[c * 64 + 32 + f] = co;
-        const float s2 = 2.0f * s * co, c2 = (co - s) * (co + s);  // double angle
-        s = s2;
-        co = c2;
-      }
+    for (int f = 0; f < 32; f++) {
+      x[c * 64 + f] = s[f];
+      x[c * 64 + 32 + f] = co[f];
     }
   }
   x[384] = rough;
@@ -127,30 +123,35 @@ __global__ void k_encode(const float* __restrict__ nv, const float* __restrict__
 // C[M, N] (ldc) = op(A)[M, K] * op(B)[K, N], op = transpose when tA / tB;
 // epilogue: + bias[N], then EPI 0 none, 1 ReLU, 2 multiply by (mask > 0)
 // (ReLU backward, mask [M, N] with ldc), beta 1 accumulates into C.
+// Split-K (gridDim.z > 1, for the weight gradients whose K is the batch):
+// block z sums K range [z * kchunk, (z + 1) * kchunk) and adds its partial
+// into C with atomicAdd (C zeroed beforehand; EPI 0, no bias, beta 0).
 template <int EPI>
 __global__ void __launch_bounds__(256)
 k_sgemm(int M, int N, int K, const float* __restrict__ A, int lda, bool tA,
         const float* __restrict__ B, int ldb, bool tB, float* __restrict__ C, int ldc,
-        const float* __restrict__ bias, const float* __restrict__ mask, float beta) {
+        const float* __restrict__ bias, const float* __restrict__ mask, float beta, int kchunk) {
   constexpr int TM = 64, TN = 64, TK = 16;
   __shared__ float As[TK][TM + 4];
   __shared__ float Bs[TK][TN + 4];
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 16 x 16 threads, 4 x 4 outputs each
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
   float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += TK) {
+  for (int k0 = kb; k0 < ke; k0 += TK) {
     for (int e = threadIdx.x; e < TK * TM; e += 256) {
-      const int kk = e / TM, mm = e % TM;
+      // transposed operands are read along m (contiguous), the others along k
+      const int kk = tA ? e / TM : e % TK, mm = tA ? e % TM : e / TK;
       const int m = m0 + mm, k = k0 + kk;
       float v = 0.0f;
-      if (m < M && k < K) v = tA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k];
+      if (m < M && k < ke) v = tA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k];
       As[kk][mm] = v;
     }
     for (int e = threadIdx.x; e < TK * TN; e += 256) {
-      const int kk = e / TN, nn = e % TN;
+      const int kk = tB ? e % TK : e / TN, nn = tB ? e / TK : e % TN;
       const int n = n0 + nn, k = k0 + kk;
       float v = 0.0f;
-      if (n < N && k < K) v = tB ? B[(int64_t)n * ldb + k] : B[(int64_t)k * ldb + n];
+      if (n < N && k < ke) v = tB ? B[(int64_t)n * ldb + k] : B[(int64_t)k * ldb + n];
       Bs[kk][nn] = v;
     }
     __syncthreads();
@@ -177,6 +178,10 @@ k_sgemm(int M, int N, int K, const float* __restrict__ A, int lda, bool tA,
       const int n = n0 + tx * 4 + j;
       if (n >= N) continue;
       float v = acc[i][j];
+      if (gridDim.z > 1) {
+        atomicAdd(C + (int64_t)m * ldc + n, v);
+        continue;
+      }
       if (beta != 0.0f) v += beta * C[(int64_t)m * ldc + n];
       if (bias) v += bias[n];
       if (EPI == 1) v = fmaxf(v, 0.0f);
@@ -191,7 +196,23 @@ static void sgemm(int M, int N, int K, const float* A, int lda, bool tA, const f
                   bool tB, float* C, int ldc, const float* bias, const float* mask, float beta,
                   cudaStream_t st) {
   dim3 grid((N + 63) / 64, (M + 63) / 64);
-  k_sgemm<EPI><<<grid, 256, 0, st>>>(M, N, K, A, lda, tA, B, ldb, tB, C, ldc, bias, mask, beta);
+  k_sgemm<EPI><<<grid, 256, 0, st>>>(M, N, K, A, lda, tA, B, ldb, tB, C, ldc, bias, mask, beta, K);
+}
+
+// C = A^T B over a long K (the batch), split into K chunks across ~2 waves of
+// blocks; C must be zero.
+static void sgemm_splitk(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
+                         int ldc, cudaStream_t st) {
+  const int tiles = ((N + 63) / 64) * ((M + 63) / 64);
+  int splits = (304 + tiles - 1) / tiles;
+  const int max_splits = (K + 255) / 256;  // at least 256 rows of K per block
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  const int kchunk = (((K + splits - 1) / splits) + 15) & ~15;
+  splits = (K + kchunk - 1) / kchunk;
+  dim3 grid((N + 63) / 64, (M + 63) / 64, splits);
+  k_sgemm<0><<<grid, 256, 0, st>>>(M, N, K, A, lda, true, B, ldb, false, C, ldc, nullptr, nullptr, 0.f,
+                                   kchunk);
 }
 
 // parameter layout (FP32): W1 [400,64] b1 [64] W2 [64,64] b2 W3 [64,64] b3 W4 [64,16] b4 [16]
@@ -433,21 +454,23 @@ int t3_mlp_backward(const float* params, const float* X, const float* acts, cons
   float* dY = dbuf;                        // [B, 16]
   float* dA = dbuf + (int64_t)B * O;       // [B, 64]
   float* dB = dA + (int64_t)B * H;         // [B, 64]
+  // the weight gradients are accumulated by split-K blocks: start from zero
+  if (cudaMemsetAsync(grads, 0, sizeof(float) * (size_t)kMlpParams, st) != cudaSuccess) return T3_ECUDA;
   k_mse<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(Y, targets, B, dY, loss);
   // layer 4
-  sgemm<0>(H, O, M, h3, H, true, dY, O, false, gW4, O, nullptr, nullptr, 0.f, st);
+  sgemm_splitk(H, O, M, h3, H, dY, O, gW4, O, st);
   k_colsum<<<O, 256, 0, st>>>(dY, B, O, gb4);
   sgemm<2>(M, H, O, dY, O, false, q.W4, O, true, dA, H, nullptr, h3, 0.f, st);  // dh3 * relu'
   // layer 3
-  sgemm<0>(H, H, M, h2, H, true, dA, H, false, gW3, H, nullptr, nullptr, 0.f, st);
+  sgemm_splitk(H, H, M, h2, H, dA, H, gW3, H, st);
   k_colsum<<<H, 256, 0, st>>>(dA, B, H, gb3);
   sgemm<2>(M, H, H, dA, H, false, q.W3, H, true, dB, H, nullptr, h2, 0.f, st);
   // layer 2
-  sgemm<0>(H, H, M, h1, H, true, dB, H, false, gW2, H, nullptr, nullptr, 0.f, st);
+  sgemm_splitk(H, H, M, h1, H, dB, H, gW2, H, st);
   k_colsum<<<H, 256, 0, st>>>(dB, B, H, gb2);
   sgemm<2>(M, H, H, dB, H, false, q.W2, H, true, dA, H, nullptr, h1, 0.f, st);
   // layer 1
-  sgemm<0>(T3_MLP_IN, H, M, X, T3_MLP_IN, true, dA, H, false, gW1, H, nullptr, nullptr, 0.f, st);
+  sgemm_splitk(T3_MLP_IN, H, M, X, T3_MLP_IN, dA, H, gW1, H, st);
   k_colsum<<<H, 256, 0, st>>>(dA, B, H, gb1);
   return rc_of(cudaGetLastError());
 }

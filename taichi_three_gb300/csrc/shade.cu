@@ -98,12 +98,14 @@ static void launch_shade_m(const DevScene* sc_dev, const unsigned long long* key
 
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
                          const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
-                         cudaStream_t st) {
+                         int32_t* status, cudaStream_t st) {
   const int64_t npix = (int64_t)fr.width * fr.height;
   if (light_mode == T3_LIGHT_LAMPS)
     launch_shade_m<T3_LIGHT_LAMPS>(sc_dev, keys, rec, out, npix, fr.height, max_lobes, st);
   else if (light_mode == T3_LIGHT_IBL_MC)
     launch_shade_m<T3_LIGHT_IBL_MC>(sc_dev, keys, rec, out, npix, fr.height, max_lobes, st);
+  else if (light_mode == T3_LIGHT_IBL_MLP)
+    return launch_shade_mlp(sc_dev, fr, keys, rec, out, max_lobes, status, st);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

@@ -1,0 +1,194 @@
+// shade_mlp.cu -- the deferred shading pass with the learned IBL term
+// (T3_LIGHT_IBL_MLP): interpolation and material evaluation on the CUDA cores,
+// the network on the tensor cores, fused in one persistent kernel.
+//
+// One CTA of 128 threads per SM (the packed network and the A / H operands
+// take 185 KB of shared memory).  The CTA walks its share of the frame in
+// chunks of 128 pixels: empty pixels get the sky along the view ray at once,
+// covered ones are appended to a shared list.  Whenever 128 covered pixels are
+// pending (or the frame is done), thread t takes list entry t: it interpolates
+// the fragment, evaluates the material into the weights of the network's nine
+// outputs, adds emission and any lamps, and writes its Fourier features as row
+// t of the A operand; one elected thread then issues the four layers'
+// tcgen05.mma (t3_mlp_tc.cuh), and thread t reads row t of the result from
+// tensor memory and composes the pixel:
+//   rgb = emission + lamps + cd * E_d + c1 * S1 + c2 * S2,
+// with (E_d, S1, S2) = expm1 of the network outputs, cd the summed Lambert lobe
+// weights, c1 / c2 the CookTorrance lobe weight times f0 / (1 - f0) -- the
+// expectation of the Monte Carlo estimator of t3_ibl.cuh (linear in the lobe
+// weights), with the integrals read from the network instead of sampled.
+#include "t3_shading.cuh"
+#include "t3_mlp_tc.cuh"
+
+namespace t3 {
+
+struct MlpCoeffs {
+  V3 cd, c1, c2, base;
+  float rough, metal;
+};
+
+// lobe weights of one fragment (materials of Lambert, CookTorrance and
+// Emission leaves with at most one CookTorrance; checked on the host)
+template <int NL>
+__device__ __forceinline__ void eval_mlp_coeffs(const DevMaterial& mat, const Frag& fg, MlpCoeffs& q) {
+  q.cd = q.c1 = q.c2 = q.base = v3(0.f, 0.f, 0.f);
+  q.rough = 1.0f;
+  q.metal = 0.0f;
+#pragma unroll
+  for (int k = 0; k < NL; k++) {
+    if (k >= mat.nlobes) continue;
+    const DevLobe& lb = mat.lobes[k];
+    V3 w = v3(1.f, 1.f, 1.f);
+    for (int j = 0; j < lb.nfac; j++) {
+      const int fj = lb.fac[j];
+      const V3 f = eval_value(mat, fj & 0xFFFF, fg);
+      w = w * ((fj & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
+    }
+    if (lb.kind == T3_OP_LAMBERT) {
+      q.cd = q.cd + w;
+    } else if (lb.kind == T3_OP_COOK) {
+      const V3 f0 = eval_value(mat, lb.p1, fg);
+      q.rough = eval_value(mat, lb.p0, fg).x;
+      q.c1 = q.c1 + w * f0;
+      q.c2 = q.c2 + w * one_minus(f0);
+      q.metal = fminf(1.0f, fmaxf(0.0f, (f0.x + f0.y + f0.z) * (1.0f / 3.0f)));
+    } else if (lb.kind == T3_OP_EMISSION) {
+      q.base = q.base + w;
+    }
+  }
+}
+
+// raster outputs of an empty pixel and the sky along its view ray
+__device__ __forceinline__ void write_sky(const t3_frame& fr, const Env& env, const t3_outputs& out,
+                                          int64_t i) {
+  const int H = fr.height;
+  const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
+  if (out.face_id) out.face_id[i] = -1;
+  if (out.depth) out.depth[i] = fr.maxdepth;
+  if (out.depth_f) out.depth_f[i] = __int_as_float(0x7f800000);
+  store_rgb(fr, out, i, env_sample(env, view_ray(fr, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1]))));
+}
+
+template <int NL>
+__global__ void __launch_bounds__(128, 1)
+k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
+            const float4* __restrict__ rec, t3_outputs out, int64_t npix, int32_t* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_list[256];  // pending covered pixels (< 128 carried + one chunk)
+  __shared__ int s_count;
+
+  const t3_frame& fr = sc->frame;
+  const t3_lighting& lt = sc->lighting;
+  const Env env{lt.env, lt.env_w, lt.env_h, lt.env_half};
+  const int H = fr.height;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) s_count = 0;
+  MlpTile t;
+  bool ok = mlp_begin(t, sm, &bar, &tmem_slot, lt.mlp);  // ends with a CTA barrier
+
+  const int64_t nchunks = (npix + 127) / 128;
+  int64_t chunk = blockIdx.x;
+  int pending = 0;
+  while (ok) {
+    // collect covered pixels until a full tile is pending or the frame is done
+    // (the loop condition is CTA-uniform: `pending` is read after a barrier)
+    while (pending < 128 && chunk < nchunks) {
+      const int64_t i = chunk * 128 + threadIdx.x;
+      bool covered = false;
+      if (i < npix) {
+        if (keys[i] == T3_EMPTY_KEY) write_sky(fr, env, out, i);
+        else covered = true;
+      }
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
+      if (m) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
+        slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+        if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = (int)i;
+      }
+      __syncthreads();
+      pending = s_count;
+      __syncthreads();  // every thread has read the count before the next appends
+      chunk += gridDim.x;
+    }
+    if (pending == 0) break;
+    const int n = pending < 128 ? pending : 128;
+
+    // thread t shades list entry t: geometry, lobe weights, lamps, features
+    bool mine = false;
+    int64_t pix = 0;
+    MlpCoeffs q;
+    if (threadIdx.x < n) {
+      pix = s_list[threadIdx.x];
+      const int x = (int)(pix / H), y = (int)(pix - (int64_t)x * H);
+      PixelGeom g;
+      if (pixel_geometry(sc, rec, keys[pix], x, y, out, g)) {
+        mine = true;
+        eval_mlp_coeffs<NL>(g.ob->mat, g.fg, q);
+        if (lt.nlights > 0) {
+          LobeState<NL> L;
+          V3 amb, emi;
+          eval_material<NL>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
+          q.base = q.base + lamps_term<NL>(lt, L, g.fg, g.vdir);
+        }
+        const float nv[6] = {g.fg.normal.x, g.fg.normal.y, g.fg.normal.z, g.vdir.x, g.vdir.y, g.vdir.z};
+        encode_row_bf16(nv, q.rough, q.metal, sm + kA, threadIdx.x);
+      } else {
+        store_rgb(fr, out, pix, env_sample(env, view_ray(fr, xadd((float)x, fr.bias[0]),
+                                                         xadd((float)y, fr.bias[1]))));
+      }
+    }
+    float y[16];
+    if (!mlp_tile(t, y)) {  // CTA-uniform outcome
+      ok = false;
+      break;
+    }
+    if (mine) {
+      const V3 ed = v3(fmaxf(0.f, expm1f(y[0])), fmaxf(0.f, expm1f(y[1])), fmaxf(0.f, expm1f(y[2])));
+      const V3 s1 = v3(fmaxf(0.f, expm1f(y[3])), fmaxf(0.f, expm1f(y[4])), fmaxf(0.f, expm1f(y[5])));
+      const V3 s2 = v3(fmaxf(0.f, expm1f(y[6])), fmaxf(0.f, expm1f(y[7])), fmaxf(0.f, expm1f(y[8])));
+      store_rgb(fr, out, pix, q.base + q.cd * ed + q.c1 * s1 + q.c2 * s2);
+    }
+    // drop the n entries just shaded (mlp_tile ended with a barrier, so every
+    // thread has read its entry)
+    const int rest = pending - n;
+    const int carry = threadIdx.x < rest ? s_list[n + threadIdx.x] : 0;
+    __syncthreads();
+    if (threadIdx.x < rest) s_list[threadIdx.x] = carry;
+    if (threadIdx.x == 0) s_count = rest;
+    __syncthreads();
+    pending = rest;
+  }
+  if (!ok && status && threadIdx.x == 0) atomicOr(status, T3_STATUS_TIMEOUT);
+  mlp_end(t);
+}
+
+template <int NL>
+static cudaError_t launch_shade_mlp_t(const DevScene* sc_dev, const unsigned long long* keys,
+                                      const float4* rec, const t3_outputs& out, int64_t npix,
+                                      int32_t* status, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_shade_mlp<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kMlpSmem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int64_t nchunks = (npix + 127) / 128;
+  const int grid = (int)(nchunks < nsm ? nchunks : nsm);
+  if (grid <= 0) return cudaSuccess;
+  k_shade_mlp<NL><<<grid, 128, kMlpSmem, st>>>(sc_dev, keys, rec, out, npix, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade_mlp(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
+                             const float4* rec, const t3_outputs& out, int max_lobes, int32_t* status,
+                             cudaStream_t st) {
+  const int64_t npix = (int64_t)fr.width * fr.height;
+  if (max_lobes <= 2) return launch_shade_mlp_t<2>(sc_dev, keys, rec, out, npix, status, st);
+  return launch_shade_mlp_t<4>(sc_dev, keys, rec, out, npix, status, st);
+}
+
+} // namespace t3

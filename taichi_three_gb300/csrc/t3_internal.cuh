@@ -36,6 +36,7 @@ struct BinArgs {
   int32_t big_tiles;     // faces touching more tiles than this go to the big list
   int32_t max_lobes;     // largest flattened material of the scene
   int32_t light_mode;    // T3_LIGHT_*
+  unsigned long long* keys;  // T3_LIGHT_IBL_MLP: the frame's packed keys, written by the tiles
 };
 
 // A material tree flattened into a sum of weighted leaf lobes:
@@ -86,7 +87,10 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
                          const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
-                         cudaStream_t st);
+                         int32_t* status, cudaStream_t st);
+cudaError_t launch_shade_mlp(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
+                             const float4* rec, const t3_outputs& out, int max_lobes, int32_t* status,
+                             cudaStream_t st);
 int max_lobes(const DevScene& sc);
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,

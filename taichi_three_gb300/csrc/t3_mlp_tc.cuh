@@ -15,6 +15,7 @@
 #pragma once
 
 #include "t3_tc.cuh"
+#include "tina3.h"
 
 namespace t3 {
 
@@ -31,6 +32,63 @@ struct MlpTile {
   uint32_t phase;   // parity of the next completion
   unsigned char* sm;
 };
+
+// Fourier features of one input coordinate c: s[f] = sin(pi c 2^(o + j/4)),
+// co[f] = cos(...), f = 4 o + j, o = 0..7, j = 0..3; one sincospi per base
+// phase j, then double-angle steps.  Shared by the training-side encoder and the
+// fused shading kernel, so both see the same FP32 features.
+__device__ __forceinline__ void encode_coord(float c, float s[32], float co[32]) {
+  const float base[4] = {1.0f, 1.189207115002721f, 1.4142135623730951f, 1.681792830507429f};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    float a, b;
+    sincospif(c * base[j], &a, &b);
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+      s[o * 4 + j] = a;
+      co[o * 4 + j] = b;
+      const float a2 = 2.0f * a * b, b2 = (b - a) * (b + a);
+      a = a2;
+      b = b2;
+    }
+  }
+}
+
+// The encoded directions: the normal n and the view direction v entered as its
+// mirror image about n, r = reflect(-v, n) = 2 (n . v) n - v -- the same
+// information, in the coordinates the specular lobes are centred on.
+__device__ __forceinline__ void mirror_inputs(const float nv[6], float in[6]) {
+  const float d = nv[0] * nv[3] + nv[1] * nv[4] + nv[2] * nv[5];
+  in[0] = nv[0];
+  in[1] = nv[1];
+  in[2] = nv[2];
+  in[3] = 2.0f * d * nv[0] - nv[3];
+  in[4] = 2.0f * d * nv[1] - nv[4];
+  in[5] = 2.0f * d * nv[2] - nv[5];
+}
+
+// Row `row` of the A operand (K = 400, BF16, core-matrix layout) from the six
+// direction coordinates (n, v), roughness and metallic.
+__device__ __forceinline__ void encode_row_bf16(const float nv[6], float rough, float metal,
+                                                unsigned char* A, int row) {
+  float in[6];
+  mirror_inputs(nv, in);
+#pragma unroll 1
+  for (int c = 0; c < 6; c++) {
+    float s[32], co[32];
+    encode_coord(in[c], s, co);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      *reinterpret_cast<uint4*>(A + tc_chunk_off(row, c * 64 + 8 * q, T3_MLP_IN)) = pack8_bf16(s + 8 * q);
+      *reinterpret_cast<uint4*>(A + tc_chunk_off(row, c * 64 + 32 + 8 * q, T3_MLP_IN)) =
+          pack8_bf16(co + 8 * q);
+    }
+  }
+  float tail[8] = {rough, metal, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  *reinterpret_cast<uint4*>(A + tc_chunk_off(row, 384, T3_MLP_IN)) = pack8_bf16(tail);
+  tail[0] = tail[1] = 0.0f;
+  *reinterpret_cast<uint4*>(A + tc_chunk_off(row, 392, T3_MLP_IN)) = pack8_bf16(tail);
+}
 
 // one layer: D[128 x N] (TMEM column col) = A[128 x K] * W^T
 __device__ __forceinline__ void mlp_issue_layer(const MlpTile& t, uint32_t a_off, uint32_t w_off, int K,

@@ -193,3 +193,18 @@ class IBLNet:
         net = cls(device=device)
         net.load_state_dict(torch.load(path, map_location='cpu'))
         return net
+
+
+def train_for_skybox(skybox, samples=1 << 24, spp=4096, steps=4000, batch=16384, lr=2e-3,
+                     lr_end=5e-5, irr_res=(256, 128), irr_spp=4096, seed=0, net=None, log_every=0):
+    """Trains an IBLNet for `skybox`: an irradiance map (irr_spp cosine samples
+    per texel), `samples` random (n, v, roughness, metallic) inputs with
+    spp-sample Monte Carlo targets, then `steps` Adam steps.  Returns
+    (net, losses)."""
+    irr = IBLNet.irradiance_map(skybox, res=irr_res, spp=irr_spp, seed=seed + 1)
+    nv, rough, metal = sample_directions(samples, seed=seed)
+    T = IBLNet.targets(skybox, irr, nv, rough, spp=spp, seed=seed + 2)
+    net = net or IBLNet(seed=seed)
+    losses = net.fit(nv, rough, metal, T, steps=steps, batch=batch, lr=lr, lr_end=lr_end, seed=seed,
+                     log_every=log_every)
+    return net, losses

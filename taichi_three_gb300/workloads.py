@@ -86,3 +86,21 @@ def soup_scene(ntri=1_000_000, res=(1920, 1080), seed=0, material='pbr', nlights
     scene.lighting.set_ambient_light([0.0, 0.0, 0.0])
     scene.engine.set_camera(lookat(back=(0, 0, 3)), perspective(60, res[0] / res[1]))
     return scene, mesh
+
+
+def ibl_soup_scene(ntri=1_000_000, res=(1920, 1080), seed=0, env_res=512, mode='mc', spp=256,
+                   mlp=None, skybox=None, nlights=0, **options):
+    """The soup of soup_scene lit by a procedural equirect environment
+    ((2*env_res) x env_res FP16: sky gradient + 12 Gaussian lobes) through
+    SkyboxLighting, Monte Carlo (mode 'mc', spp samples) or the learned
+    network (mode 'mlp'); nlights point lamps on top (0 by default)."""
+    from .skybox import Skybox, SkyboxLighting, procedural_sky
+    sky = skybox if skybox is not None else Skybox(procedural_sky(env_res, seed=seed))
+    light = SkyboxLighting(sky, mode=mode, spp=spp, seed=seed, mlp=mlp)
+    scene, mesh = soup_scene(ntri=ntri, res=res, seed=seed, nlights=0, ibl=True, lighting=light,
+                             **options)
+    if nlights:
+        pos, inten = point_lights(nlights, seed)
+        for p, i in zip(pos, inten):
+            light.add_light(pos=p.tolist(), color=[float(i)] * 3)
+    return scene, mesh

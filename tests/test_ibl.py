@@ -77,3 +77,67 @@ def test_mc_converges_to_fp64(cuda, oracle_mod):
         errs.append(np.abs(g['rgb'].reshape(-1, 3)[cov] - post).mean())
     print('mean |err| vs FP64 at 4 / 64 spp:', errs)
     assert errs[1] < 0.5 * errs[0]
+
+
+# ---------------------------------------------------------------------------
+# learned IBL (mode 'mlp'): the fused tensor-core shading pass
+# ---------------------------------------------------------------------------
+
+@pytest.fixture(scope='module')
+def small_net(cuda):
+    sky = tina.Skybox(tina.procedural_sky(32, seed=3))
+    net, _ = tina.train_for_skybox(sky, samples=1 << 16, spp=256, steps=300, batch=4096,
+                                   irr_res=(64, 32), irr_spp=256)
+    return sky, net
+
+
+def _mlp_scene(sky, net, raster='direct', nlights=0, tonemap=True, mode='mlp', spp=1):
+    light = tina.SkyboxLighting(sky, mode=mode, mlp=net, spp=spp)
+    scene = random_soup_scene(6, ntri=400, res=(96, 80), material='pbr', nlights=0, ibl=True,
+                              lighting=light, raster=raster, tonemap=tonemap)[0]
+    if nlights:
+        for k in range(nlights):
+            light.add_light(pos=[2.0 * (k + 1), 1.0, 3.0], color=[2.0, 2.0, 2.0])
+    return scene
+
+
+def test_mlp_frame_direct_and_binned(cuda, oracle_mod, small_net):
+    sky, net = small_net
+    gd = _render(_mlp_scene(sky, net, 'direct'))
+    gb = _render(_mlp_scene(sky, net, 'binned'))
+    o = oracle_mod.render(_mlp_scene(sky, net, 'direct', mode='mc'))
+    for g in (gd, gb):
+        assert np.array_equal(g['face_id'], o['face_id'])
+        assert np.array_equal(g['depth'], o['depth'])
+    assert np.array_equal(gd['rgb'], gb['rgb'])
+    assert np.isfinite(gd['rgb']).all()
+    bg = gd['face_id'] < 0
+    assert np.abs(gd['rgb'][bg] - o['rgb'][bg]).max() < 1e-4
+    cov = ~bg
+    assert cov.sum() > 1000 and gd['rgb'][cov].std() > 0.01
+
+
+def test_mlp_lamps_add_on_top(cuda, small_net):
+    """mode 'mlp' with lamps = mode 'mlp' without + the lamps' own frame."""
+    sky, net = small_net
+    a = _render(_mlp_scene(sky, net, nlights=2, tonemap=False))['rgb']
+    b = _render(_mlp_scene(sky, net, nlights=0, tonemap=False))['rgb']
+    sc = _mlp_scene(sky, net, nlights=0, tonemap=False)
+    lamps = tina.Lighting()
+    for k in range(2):
+        lamps.add_light(pos=[2.0 * (k + 1), 1.0, 3.0], color=[2.0, 2.0, 2.0])
+    lamps.set_ambient_light([0.0, 0.0, 0.0])
+    sc.lighting = lamps
+    c = _render(sc)
+    cov = c['face_id'] >= 0
+    err = np.abs(a[cov] - (b[cov] + c['rgb'][cov])) / np.maximum(1.0, np.abs(a[cov]))
+    assert err.max() < 1e-5
+
+
+def test_mlp_rejects_phong_materials(cuda, small_net):
+    sky, net = small_net
+    light = tina.SkyboxLighting(sky, mode='mlp', mlp=net)
+    scene = random_soup_scene(6, ntri=50, res=(32, 32), material='classic', nlights=0, ibl=True,
+                              lighting=light)[0]
+    with pytest.raises(RuntimeError):
+        scene.render()
