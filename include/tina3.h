@@ -279,6 +279,29 @@ int t3_event_elapsed_ms(void* start, void* end, float* ms); /* waits for `end` *
  * race and must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
 int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* out, void* stream);
 
+/* ---- batched multi-view rendering ------------------------------------------
+ * No reference counterpart: the reference renders one Scene per call
+ * (tina/scene/raster.py:168-207).  Up to T3_BATCH_MAX_SCENES independent
+ * frames (each its own t3_scene: resolution <= 4096 x 4096, camera, objects,
+ * lamps; lighting T3_LIGHT_LAMPS) are rendered by one persistent launch whose
+ * CTAs take raster and shading items from a global work queue. */
+#define T3_BATCH_MAX_SCENES 64
+
+typedef struct t3_batch_config {
+  int32_t faces_per_item;   /* faces per raster item, multiple of 256 (0: 1024)       */
+  int32_t pixels_per_item;  /* pixels per shading item, multiple of 1024 (0: 4096)    */
+  int32_t ctas_per_sm;      /* resident CTAs per SM, 1 or 2 (0: as many as fit)       */
+  int32_t _pad;
+} t3_batch_config;
+
+int t3_batch_workspace_size(const t3_scene* scenes, int nscenes, size_t* bytes);
+
+/* Renders scenes[i] into outs[i] for i < nscenes (every output as t3_render). */
+int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
+                    const t3_batch_config* config, void* workspace, size_t workspace_bytes,
+                    int32_t* status, void* stream);
+
+
 /* ---- MLP-IBL (learned image-based lighting) -------------------------------
  * The network maps (normal, view direction, roughness, metallic) to log1p of
  * the albedo-independent IBL integrals of the Lambert and CookTorrance lobes

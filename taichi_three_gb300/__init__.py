@@ -24,3 +24,5 @@ from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from . import workloads
 from .mlp import IBLNet, train_for_skybox
 from . import colour
+from .batch import BatchRenderer
+from .autotune import Autotuner, tune_scene

@@ -96,6 +96,13 @@ class t3_outputs(C.Structure):
                 ("depth_f", C.c_void_p)]
 
 
+class t3_batch_config(C.Structure):
+    _fields_ = [("faces_per_item", C.c_int32), ("pixels_per_item", C.c_int32),
+                ("ctas_per_sm", C.c_int32), ("_pad", C.c_int32)]
+
+
+T3_BATCH_MAX_SCENES = 64
+
 STRUCTS = [t3_frame, t3_mesh, t3_node, t3_material, t3_object, t3_light, t3_lighting, t3_scene,
            t3_outputs]
 
@@ -120,6 +127,9 @@ SIGNATURES = {
     "t3_render_staged": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,
                                    C.POINTER(t3_outputs), _VP, C.POINTER(C.c_void_p)]),
     "t3_render_noalloc": (C.c_int, [C.POINTER(t3_scene), _VP, C.POINTER(t3_outputs), _VP]),
+    "t3_batch_workspace_size": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.POINTER(C.c_size_t)]),
+    "t3_render_batch": (C.c_int, [C.POINTER(t3_scene), C.POINTER(t3_outputs), C.c_int,
+                                  C.POINTER(t3_batch_config), _VP, _SZ, _VP, _VP]),
     "t3_mlp_param_count": (C.c_int64, []),
     "t3_mlp_packed_bytes": (C.c_int64, []),
     "t3_mlp_irradiance_map": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

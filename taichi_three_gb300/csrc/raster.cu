@@ -36,9 +36,9 @@ struct GlobalKeySink {
   unsigned long long* keys;
   int64_t H;
   __device__ __forceinline__ void operator()(int x, int y, unsigned long long key) const {
-    unsigned long long* p = keys + (int64_t)x * H + y;
-    // keys only decrease: a stale read can only send us to the atomic
-    if (key < *reinterpret_cast<volatile unsigned long long*>(p)) atomicMin(p, key);
+    // fire-and-forget reduction (no return value, so no load latency on the
+    // fragment path)
+    atomicMin(keys + (int64_t)x * H + y, key);
   }
 };
 

@@ -36,9 +36,7 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
   return cudaGetLastError();
 }
 
-// Each block owns PPT * BLOCK consecutive pixels.  Empty pixels are written as
-// background at once; covered ones are compacted into a shared list (warp
-// ballot + one shared atomic per warp) so that full warps run the shading.
+// Each block owns PPT * BLOCK consecutive pixels (shade_block).
 template <int BLOCK, int PPT, int NL, int MODE>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
@@ -47,35 +45,9 @@ k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ 
   __shared__ int s_count;
   if (threadIdx.x == 0) s_count = 0;
   __syncthreads();
-  const t3_frame& fr = sc->frame;
-  const int64_t base = (int64_t)blockIdx.x * BLOCK * PPT;
-  const V3 bg = background(fr);
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 0; k < PPT; k++) {
-    const int local = k * BLOCK + threadIdx.x;
-    const int64_t i = base + local;
-    bool covered = false;
-    if (i < npix) {
-      // with IBL, empty pixels show the sky and go through the shading list too
-      if (MODE == T3_LIGHT_LAMPS && keys[i] == T3_EMPTY_KEY) write_empty(fr, out, i, bg);
-      else covered = true;
-    }
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
-    if (m) {
-      int slot = 0;
-      if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
-      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-      if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = local;
-    }
-  }
-  __syncthreads();
-  const int n = s_count;
-  for (int j = threadIdx.x; j < n; j += BLOCK) {
-    const int64_t i = base + s_list[j];
-    const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
-    shade_pixel_from_key<NL, MODE>(sc, rec, keys[i], x, y, out);
-  }
+  (void)H;
+  shade_block<BLOCK, PPT, NL, MODE>(sc, keys, rec, out, npix, (int64_t)blockIdx.x * BLOCK * PPT, s_list,
+                                    &s_count);
 }
 
 template <int NL, int MODE>

@@ -58,30 +58,20 @@ __device__ __forceinline__ void test_pixel(const Setup& t, int x, int y, uint32_
 
 // Every lane of the warp must call this.  `active` lanes contribute the face
 // `s` clipped to [cx0, cx1] x [cy0, cy1]; sink(x, y, key) receives every
-// covered pixel with its packed (depth, id) key.  Faces of at most
-// kSmallArea pixels walk their own pixels (a short, nearly uniform loop);
-// larger ones go through the cooperative prefix-sum walk.
+// covered pixel with its packed (depth, id) key.  Every face, however small,
+// goes through the cooperative prefix-sum walk (measured faster than letting
+// faces of a few pixels walk their own bbox per lane).
 template <class Sink>
 __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool active, uint32_t id,
                                             int cx0, int cx1, int cy0, int cy1,
                                             const t3_frame& fr, Sink sink) {
-  constexpr int kSmallArea = 4;
   const unsigned FULL = 0xFFFFFFFFu;
   const int lane = threadIdx.x & 31;
   const int x0 = max(s.botx, cx0), x1 = min(s.topx, cx1);
   const int y0 = max(s.boty, cy0), y1 = min(s.topy, cy1);
-  const int full_area = (active && x0 <= x1 && y0 <= y1) ? (x1 - x0 + 1) * (y1 - y0 + 1) : 0;
+  const int area = (active && x0 <= x1 && y0 <= y1) ? (x1 - x0 + 1) * (y1 - y0 + 1) : 0;
   const float maxd = (float)fr.maxdepth;
   const float biasx = fr.bias[0], biasy = fr.bias[1];
-  // small faces: per-lane walk
-  if (full_area > 0 && full_area <= kSmallArea) {
-    const int h = y1 - y0 + 1;
-    for (int k = 0; k < full_area; k++) {
-      const int q = k / h;  // h <= 4
-      test_pixel(s, x0 + q, y0 + (k - q * h), id, biasx, biasy, maxd, fr.maxdepth, sink);
-    }
-  }
-  const int area = full_area > kSmallArea ? full_area : 0;
   if (!__any_sync(FULL, area > 0)) return;
   if (area > 0) {
     wf.bx[lane] = s.bx; wf.by[lane] = s.by; wf.cx[lane] = s.cx; wf.cy[lane] = s.cy;

@@ -216,7 +216,9 @@ struct PixelGeom {
 // triangle.py:32-49 and calc_viewdir of shader.py:82-93).  Returns false for
 // an empty pixel.  `rec` (nullable) holds the rasteriser's setup records
 // (64 bytes per face id); without it the face setup is recomputed,
-// bit-identically.
+// bit-identically.  COHERENT_REC: the records were written by the same kernel
+// launch (read through L2, not the read-only path).
+template <bool COHERENT_REC = false>
 __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
                                                const float4* __restrict__ rec,
                                                unsigned long long key, int x, int y,
@@ -260,7 +262,12 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   Setup s;
   if (rec) {
     const float4* r = rec + (size_t)gid * 4;
-    const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+    float4 a, b, c, d;
+    if (COHERENT_REC) {
+      a = __ldcg(r); b = __ldcg(r + 1); c = __ldcg(r + 2); d = __ldcg(r + 3);
+    } else {
+      a = __ldg(r); b = __ldg(r + 1); c = __ldg(r + 2); d = __ldg(r + 3);
+    }
     s.bx = a.x; s.by = a.y; s.cx = a.z; s.cy = a.w;
     s.bcnx = b.x; s.bcny = b.y; s.canx = b.z; s.cany = b.w;
     s.wsa = c.x; s.wsb = c.y; s.wsc = c.z; s.Az = c.w;
@@ -336,7 +343,7 @@ __device__ __forceinline__ void store_rgb(const t3_frame& fr, const t3_outputs& 
 
 // Shades pixel (x, y) from its packed (depth, id) key and writes every output.
 // MODE is the lighting (T3_LIGHT_LAMPS or T3_LIGHT_IBL_MC).
-template <int NL, int MODE>
+template <int NL, int MODE, bool COHERENT_REC = false>
 __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
                                                      const float4* __restrict__ rec,
                                                      unsigned long long key, int x, int y,
@@ -344,7 +351,7 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
   const t3_frame& fr = sc->frame;
   PixelGeom g;
   const t3_lighting& lt = sc->lighting;
-  if (!pixel_geometry(sc, rec, key, x, y, out, g)) {
+  if (!pixel_geometry<COHERENT_REC>(sc, rec, key, x, y, out, g)) {
     V3 bg = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
     if (MODE != T3_LIGHT_LAMPS) {
       // Engine.render_background (engine.py:42-49): the sky along the view ray
@@ -376,6 +383,49 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     }
   }
   store_rgb(fr, out, g.i, color);
+}
+
+// One block's share of the shading pass: pixels [base, base + BLOCK * PPT) of
+// the frame.  Empty pixels are written as background at once; covered ones are
+// compacted into a shared list (warp ballot + one shared atomic per warp) so
+// that full warps run the shading.  s_list holds BLOCK * PPT entries; s_count
+// must be zero on entry and is left non-zero (callers reset it after a barrier).
+template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false>
+__device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
+                                            const unsigned long long* __restrict__ keys,
+                                            const float4* __restrict__ rec, const t3_outputs& out,
+                                            int64_t npix, int64_t base, int* s_list, int* s_count) {
+  const t3_frame& fr = sc->frame;
+  const int H = fr.height;
+  const V3 bg = background(fr);
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < PPT; k++) {
+    const int local = k * BLOCK + threadIdx.x;
+    const int64_t i = base + local;
+    bool covered = false;
+    if (i < npix) {
+      // with IBL, empty pixels show the sky and go through the shading list too
+      const unsigned long long key = COHERENT ? __ldcg(keys + i) : keys[i];
+      if (MODE == T3_LIGHT_LAMPS && key == T3_EMPTY_KEY) write_empty(fr, out, i, bg);
+      else covered = true;
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
+    if (m) {
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(s_count, __popc(m));
+      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+      if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = local;
+    }
+  }
+  __syncthreads();
+  const int n = *s_count;
+  for (int j = threadIdx.x; j < n; j += BLOCK) {
+    const int64_t i = base + s_list[j];
+    const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
+    const unsigned long long key = COHERENT ? __ldcg(keys + i) : keys[i];
+    shade_pixel_from_key<NL, MODE, COHERENT>(sc, rec, key, x, y, out);
+  }
 }
 
 } // namespace t3

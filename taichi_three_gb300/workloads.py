@@ -104,3 +104,24 @@ def ibl_soup_scene(ntri=1_000_000, res=(1920, 1080), seed=0, env_res=512, mode='
         for p, i in zip(pos, inten):
             light.add_light(pos=p.tolist(), color=[float(i)] * 3)
     return scene, mesh
+
+
+def batch_scenes(n=64, seed=0, t_min=1_000, t_max=2_000_000, resolutions=(256, 512, 768, 1024),
+                 nlights=8, material='classic'):
+    """Multi-view batch: n soups with T_i = round(exp(U[ln t_min, ln t_max]))
+    faces from the soup generator (seed + i), square resolution drawn from
+    `resolutions`, camera uniform on the radius-3 sphere looking at the origin,
+    Classic (Lambert + Phong) per-face albedo, nlights point lamps."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    scenes = []
+    for i in range(n):
+        T = int(round(np.exp(rng.uniform(np.log(t_min), np.log(t_max)))))
+        res = int(rng.choice(resolutions))
+        d = rng.normal(size=3)
+        d = d / np.linalg.norm(d) * 3.0
+        up = (0, 1, 1e-12) if abs(d[1]) < 2.9 else (1, 0, 1e-12)
+        scene, _ = soup_scene(ntri=T, res=(res, res), seed=seed * 1000 + i, material=material,
+                              nlights=nlights)
+        scene.engine.set_camera(lookat(back=tuple(d), up=up), perspective(60, 1.0))
+        scenes.append(scene)
+    return scenes

@@ -1,0 +1,111 @@
+"""Batched multi-view rendering (t3_render_batch, one persistent launch over a
+global work queue) against per-scene Scene.render and the oracle, plus the
+autotuner (its caching logic on the CPU, its choice on the GPU)."""
+import json
+
+import numpy as np
+import pytest
+
+import taichi_three_gb300 as tina
+from taichi_three_gb300.autotune import Autotuner
+
+
+def test_autotuner_picks_fastest_and_persists(tmp_path):
+    cost = {1: 5.0, 2: 1.0, 3: 3.0}
+    calls = []
+    clock = {'t': 0.0}
+
+    def timer(fn):
+        fn()
+        return clock['t']
+
+    def run(c):
+        calls.append(c['k'])
+        clock['t'] = cost[c['k']]
+
+    path = str(tmp_path / 'tune.json')
+    t = Autotuner(path=path, timer=timer)
+    best, ms = t.tune(('w', 1), [dict(k=1), dict(k=2), dict(k=3)], run, repeats=2)
+    assert best == dict(k=2) and ms == 1.0
+    assert len(calls) == 9  # warm-up + 2 timed runs per candidate
+    again = t.tune(('w', 1), [dict(k=1)], run)
+    assert again == (dict(k=2), 1.0) and len(calls) == 9  # cached
+    t2 = Autotuner(path=path, timer=timer)
+    assert t2.tune(('w', 1), [dict(k=3)], run)[0] == dict(k=2)
+    assert json.load(open(path))
+
+
+def _small_batch(seed=0):
+    scenes = tina.workloads.batch_scenes(6, seed=seed, t_min=200, t_max=30000,
+                                         resolutions=(64, 96, 128, 200))
+    # one scene with a face far larger than the CTA-cooperative threshold
+    big = tina.Scene(256, 256, tonemap=True, smoothing=True)
+    verts = np.array([[[-0.99, -0.99, 0.2], [0.99, -0.99, 0.2], [0, 0.99, 0.2]],
+                      [[-0.5, -0.5, 0.5], [0.5, -0.5, 0.5], [0, 0.5, 0.5]]], np.float32)
+    m = tina.SimpleMesh()
+    m.set_face_verts(verts)
+    m.set_face_norms(np.tile(np.array([0, 0, 1], np.float32), (2, 3, 1)))
+    big.add_object(m, tina.Classic())
+    scenes.append(big)
+    return scenes
+
+
+def _outputs(scene):
+    import torch
+    torch.cuda.synchronize()
+    return (scene.img.cpu().numpy().copy(), scene.face_id.cpu().numpy().copy(),
+            scene.engine.depth.cpu().numpy().copy(), scene.depth_f.cpu().numpy().copy())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('config', [dict(), dict(faces_per_item=256, pixels_per_item=1024, ctas_per_sm=1),
+                                    dict(faces_per_item=4096, pixels_per_item=16384, ctas_per_sm=2)])
+def test_batch_matches_single_renders(cuda, config):
+    scenes = _small_batch()
+    ref = []
+    for s in scenes:
+        s.render()
+        ref.append(_outputs(s))
+    b = tina.BatchRenderer(scenes, **config)
+    b.render()
+    assert b.status() == 0
+    for s, (rgb, fid, dep, dpf) in zip(scenes, ref):
+        g = _outputs(s)
+        assert np.array_equal(g[1], fid)
+        assert np.array_equal(g[2], dep)
+        assert np.array_equal(g[3].view(np.uint32), dpf.view(np.uint32))
+        assert np.abs(g[0] - rgb).max() <= 1e-5
+    assert (ref[-1][1] == 0).sum() > 25000  # the big face covers most of its frame
+
+
+@pytest.mark.gpu
+def test_batch_against_oracle(cuda, oracle_mod):
+    scenes = _small_batch(1)[:3]
+    tina.BatchRenderer(scenes).render()
+    for s in scenes:
+        g = _outputs(s)
+        o = oracle_mod.render(s)
+        assert np.array_equal(g[1], o['face_id'])
+        assert np.array_equal(g[2], o['depth'])
+        assert np.abs(g[0] - o['rgb']).max() <= 1e-4
+
+
+@pytest.mark.gpu
+def test_batch_autotune(cuda):
+    scenes = _small_batch(2)
+    b = tina.BatchRenderer(scenes)
+    cands = [dict(faces_per_item=256, pixels_per_item=1024, ctas_per_sm=1),
+             dict(faces_per_item=1024, pixels_per_item=4096, ctas_per_sm=2)]
+    cfg, ms = b.autotune(candidates=cands, tuner=Autotuner())
+    assert cfg in cands and ms > 0
+    b.render()
+    assert b.status() == 0
+
+
+@pytest.mark.gpu
+def test_tune_scene(cuda):
+    scene, _ = tina.workloads.soup_scene(ntri=20000, res=(160, 120), seed=3)
+    cfg, ms = tina.tune_scene(scene, tuner=Autotuner())
+    assert cfg['raster'] in ('direct', 'binned') and ms > 0
+    scene.render()
+    assert scene.status() == 0
