@@ -283,14 +283,15 @@ int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* 
  * No reference counterpart: the reference renders one Scene per call
  * (tina/scene/raster.py:168-207).  Up to T3_BATCH_MAX_SCENES independent
  * frames (each its own t3_scene: resolution <= 4096 x 4096, camera, objects,
- * lamps; lighting T3_LIGHT_LAMPS) are rendered by one persistent launch whose
- * CTAs take raster and shading items from a global work queue. */
+ * lamps; lighting T3_LIGHT_LAMPS) are rasterised by one persistent launch whose
+ * CTAs take (scene, object, face chunk) items from a global work queue, then
+ * shaded by a second persistent launch over (scene, pixel chunk) items. */
 #define T3_BATCH_MAX_SCENES 64
 
 typedef struct t3_batch_config {
   int32_t faces_per_item;   /* faces per raster item, multiple of 256 (0: 1024)       */
   int32_t pixels_per_item;  /* pixels per shading item, multiple of 1024 (0: 4096)    */
-  int32_t ctas_per_sm;      /* resident CTAs per SM, 1 or 2 (0: as many as fit)       */
+  int32_t ctas_per_sm;      /* cap on resident CTAs per SM, 1..8 (0: as many as fit)  */
   int32_t _pad;
 } t3_batch_config;
 

@@ -3,8 +3,9 @@
 No reference counterpart (Tina renders one Scene per Scene.render call,
 tina/scene/raster.py:168-207).  A BatchRenderer holds up to 64 Scenes (each
 with its own resolution, camera, objects and lamps) and renders all of them
-with one persistent CUDA launch whose CTAs take raster and shading items from
-a global work queue; each Scene's img / face_id / depth / depth_f are written
+with two persistent CUDA launches -- every scene's rasterisation in one, every
+scene's shading in the next -- whose CTAs take work items from global queues;
+each Scene's img / face_id / depth / depth_f are written
 exactly as Scene.render would write them.  BatchRenderer.autotune times the
 work-item sizes and residency on the actual batch and keeps the fastest.
 """
@@ -51,7 +52,7 @@ class BatchRenderer:
         return descs, outs, keep
 
     def render(self, config=None):
-        """Renders every scene of the batch (one persistent launch)."""
+        """Renders every scene of the batch (one raster launch, one shading launch)."""
         require_cuda('BatchRenderer.render')
         lib = N.load()
         dev = default_device()
@@ -84,7 +85,7 @@ class BatchRenderer:
         return ('batch', tuple(sig))
 
     CANDIDATES = [dict(faces_per_item=f, pixels_per_item=p, ctas_per_sm=c)
-                  for f in (256, 1024, 4096) for p in (1024, 4096, 16384) for c in (1, 2)]
+                  for f in (256, 1024, 4096) for p in (1024, 4096, 16384) for c in (0, 2)]
 
     def autotune(self, candidates=None, tuner=None, repeats=3):
         """Times each candidate configuration on this batch (CUDA events,

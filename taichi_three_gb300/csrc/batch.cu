@@ -1,4 +1,5 @@
-// batch.cu -- many views in one persistent launch driven by a global work queue.
+// batch.cu -- many views rendered by two persistent launches driven by global
+// work queues.
 //
 // A batch is up to T3_BATCH_MAX_SCENES independent frames (own resolution,
 // camera, objects, lamps).  Their work is cut into items:
@@ -7,13 +8,11 @@
 //                 buffer (atomicMin), setup records for shading;
 //   shade items   (scene, chunk of pixels_per_item pixels): the deferred
 //                 shading pass of that scene's pixels.
-// All raster items precede all shade items in the queue.  CTAs of one
-// persistent grid take items from a global counter; after a raster item a CTA
-// publishes it (fence, then a per-scene done counter).  A shade item of scene s
-// first waits until every raster item of s is done.  The wait cannot deadlock:
-// a CTA takes a shade item only after every raster item has been taken, and a
-// CTA holding a raster item never waits, so every awaited item completes.  The
-// wait is bounded all the same (status T3_STATUS_TIMEOUT).
+// One persistent grid takes every raster item of every scene from a global
+// counter, then a second persistent grid takes every shade item the same way:
+// the whole batch's rasterisation is one launch, load-balanced across scenes
+// of very different sizes, and each phase runs at its own occupancy (the
+// raster walk wants many light threads, shading fewer heavy ones).
 //
 // Faces whose bbox exceeds kBigArea pixels are kept out of the warps' walk and
 // rasterised by the whole CTA after its chunk (a CTA-wide stride over the bbox).
@@ -43,9 +42,7 @@ struct BatchArgs {
   int32_t faces_per_item;   // multiple of kBatchBlock
   int32_t pixels_per_item;  // multiple of kBatchBlock * kBatchPPT
   uint32_t n_raster, n_items;
-  uint32_t* queue;          // global item counter
-  uint32_t* done;           // [nscenes] completed raster items
-  int32_t* status;
+  uint32_t* queue;          // [0] raster item counter, [1] shade item counter
   BatchView v[T3_BATCH_MAX_SCENES];
   uint32_t obj_item0[T3_BATCH_MAX_SCENES][T3_MAX_OBJECTS + 1];  // first item of each object (+ end)
 };
@@ -71,124 +68,107 @@ __device__ __forceinline__ int find_scene(const BatchArgs& a, uint32_t g, bool s
   return lo;
 }
 
-template <int NL>
-__global__ void __launch_bounds__(kBatchBlock, 3) k_batch(const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(kBatchBlock, 4) k_batch_raster(const __grid_constant__ BatchArgs a) {
   __shared__ __align__(16) float sv[kBatchBlock * 9];
   __shared__ WarpFaces wfs[kBatchBlock / 32];
-  __shared__ int s_list[kBatchBlock * kBatchPPT];
-  __shared__ int s_count;
   __shared__ uint32_t s_item;
   __shared__ uint32_t s_big[kBigSlots];
   __shared__ int s_nbig;
-  __shared__ int s_ok;
 
   for (;;) {
     if (threadIdx.x == 0) {
       s_item = atomicAdd(a.queue, 1u);
-      s_count = 0;
       s_nbig = 0;
-      s_ok = 1;
     }
     __syncthreads();
     const uint32_t g = s_item;
-    if (g >= a.n_items) break;
-    if (g < a.n_raster) {
-      const int s = find_scene(a, g, false);
-      const BatchView& v = a.v[s];
-      const DevScene* sc = v.sc;
-      const t3_frame& fr = sc->frame;
-      int o = 0;
-      while (o + 1 < sc->nobjects && a.obj_item0[s][o + 1] <= g) o++;
-      const DevObject& ob = sc->obj[o];
-      const int64_t first = (int64_t)(g - a.obj_item0[s][o]) * a.faces_per_item;
-      const int64_t last = min(first + a.faces_per_item, ob.nfaces);
-      GlobalSink sink{v.keys, fr.height};
-      for (int64_t f0 = first; f0 < last; f0 += kBatchBlock) {
-        const bool staged = stage_soup<kBatchBlock>(ob.mesh, last, f0, sv);
-        const int64_t n = f0 + threadIdx.x;
-        Setup st{};
-        bool vis = false;
-        if (n < last) {
-          f3 vv[3];
-          load_face(ob.mesh, n, staged, sv, vv);
-          vis = face_setup(fr, vv, st) && st.botx <= st.topx && st.boty <= st.topy;
-        }
-        const uint32_t gid = (uint32_t)(ob.face_base + n);
-        if (vis) {
-          store_record(v.rec, gid, st);
-          const int64_t area = (int64_t)(st.topx - st.botx + 1) * (int64_t)(st.topy - st.boty + 1);
-          if (area > kBigArea) {
-            const int slot = atomicAdd(&s_nbig, 1);
-            if (slot < kBigSlots) {
-              s_big[slot] = (uint32_t)n;
-              vis = false;
-            }
-            // beyond the slots the face stays in the warp walk (correct, slower)
-          }
-        }
-        warp_raster(wfs[threadIdx.x >> 5], st, vis, gid, 0, fr.width - 1, 0, fr.height - 1, fr, sink);
-        __syncthreads();  // sv is restaged by the next pass
-      }
-      // big faces of this chunk: the whole CTA strides over each bbox
-      const int nbig = min(s_nbig, kBigSlots);
-      const float maxd = (float)fr.maxdepth;
-      for (int b = 0; b < nbig; b++) {
-        const int64_t n = s_big[b];
+    if (g >= a.n_raster) break;
+    const int s = find_scene(a, g, false);
+    const BatchView& v = a.v[s];
+    const DevScene* sc = v.sc;
+    const t3_frame& fr = sc->frame;
+    int o = 0;
+    while (o + 1 < sc->nobjects && a.obj_item0[s][o + 1] <= g) o++;
+    const DevObject& ob = sc->obj[o];
+    const int64_t first = (int64_t)(g - a.obj_item0[s][o]) * a.faces_per_item;
+    const int64_t last = min(first + a.faces_per_item, ob.nfaces);
+    GlobalSink sink{v.keys, fr.height};
+    for (int64_t f0 = first; f0 < last; f0 += kBatchBlock) {
+      const bool staged = stage_soup<kBatchBlock>(ob.mesh, last, f0, sv);
+      const int64_t n = f0 + threadIdx.x;
+      Setup st{};
+      bool vis = false;
+      if (n < last) {
         f3 vv[3];
-        face_verts(ob.mesh, face_ref(ob.mesh, n), vv);
-        Setup st;
-        if (!face_setup(fr, vv, st)) continue;  // CTA-uniform
-        const int32_t h = st.topy - st.boty + 1;
-        const int64_t area = (int64_t)(st.topx - st.botx + 1) * h;
-        const uint32_t gid = (uint32_t)(ob.face_base + n);
-        for (int64_t k = threadIdx.x; k < area; k += kBatchBlock) {
-          const int32_t x = st.botx + (int32_t)(k / h);
-          const int32_t y = st.boty + (int32_t)(k - (k / h) * h);
-          float wx, wy, wz, sum;
-          face_raw_weights(st, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1]), wx, wy, wz, sum);
-          f3 wei;
-          if (!face_inside(wx, wy, wz, sum, wei)) continue;
-          const int32_t d = trunc_i32(xmul(face_depth(st, wei), maxd));
-          if (d < fr.maxdepth) sink(x, y, pack_key(d, gid));
-        }
+        load_face(ob.mesh, n, staged, sv, vv);
+        vis = face_setup(fr, vv, st) && st.botx <= st.topx && st.boty <= st.topy;
       }
-      // publish: every thread's key reductions and records, then the count
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(a.done + s, 1u);
-    } else {
-      const uint32_t gs = g - a.n_raster;
-      const int s = find_scene(a, gs, true);
-      const BatchView& v = a.v[s];
-      if (threadIdx.x == 0) {
-        // wait for the scene's raster items (bounded; see the file comment)
-        const volatile uint32_t* dp = a.done + s;
-        uint32_t it = 0;
-        while (*dp < v.raster_items) {
-          if (++it > (1u << 22)) {
-            s_ok = 0;
-            atomicOr(a.status, T3_STATUS_TIMEOUT);
-            break;
+      const uint32_t gid = (uint32_t)(ob.face_base + n);
+      if (vis) {
+        store_record(v.rec, gid, st);
+        const int64_t area = (int64_t)(st.topx - st.botx + 1) * (int64_t)(st.topy - st.boty + 1);
+        if (area > kBigArea) {
+          const int slot = atomicAdd(&s_nbig, 1);
+          if (slot < kBigSlots) {
+            s_big[slot] = (uint32_t)n;
+            vis = false;
           }
-          __nanosleep(256);
+          // beyond the slots the face stays in the warp walk (correct, slower)
         }
-        __threadfence();
       }
-      __syncthreads();
-      if (!s_ok) break;  // a timed-out wait ends this CTA's work (CTA-uniform)
-      {
-        const int64_t base = (int64_t)(gs - v.shade_item0) * a.pixels_per_item;
-        for (int64_t p0 = base; p0 < base + a.pixels_per_item && p0 < v.npix;
-             p0 += kBatchBlock * kBatchPPT) {
-          shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS, true>(v.sc, v.keys, v.rec, v.out,
-                                                                         v.npix, p0, s_list, &s_count);
-          __syncthreads();
-          if (threadIdx.x == 0) s_count = 0;
-          __syncthreads();
-        }
+      warp_raster(wfs[threadIdx.x >> 5], st, vis, gid, 0, fr.width - 1, 0, fr.height - 1, fr, sink);
+      __syncthreads();  // sv is restaged by the next pass
+    }
+    // big faces of this chunk: the whole CTA strides over each bbox
+    const int nbig = min(s_nbig, kBigSlots);
+    const float maxd = (float)fr.maxdepth;
+    for (int b = 0; b < nbig; b++) {
+      const int64_t n = s_big[b];
+      f3 vv[3];
+      face_verts(ob.mesh, face_ref(ob.mesh, n), vv);
+      Setup st;
+      if (!face_setup(fr, vv, st)) continue;  // CTA-uniform
+      const int32_t h = st.topy - st.boty + 1;
+      const int64_t area = (int64_t)(st.topx - st.botx + 1) * h;
+      const uint32_t gid = (uint32_t)(ob.face_base + n);
+      for (int64_t k = threadIdx.x; k < area; k += kBatchBlock) {
+        const int32_t x = st.botx + (int32_t)(k / h);
+        const int32_t y = st.boty + (int32_t)(k - (k / h) * h);
+        float wx, wy, wz, sum;
+        face_raw_weights(st, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1]), wx, wy, wz, sum);
+        f3 wei;
+        if (!face_inside(wx, wy, wz, sum, wei)) continue;
+        const int32_t d = trunc_i32(xmul(face_depth(st, wei), maxd));
+        if (d < fr.maxdepth) sink(x, y, pack_key(d, gid));
       }
     }
-    __syncthreads();  // s_item / s_count are rewritten by the next iteration
+    __syncthreads();  // s_item / s_big are rewritten by the next iteration
+  }
+}
+
+template <int NL>
+__global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_constant__ BatchArgs a) {
+  __shared__ int s_list[kBatchBlock * kBatchPPT];
+  __shared__ int s_count;
+  __shared__ uint32_t s_item;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = atomicAdd(a.queue + 1, 1u);
+      s_count = 0;
+    }
+    __syncthreads();
+    const uint32_t gs = s_item;
+    if (gs >= a.n_items - a.n_raster) break;
+    const int s = find_scene(a, gs, true);
+    const BatchView& v = a.v[s];
+    const int64_t base = (int64_t)(gs - v.shade_item0) * a.pixels_per_item;
+    for (int64_t p0 = base; p0 < base + a.pixels_per_item && p0 < v.npix; p0 += kBatchBlock * kBatchPPT) {
+      shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS>(v.sc, v.keys, v.rec, v.out, v.npix, p0,
+                                                               s_list, &s_count);
+      __syncthreads();
+      if (threadIdx.x == 0) s_count = 0;
+      __syncthreads();
+    }
   }
 }
 
@@ -211,7 +191,7 @@ static int batch_layout(const t3_scene* scenes, int n, BatchLayout& L) {
   if (!scenes || n <= 0) return T3_EINVAL;
   if (n > T3_BATCH_MAX_SCENES) return T3_ETOOBIG;
   L.counters = 0;
-  L.scenes = 256 + align256b(4 * (size_t)(T3_BATCH_MAX_SCENES + 1));
+  L.scenes = 256;
   size_t at = L.scenes + align256b(sizeof(DevScene)) * (size_t)n;
   // key buffers back to back: one clear covers them all
   L.total_pix = 0;
@@ -260,7 +240,7 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   if (c.faces_per_item <= 0) c.faces_per_item = 1024;
   if (c.pixels_per_item <= 0) c.pixels_per_item = 4096;
   if (c.faces_per_item % kBatchBlock || c.pixels_per_item % (kBatchBlock * kBatchPPT)) return T3_EINVAL;
-  if (c.ctas_per_sm < 0 || c.ctas_per_sm > 2) return T3_EINVAL;
+  if (c.ctas_per_sm < 0 || c.ctas_per_sm > 8) return T3_EINVAL;
 
   static thread_local BatchArgs a;
   static thread_local DevScene ds;
@@ -271,8 +251,6 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   a.faces_per_item = c.faces_per_item;
   a.pixels_per_item = c.pixels_per_item;
   a.queue = reinterpret_cast<uint32_t*>(ws + L.counters);
-  a.done = a.queue + 1;
-  a.status = status;
   int nl = 1;
   uint32_t item = 0;
   cudaError_t e = cudaSuccess;
@@ -283,9 +261,9 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
     if (!outs[s].rgb) return T3_EINVAL;
     nl = max_lobes(ds) > nl ? max_lobes(ds) : nl;
     DevScene* dst = reinterpret_cast<DevScene*>(ws + L.scenes + align256b(sizeof(DevScene)) * (size_t)s);
-    // the first upload also zeroes the queue, the done counters and the status
-    e = launch_upload_scene(ds, dst, s == 0 ? a.queue : nullptr, s == 0 ? 1 + T3_BATCH_MAX_SCENES : 0,
-                            s == 0 ? status : nullptr, st);
+    // the first upload also zeroes the queue counters and the status
+    e = launch_upload_scene(ds, dst, s == 0 ? a.queue : nullptr, s == 0 ? 2 : 0, s == 0 ? status : nullptr,
+                            st);
     BatchView& v = a.v[s];
     v.sc = dst;
     v.keys = reinterpret_cast<unsigned long long*>(ws + L.keys[s]);
@@ -311,17 +289,18 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   a.n_items = a.n_raster + sitem;
   e = launch_clear(reinterpret_cast<unsigned long long*>(ws + L.keys[0]), L.total_pix, st);
   if (e != cudaSuccess) return T3_ECUDA;
-  int dev = 0, nsm = 0, occ = 0;
+  int dev = 0, nsm = 0, occ_r = 0, occ_s = 0;
   e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const void* shade_fn = nl <= 2 ? (const void*)k_batch_shade<2> : (const void*)k_batch_shade<4>;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_r, (const void*)k_batch_raster, kBatchBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, shade_fn, kBatchBlock, 0);
   if (e != cudaSuccess) return T3_ECUDA;
-  const void* fn = nl <= 2 ? (const void*)k_batch<2> : (const void*)k_batch<4>;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kBatchBlock, 0);
-  if (e != cudaSuccess) return T3_ECUDA;
-  const int per_sm = c.ctas_per_sm > 0 && c.ctas_per_sm < occ ? c.ctas_per_sm : (occ > 0 ? occ : 1);
-  const int grid = nsm * per_sm;
-  if (nl <= 2) k_batch<2><<<grid, kBatchBlock, 0, st>>>(a);
-  else k_batch<4><<<grid, kBatchBlock, 0, st>>>(a);
+  auto per_sm = [&](int occ) { return c.ctas_per_sm > 0 && c.ctas_per_sm < occ ? c.ctas_per_sm : (occ > 0 ? occ : 1); };
+  k_batch_raster<<<nsm * per_sm(occ_r), kBatchBlock, 0, st>>>(a);
+  if (nl <= 2) k_batch_shade<2><<<nsm * per_sm(occ_s), kBatchBlock, 0, st>>>(a);
+  else k_batch_shade<4><<<nsm * per_sm(occ_s), kBatchBlock, 0, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? T3_OK : T3_ECUDA;
 }
 

@@ -75,7 +75,7 @@ def test_batch_matches_single_renders(cuda, config):
         assert np.array_equal(g[2], dep)
         assert np.array_equal(g[3].view(np.uint32), dpf.view(np.uint32))
         assert np.abs(g[0] - rgb).max() <= 1e-5
-    assert (ref[-1][1] == 0).sum() > 25000  # the big face covers most of its frame
+    assert (ref[-1][1] == 0).sum() > 20000  # the big face covers most of its frame
 
 
 @pytest.mark.gpu
