@@ -241,6 +241,12 @@ int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
  * clamped neighbours, for a [nx, ny, 3] float grid. */
 int t3_grid_normals(const float* pos, float* nrm, int nx, int ny, void* stream);
 
+/* Height-field animation of a grid's positions [nx, ny, 3] (no reference
+ * counterpart; the reference's demos animate grids from Python):
+ * pos[i, j].z = amp * sin(fx * x + wx * t) * cos(fy * y + wy * t). */
+int t3_grid_wave(float* pos, int nx, int ny, float amp, float fx, float fy, float wx, float wy,
+                 float t, void* stream);
+
 /* ToneMapping.apply (tina/postp/tonemap.py:10-12): in-place ACES on n floats. */
 int t3_tonemap(float* rgb, int64_t n, void* stream);
 

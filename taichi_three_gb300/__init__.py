@@ -26,3 +26,4 @@ from .mlp import IBLNet, train_for_skybox
 from . import colour
 from .batch import BatchRenderer
 from .autotune import Autotuner, tune_scene
+from .animate import FrameGraph

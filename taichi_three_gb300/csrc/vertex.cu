@@ -53,3 +53,26 @@ extern "C" int t3_tonemap(float* rgb, int64_t n, void* stream) {
   t3::k_tonemap<<<(unsigned)((n + block - 1) / block), block, 0, (cudaStream_t)stream>>>(rgb, n);
   return cudaGetLastError() == cudaSuccess ? T3_OK : T3_ECUDA;
 }
+
+namespace t3 {
+// z = amp * sin(fx * x + wx * t) * cos(fy * y + wy * t) at every grid vertex
+// (x, y read from the vertex itself)
+__global__ void k_grid_wave(float* __restrict__ pos, int64_t n, float amp, float fx, float fy, float wx,
+                            float wy, float t) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float x = pos[i * 3], y = pos[i * 3 + 1];
+  pos[i * 3 + 2] = amp * sinf(fx * x + wx * t) * cosf(fy * y + wy * t);
+}
+} // namespace t3
+
+// Height-field animation of a grid: pos[i, j].z = amp sin(fx x + wx t) cos(fy y + wy t).
+extern "C" int t3_grid_wave(float* pos, int nx, int ny, float amp, float fx, float fy, float wx, float wy,
+                            float t, void* stream) {
+  if (!pos || nx < 1 || ny < 1) return T3_EINVAL;
+  const int64_t n = (int64_t)nx * ny;
+  const int block = 256;
+  t3::k_grid_wave<<<(unsigned)((n + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
+      pos, n, amp, fx, fy, wx, wy, t);
+  return cudaGetLastError() == cudaSuccess ? T3_OK : T3_ECUDA;
+}

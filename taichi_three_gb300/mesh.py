@@ -189,6 +189,14 @@ class MeshGrid(MeshBase):
     def get_nfaces(self):
         return (self.res[0] - 1) * (self.res[1] - 1) * 2
 
+    def displace_wave(self, t, amp=0.1, fx=8.0, fy=8.0, wx=1.0, wy=1.3):
+        """pos.z = amp sin(fx x + wx t) cos(fy y + wy t) on the device (the
+        animated grid of the benchmark; x, y are the vertices' own)."""
+        lib = N.load()
+        stream = torch.cuda.current_stream(self.pos.device).cuda_stream
+        N.check(lib.t3_grid_wave(self.pos.data_ptr(), self.res[0], self.res[1], amp, fx, fy, wx, wy,
+                                 float(t), stream), 't3_grid_wave')
+
     def pre_compute(self):
         if not self.auto_normals:
             return
