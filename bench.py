@@ -44,11 +44,13 @@ def parse():
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="soup1080", choices=["soup1080", "sphere512"])
+    p.add_argument("--workload", default="soup1080", choices=["soup1080", "sphere512", "ibl1080"])
     p.add_argument("--raster", default="direct", choices=["direct", "binned"])
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the learned-IBL, multi-view batch and animated-grid sections")
     return p.parse_args()
 
 
@@ -61,12 +63,31 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def tc_peak():
+    """Dense BF16 TFLOP/s (burst: the shading kernel is timed alone)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
+
+
 def build_workload(name, seed, raster):
     import taichi_three_gb300 as tina
     if name == "soup1080":
         scene, mesh = tina.workloads.soup_scene(ntri=1_000_000, res=(1920, 1080), seed=seed,
                                                 raster=raster)
         cfg = {"workload": "triangle soup 1920x1080, 1,000,000 faces, PBR per-face, 8 point lamps",
+               "faces": 1_000_000, "width": 1920, "height": 1080}
+    elif name == "ibl1080":
+        # the soup lit by the learned IBL term; an untrained network costs the
+        # same as a trained one, so this profiles the fused network shading pass
+        net = tina.IBLNet(seed=seed)
+        scene, mesh = tina.workloads.ibl_soup_scene(ntri=1_000_000, res=(1920, 1080), seed=seed,
+                                                    mode="mlp", mlp=net, raster=raster)
+        scene._bench_net = net
+        cfg = {"workload": "triangle soup 1920x1080, 1,000,000 faces, PBR per-face, learned IBL "
+                           "(fused tcgen05 network shading)",
                "faces": 1_000_000, "width": 1920, "height": 1080}
     else:
         scene, mesh = tina.workloads.sphere_scene(512, raster=raster)
@@ -154,6 +175,154 @@ def allmax(x, world):
     t = torch.tensor([x], dtype=torch.float64, device="cuda")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def graph_of(fn):
+    """fn() captured into a CUDA graph (after two eager warm-up calls)."""
+    fn()
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        fn()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            fn()
+    torch.cuda.synchronize()
+    return g
+
+
+def time_graph(g, reps, flush=None):
+    """Median ms of g.replay() between CUDA events (L2 flushed before each)."""
+    times = []
+    for i in range(reps):
+        if flush is not None:
+            flush.fill_(float(i))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return statistics.median(times)
+
+
+def stage_times(scene, reps=10):
+    """Median ms of the three stages of t3_render_staged for the scene's
+    current state (upload+clear | raster | shade)."""
+    from taichi_three_gb300 import _native as N
+    lib = N.load()
+    scene.render()
+    sc, keep = scene.describe()
+    outs = N.t3_outputs(scene.image.data_ptr(), scene.face_id.data_ptr(),
+                        scene.engine.depth.data_ptr(), scene.depth_f.data_ptr())
+    evs = [C.c_void_p() for _ in range(4)]
+    for e in evs:
+        N.check(lib.t3_event_create(C.byref(e)), "t3_event_create")
+    arr = (C.c_void_p * 4)(*[e.value for e in evs])
+    st = {k: [] for k in ("clear", "raster", "shade")}
+    mode = N.T3_RASTER_DIRECT if scene.raster_mode == "direct" else N.T3_RASTER_BINNED
+    for _ in range(reps):
+        N.check(lib.t3_render_staged(C.byref(sc), mode, scene.tile, scene.bin_capacity,
+                                     scene._ws.data_ptr(), scene._ws.numel(),
+                                     scene._status.data_ptr(), C.byref(outs),
+                                     torch.cuda.current_stream().cuda_stream, arr), "staged")
+        ms = C.c_float()
+        for name, (a, b) in zip(st, ((0, 1), (1, 2), (2, 3))):
+            N.check(lib.t3_event_elapsed_ms(evs[a], evs[b], C.byref(ms)), "elapsed")
+            st[name].append(ms.value)
+    for e in evs:
+        lib.t3_event_destroy(e)
+    return {k: statistics.median(v) for k, v in st.items()}
+
+
+# FLOPs of one network evaluation counted on the real inputs and outputs:
+# 2 * (386 * 64 + 64 * 64 + 64 * 64 + 64 * 9) (the 400-wide input and 16-wide
+# output rows are padding for the MMA shapes)
+MLP_FLOP_PER_PIXEL = 2 * (386 * 64 + 64 * 64 + 64 * 64 + 64 * 9)
+
+
+def bench_learned_ibl(flush, tc_peak):
+    """1080p soup lit by the procedural sky: the network frame against the
+    256-sample Monte Carlo frame (fps, dE2000 against the FP64 oracle)."""
+    import taichi_three_gb300 as tina
+    from oracle import oracle
+    sky = tina.Skybox(tina.procedural_sky(512, seed=0))
+    t0 = time.time()
+    net, losses = tina.train_for_skybox(sky, samples=1 << 24, spp=4096, steps=12000, batch=32768)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    res = {}
+    for key, mode, spp in (("mlp", "mlp", 1), ("mc256", "mc", 256)):
+        scene, _ = tina.workloads.ibl_soup_scene(skybox=sky, mode=mode, spp=spp, mlp=net)
+        g = graph_of(scene.render)
+        ms = time_graph(g, 20 if mode == "mlp" else 5, flush)
+        stages = stage_times(scene, 5)
+        res[key] = (ms, scene.img.cpu().numpy().reshape(-1, 3), scene, stages)
+    scene = res["mlp"][2]
+    fid = scene.face_id.cpu().numpy().ravel()
+    cov = np.argwhere(fid >= 0).ravel()
+    pick = np.sort(np.random.default_rng(0).choice(cov, 4000, replace=False))
+    _, truth = oracle.pixels_f64(scene, pick, spp=4096, seed=12345)
+    de = {k: float(tina.colour.delta_e2000(v[1][pick], truth).mean()) for k, v in res.items()}
+    shade_ms = res["mlp"][3]["shade"]
+    flop = MLP_FLOP_PER_PIXEL * len(cov)
+    return {"workload": "1920x1080 soup, 1,000,000 faces, PBR per-face, lit only by a 1024x512 "
+                        "FP16 procedural sky (gradient + 12 Gaussian lobes)",
+            "mlp_ms_per_frame": res["mlp"][0], "mc256_ms_per_frame": res["mc256"][0],
+            "mlp_fps": 1e3 / res["mlp"][0], "mc256_fps": 1e3 / res["mc256"][0],
+            "speedup": res["mc256"][0] / res["mlp"][0],
+            "dE2000_mean_mlp": de["mlp"], "dE2000_mean_mc256": de["mc256"],
+            "dE2000_reference": "FP64 oracle, 4096 samples/pixel, 4000 random covered pixels",
+            "train_s": train_s, "train": "16M samples, 4096-sample MC targets, 12000 Adam steps of 32768",
+            "mlp_shade_kernel_ms": shade_ms,
+            "roofline_mlp": {"bound": "tensor", "achieved": flop / (shade_ms / 1e3) / 1e12,
+                             "peak": tc_peak, "unit": "TFLOP/s",
+                             "frac": flop / (shade_ms / 1e3) / 1e12 / tc_peak,
+                             "flop_per_pixel": MLP_FLOP_PER_PIXEL, "pixels": int(len(cov))},
+            "stages_ms": {k: v[3] for k, v in res.items()}}, sky, net
+
+
+def bench_batch(flush):
+    """64 views (1e3..2e6 faces, 256..1024 px square, Classic + 8 lamps) in one
+    raster launch + one shading launch, against the same frames rendered one
+    scene at a time (both captured as CUDA graphs)."""
+    import taichi_three_gb300 as tina
+    from taichi_three_gb300.autotune import Autotuner
+    scenes = tina.workloads.batch_scenes(64, seed=0)
+    faces = sum(list(s.objects)[0].get_nfaces() for s in scenes)
+    pix = sum(s.res[0] * s.res[1] for s in scenes)
+
+    def seq():
+        for s in scenes:
+            s.render()
+    ms_seq = time_graph(graph_of(seq), 5, flush)
+    b = tina.BatchRenderer(scenes)
+    tuner = Autotuner(timer=lambda fn: time_graph(graph_of(fn), 3))
+    cfg, _ = b.autotune(tuner=tuner, repeats=1)
+    ms = time_graph(graph_of(lambda: b.render(cfg)), 10, flush)
+    return {"workload": "64 views: soups of round(exp(U[ln 1e3, ln 2e6])) faces, square "
+                        "256/512/768/1024 px, cameras on the radius-3 sphere, Classic, 8 lamps",
+            "faces": faces, "pixels": pix, "ms_per_batch": ms, "mtri_s": faces / ms / 1e3,
+            "mpix_s": pix / ms / 1e3, "views_per_s": 64e3 / ms, "per_scene_graph_ms": ms_seq,
+            "speedup_vs_per_scene": ms_seq / ms, "autotuned": cfg}
+
+
+def bench_anim_grid(sky, net, flush):
+    """3840x2160, MeshGrid(2048) displaced per frame, PBR + learned IBL + 2
+    lamps, 120 frames in one CUDA graph."""
+    import taichi_three_gb300 as tina
+    scene, grid = tina.workloads.wave_grid_scene(skybox=sky, mlp=net)
+    fg = tina.FrameGraph(scene, 120, update=lambda k: grid.displace_wave(k / 30.0)).capture()
+    ms = time_graph(fg.graph, 3, flush)
+    T = grid.get_nfaces()
+    return {"workload": "3840x2160, MeshGrid(2048) (8,380,418 faces), z = 0.1 sin(8x+t) cos(8y+1.3t) "
+                        "per frame, PBR + learned IBL + 2 point lamps, 120 frames in one CUDA graph",
+            "ms_per_120_frames": ms, "ms_per_frame": ms / 120, "fps": 120e3 / ms,
+            "mtri_s": T * 120 / ms / 1e3, "coverage": float((scene.face_id >= 0).float().mean()),
+            "status": scene.status()}
 
 
 def cpu_baseline(scene, faces, seconds, label):
@@ -386,8 +555,16 @@ def main():
             "fps": world * 1e3 / ms_per_step, "mpix_s": world * P / (ms_per_step / 1e3) / 1e6,
             "gpu_launches": kernels_per_frame * args.steps, "e2e": e2e, "roofline": roofline,
             "clocks": clocks, "wall_s_timed": wall}
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.workload != "ibl1080":
         line["cpu_baseline"] = cpu_baseline(scene, faces, args.cpu_seconds, cfg["workload"])
+    if rank == 0 and world == 1 and not args.no_extras:
+        del scene, mesh, ws, status
+        torch.cuda.empty_cache()
+        line["learned_ibl"], sky, net = bench_learned_ibl(flush, tc_peak())
+        torch.cuda.empty_cache()
+        line["batch"] = bench_batch(flush)
+        torch.cuda.empty_cache()
+        line["anim_grid"] = bench_anim_grid(sky, net, flush)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -147,5 +147,5 @@ def wave_grid_scene(grid_res=2048, res=(3840, 2160), skybox=None, mlp=None, nlig
     pos, inten = point_lights(nlights, seed)
     for p, i in zip(pos, inten):
         light.add_light(pos=p.tolist(), color=[float(i)] * 3)
-    scene.engine.set_camera(lookat(back=(0.0, -1.6, 2.2)), perspective(60, res[0] / res[1]))
+    scene.engine.set_camera(lookat(back=(0.0, -1.1, 1.45)), perspective(60, res[0] / res[1]))
     return scene, grid

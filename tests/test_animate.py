@@ -38,7 +38,7 @@ def test_frame_graph_equals_eager_frames(cuda, oracle_mod):
     assert fg.sums.cpu().numpy().tolist() == eager
     assert len(set(eager)) == frames  # the surface moves
     assert np.array_equal(scene.img.cpu().numpy(), last_eager)
-    o = oracle_mod.render(scene)  # the positions of the last frame, normals recomputed on the host
+    o = oracle_mod.render(scene)  # positions and normals of the last frame
     assert np.array_equal(scene.face_id.cpu().numpy(), o['face_id'])
     assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
     assert np.abs(scene.img.cpu().numpy() - o['rgb']).max() <= 1e-4
