@@ -8,8 +8,11 @@ IN, HID, OUT = 400, 64, 16
 
 def encode(nv, rough, metal):
     """Features [B, 400]: sin / cos of pi * c * 2^(o + j/4), o = 0..7, j = 0..3,
-    per coordinate of n and v, then roughness, metallic, zeros."""
+    per coordinate of n and of r = 2 (n . v) n - v, then roughness, metallic,
+    zeros."""
     nv = np.asarray(nv, np.float64)
+    n, v = nv[:, :3], nv[:, 3:]
+    nv = np.concatenate([n, 2 * (n * v).sum(1, keepdims=True) * n - v], axis=1)
     B = nv.shape[0]
     X = np.zeros((B, IN))
     for c in range(6):

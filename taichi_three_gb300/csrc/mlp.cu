@@ -16,8 +16,10 @@
 // shading composes them with the pixel's albedo, f0 and lobe weights, so one
 // network serves every albedo.
 //
-// Input encoding (400 floats): for each of the six coordinates of n and v,
-// sin and cos of pi * c * 2^(o + j/4), o = 0..7, j = 0..3 (32 frequencies),
+// Input encoding (400 floats): for each of the six coordinates of n and of the
+// mirrored view direction r = 2 (n . v) n - v (v's information in the frame of
+// the specular lobes), sin and cos of pi * c * 2^(o + j/4), o = 0..7, j = 0..3
+// (32 frequencies),
 // evaluated as one sincos per base phase j followed by double-angle steps;
 // then roughness, metallic, and zeros up to 400.
 #include "t3_shading.cuh"
@@ -89,10 +91,12 @@ __global__ void k_targets(Env env, Env irr, const float* __restrict__ nv, const 
 
 // ---- encoding --------------------------------------------------------------
 __device__ __forceinline__ void encode_features(const float nv[6], float rough, float metal, float* x) {
+  float in[6];
+  mirror_inputs(nv, in);
 #pragma unroll 1
   for (int c = 0; c < 6; c++) {
     float s[32], co[32];
-    encode_coord(nv[c], s, co);
+    encode_coord(in[c], s, co);
 #pragma unroll
     for (int f = 0; f < 32; f++) {
       x[c * 64 + f] = s[f];

@@ -54,14 +54,29 @@ __device__ __forceinline__ void encode_coord(float c, float s[32], float co[32])
   }
 }
 
+// The encoded directions: the normal n and the view direction v entered as its
+// mirror image about n, r = reflect(-v, n) = 2 (n . v) n - v -- the same
+// information, in the coordinates the specular lobes are centred on.
+__device__ __forceinline__ void mirror_inputs(const float nv[6], float in[6]) {
+  const float d = nv[0] * nv[3] + nv[1] * nv[4] + nv[2] * nv[5];
+  in[0] = nv[0];
+  in[1] = nv[1];
+  in[2] = nv[2];
+  in[3] = 2.0f * d * nv[0] - nv[3];
+  in[4] = 2.0f * d * nv[1] - nv[4];
+  in[5] = 2.0f * d * nv[2] - nv[5];
+}
+
 // Row `row` of the A operand (K = 400, BF16, core-matrix layout) from the six
 // direction coordinates (n, v), roughness and metallic.
 __device__ __forceinline__ void encode_row_bf16(const float nv[6], float rough, float metal,
                                                 unsigned char* A, int row) {
+  float in[6];
+  mirror_inputs(nv, in);
 #pragma unroll 1
   for (int c = 0; c < 6; c++) {
     float s[32], co[32];
-    encode_coord(nv[c], s, co);
+    encode_coord(in[c], s, co);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       *reinterpret_cast<uint4*>(A + tc_chunk_off(row, c * 64 + 8 * q, T3_MLP_IN)) = pack8_bf16(s + 8 * q);
