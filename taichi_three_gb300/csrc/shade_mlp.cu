@@ -18,7 +18,7 @@
 // expectation of the Monte Carlo estimator of t3_ibl.cuh (linear in the lobe
 // weights), with the integrals read from the network instead of sampled.
 #include "t3_shading.cuh"
-#include "t3_mlp_tc.cuh"
+#include "t3_mlp_group.cuh"
 
 namespace t3 {
 
@@ -70,32 +70,37 @@ __device__ __forceinline__ void write_sky(const t3_frame& fr, const Env& env, co
 }
 
 template <int NL>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kMlpGroups * 128, 1)
 k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
             const float4* __restrict__ rec, t3_outputs out, int64_t npix, int32_t* __restrict__ status) {
-  extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ __align__(8) uint64_t bar;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t cta_bar;
+  __shared__ __align__(8) uint64_t gbar[kMlpGroups][3];
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_list[256];  // pending covered pixels (< 128 carried + one chunk)
-  __shared__ int s_count;
+  __shared__ int s_list[kMlpGroups][256];  // pending covered pixels (< 128 carried + one chunk)
+  __shared__ int s_count[kMlpGroups];
 
   const t3_frame& fr = sc->frame;
   const t3_lighting& lt = sc->lighting;
   const Env env{lt.env, lt.env_w, lt.env_h, lt.env_half};
   const int H = fr.height;
   const int lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) s_count = 0;
-  MlpTile t;
-  bool ok = mlp_begin(t, sm, &bar, &tmem_slot, lt.mlp);  // ends with a CTA barrier
+  const int g = threadIdx.x >> 7;
+  if (threadIdx.x < kMlpGroups) s_count[threadIdx.x] = 0;
+  bool ok = group_cta_begin(sm, &cta_bar, gbar, &tmem_slot, lt.mlp);  // ends with a CTA barrier
+  const uint32_t tmem_base = tmem_slot;
+  MlpGroup G = group_init(sm, gbar, tmem_base);
+  int* list = s_list[g];
 
+  // each group walks its own stream of 128-pixel chunks
   const int64_t nchunks = (npix + 127) / 128;
-  int64_t chunk = blockIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * kMlpGroups;
+  int64_t chunk = (int64_t)blockIdx.x * kMlpGroups + g;
   int pending = 0;
   while (ok) {
-    // collect covered pixels until a full tile is pending or the frame is done
-    // (the loop condition is CTA-uniform: `pending` is read after a barrier)
+    // collect covered pixels until a full tile is pending or the stream ends
     while (pending < 128 && chunk < nchunks) {
-      const int64_t i = chunk * 128 + threadIdx.x;
+      const int64_t i = chunk * 128 + G.row;
       bool covered = false;
       if (i < npix) {
         if (keys[i] == T3_EMPTY_KEY) write_sky(fr, env, out, i);
@@ -104,44 +109,47 @@ k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restric
       const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
       if (m) {
         int slot = 0;
-        if (lane == 0) slot = atomicAdd(&s_count, __popc(m));
+        if (lane == 0) slot = atomicAdd(&s_count[g], __popc(m));
         slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-        if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = (int)i;
+        if (covered) list[slot + __popc(m & ((1u << lane) - 1u))] = (int)i;
       }
-      __syncthreads();
-      pending = s_count;
-      __syncthreads();  // every thread has read the count before the next appends
-      chunk += gridDim.x;
+      group_sync(G.id);
+      pending = s_count[g];
+      group_sync(G.id);  // every thread has read the count before the next appends
+      chunk += stride;
     }
     if (pending == 0) break;
     const int n = pending < 128 ? pending : 128;
 
-    // thread t shades list entry t: geometry, lobe weights, lamps, features
+    // thread row r shades list entry r: geometry, lobe weights, lamps, inputs
     bool mine = false;
     int64_t pix = 0;
     MlpCoeffs q;
-    if (threadIdx.x < n) {
-      pix = s_list[threadIdx.x];
+    float in[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    q.rough = 1.0f;
+    q.metal = 0.0f;
+    if (G.row < n) {
+      pix = list[G.row];
       const int x = (int)(pix / H), y = (int)(pix - (int64_t)x * H);
-      PixelGeom g;
-      if (pixel_geometry(sc, rec, keys[pix], x, y, out, g)) {
+      PixelGeom pg;
+      if (pixel_geometry(sc, rec, keys[pix], x, y, out, pg)) {
         mine = true;
-        eval_mlp_coeffs<NL>(g.ob->mat, g.fg, q);
+        eval_mlp_coeffs<NL>(pg.ob->mat, pg.fg, q);
         if (lt.nlights > 0) {
           LobeState<NL> L;
           V3 amb, emi;
-          eval_material<NL>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
-          q.base = q.base + lamps_term<NL>(lt, L, g.fg, g.vdir);
+          eval_material<NL>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
+          q.base = q.base + lamps_term<NL>(lt, L, pg.fg, pg.vdir);
         }
-        const float nv[6] = {g.fg.normal.x, g.fg.normal.y, g.fg.normal.z, g.vdir.x, g.vdir.y, g.vdir.z};
-        encode_row_bf16(nv, q.rough, q.metal, sm + kA, threadIdx.x);
+        const float nv[6] = {pg.fg.normal.x, pg.fg.normal.y, pg.fg.normal.z, pg.vdir.x, pg.vdir.y, pg.vdir.z};
+        mirror_inputs(nv, in);
       } else {
         store_rgb(fr, out, pix, env_sample(env, view_ray(fr, xadd((float)x, fr.bias[0]),
                                                          xadd((float)y, fr.bias[1]))));
       }
     }
     float y[16];
-    if (!mlp_tile(t, y)) {  // CTA-uniform outcome
+    if (!group_tile(G, in, q.rough, q.metal, y)) {  // group-uniform outcome
       ok = false;
       break;
     }
@@ -151,18 +159,18 @@ k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restric
       const V3 s2 = v3(fmaxf(0.f, expm1f(y[6])), fmaxf(0.f, expm1f(y[7])), fmaxf(0.f, expm1f(y[8])));
       store_rgb(fr, out, pix, q.base + q.cd * ed + q.c1 * s1 + q.c2 * s2);
     }
-    // drop the n entries just shaded (mlp_tile ended with a barrier, so every
-    // thread has read its entry)
+    // drop the n entries just shaded (every thread read its entry before the
+    // tile's first group barrier)
     const int rest = pending - n;
-    const int carry = threadIdx.x < rest ? s_list[n + threadIdx.x] : 0;
-    __syncthreads();
-    if (threadIdx.x < rest) s_list[threadIdx.x] = carry;
-    if (threadIdx.x == 0) s_count = rest;
-    __syncthreads();
+    const int carry = G.row < rest ? list[n + G.row] : 0;
+    group_sync(G.id);
+    if (G.row < rest) list[G.row] = carry;
+    if (G.row == 0) s_count[g] = rest;
+    group_sync(G.id);
     pending = rest;
   }
-  if (!ok && status && threadIdx.x == 0) atomicOr(status, T3_STATUS_TIMEOUT);
-  mlp_end(t);
+  if (!ok && status && G.row == 0) atomicOr(status, T3_STATUS_TIMEOUT);
+  group_cta_end(tmem_base);
 }
 
 template <int NL>
@@ -170,16 +178,17 @@ static cudaError_t launch_shade_mlp_t(const DevScene* sc_dev, const unsigned lon
                                       const float4* rec, const t3_outputs& out, int64_t npix,
                                       int32_t* status, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_shade_mlp<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kMlpSmem);
+                                       (int)kMlpGroupSmem);
   if (e != cudaSuccess) return e;
   int dev = 0, nsm = 0;
   e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   const int64_t nchunks = (npix + 127) / 128;
-  const int grid = (int)(nchunks < nsm ? nchunks : nsm);
+  const int64_t want = (nchunks + kMlpGroups - 1) / kMlpGroups;
+  const int grid = (int)(want < nsm ? want : nsm);
   if (grid <= 0) return cudaSuccess;
-  k_shade_mlp<NL><<<grid, 128, kMlpSmem, st>>>(sc_dev, keys, rec, out, npix, status);
+  k_shade_mlp<NL><<<grid, kMlpGroups * 128, kMlpGroupSmem, st>>>(sc_dev, keys, rec, out, npix, status);
   return cudaGetLastError();
 }
 

@@ -141,3 +141,35 @@ def test_mlp_rejects_phong_materials(cuda, small_net):
                               lighting=light)[0]
     with pytest.raises(RuntimeError):
         scene.render()
+
+
+def test_fused_network_pixel_equals_standalone_inference(cuda, small_net):
+    """Orthographic view of a flat PBR quad: every covered pixel has n = v =
+    (0, 0, 1) and the same material, so the fused shading pass must give the
+    network's output for that one input (computed here with t3_mlp_encode +
+    t3_mlp_infer) composed with the lobe weights."""
+    sky, net = small_net
+    light = tina.SkyboxLighting(sky, mode='mlp', mlp=net)
+    W, H = 64, 48
+    scene = tina.Scene(W, H, ibl=True, lighting=light, tonemap=False, smoothing=True)
+    q = np.array([[-0.8, -0.8, 0.0], [0.8, -0.8, 0.0], [0.8, 0.8, 0.0], [-0.8, 0.8, 0.0]], np.float32)
+    mesh = tina.SimpleMesh()
+    mesh.set_face_verts(np.stack([q[[0, 1, 2]], q[[0, 2, 3]]]))
+    mesh.set_face_norms(np.tile(np.array([0, 0, 1], np.float32), (2, 3, 1)))
+    albedo, metallic, rough = np.array([0.6, 0.5, 0.4], np.float32), 0.3, 0.4
+    scene.add_object(mesh, tina.PBR(basecolor=tuple(albedo.tolist()), metallic=metallic, roughness=rough))
+    scene.engine.set_camera(tina.lookat(back=(0, 0, 3)), tina.ortho())
+    img = _render(scene)
+    cov = img['face_id'] >= 0
+    assert cov.sum() > 1000
+    f0 = metallic * albedo + (1 - metallic) * 0.16 * 0.25
+    nv = torch.tensor([[0, 0, 1, 0, 0, 1]], dtype=torch.float32, device='cuda')
+    X = net.encode(nv, torch.tensor([rough], device='cuda'),
+                   torch.tensor([float(np.clip(f0.mean(), 0, 1))], device='cuda'))
+    y = net.infer(X).cpu().numpy()[0].astype(np.float64)
+    ed, s1, s2 = np.maximum(0, np.expm1(y[0:3])), np.maximum(0, np.expm1(y[3:6])), np.maximum(0, np.expm1(y[6:9]))
+    expect = albedo * (1 - f0) * ed + f0 * f0 * s1 + f0 * (1 - f0) * s2
+    got = img['rgb'][cov]
+    err = np.abs(got - expect).max() / max(1e-3, np.abs(expect).max())
+    assert err < 2e-3, (err, got[:2], expect)
+    assert got.std(axis=0).max() < 1e-4  # one input (up to the rounding of n and v) -> one colour
