@@ -154,9 +154,10 @@ k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restric
       break;
     }
     if (mine) {
-      const V3 ed = v3(fmaxf(0.f, expm1f(y[0])), fmaxf(0.f, expm1f(y[1])), fmaxf(0.f, expm1f(y[2])));
-      const V3 s1 = v3(fmaxf(0.f, expm1f(y[3])), fmaxf(0.f, expm1f(y[4])), fmaxf(0.f, expm1f(y[5])));
-      const V3 s2 = v3(fmaxf(0.f, expm1f(y[6])), fmaxf(0.f, expm1f(y[7])), fmaxf(0.f, expm1f(y[8])));
+      float e[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) e[k] = fmaxf(0.f, __expf(y[k]) - 1.0f);  // outputs are log1p
+      const V3 ed = v3(e[0], e[1], e[2]), s1 = v3(e[3], e[4], e[5]), s2 = v3(e[6], e[7], e[8]);
       store_rgb(fr, out, pix, q.base + q.cd * ed + q.c1 * s1 + q.c2 * s2);
     }
     // drop the n entries just shaded (every thread read its entry before the

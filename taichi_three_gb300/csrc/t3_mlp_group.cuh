@@ -4,7 +4,8 @@
 // A CTA holds the packed network once (t3_mlp_tc.cuh layout, 70,464 bytes) and
 // kMlpGroups groups of 128 threads (4 warps each).  Group g owns TMEM columns
 // [128 g, 128 g + 128) of the CTA's 512 (layer outputs alternate between
-// columns +0 and +64), two 16 KB A-chunk buffers and a 16 KB hidden operand H.
+// columns +0 and +64) and two 16 KB A-chunk buffers; once the first layer is
+// done, buffer 0 holds the hidden operand H of the later layers.
 // The first layer's A operand (128 rows x 400 features) is never materialised
 // whole: the group encodes one input coordinate (64 features) at a time into a
 // chunk buffer and its elected thread issues that chunk's four K = 16 MMAs,
@@ -22,11 +23,15 @@
 
 namespace t3 {
 
-constexpr int kMlpGroups = 3;
+#ifndef T3_MLP_GROUPS
+#define T3_MLP_GROUPS 4
+#endif
+constexpr int kMlpGroups = T3_MLP_GROUPS;        // 3 or 4 (TMEM: 128 columns each)
 constexpr uint32_t kGroupBase = 71680;           // kBlob rounded up to 1 KB
 constexpr uint32_t kChunkBytes = 128 * 64 * 2;   // 128 rows x 64 BF16
-constexpr uint32_t kGroupBytes = 3 * kChunkBytes;  // A0, A1, H
-constexpr uint32_t kMlpGroupSmem = kGroupBase + kMlpGroups * kGroupBytes;  // 219,136 bytes
+constexpr uint32_t kGroupBytes = 2 * kChunkBytes;  // A0 (later H), A1
+constexpr uint32_t kMlpGroupSmem = kGroupBase + kMlpGroups * kGroupBytes;
+static_assert(kMlpGroups * 128 <= 512, "TMEM holds 512 columns");
 constexpr uint32_t kGroupTmemCols = 512;
 static_assert(kGroupBase >= kBlob, "packed network overlaps the group areas");
 
@@ -54,12 +59,19 @@ struct MlpGroup {
   uint32_t a[2], h;    // shared byte offsets of the chunk buffers and H
 };
 
+// One thread polls the mbarrier; the rest of the group sleeps in the named
+// barrier that publishes the outcome (polling by every thread would spend the
+// issue slots the other groups need).
 __device__ __forceinline__ bool group_wait(MlpGroup& G, int b) {
-  bool ok = mbar_wait_bounded(G.bar[b], G.ph[b], 1u << 24);
-  if (!ok) mbar_wait_bounded(G.bar[b], G.ph[b], 1u << 24);
+  bool ok = true;
+  if (G.row == 0) {
+    ok = mbar_wait_bounded(G.bar[b], G.ph[b], 1u << 24);
+    if (!ok) mbar_wait_bounded(G.bar[b], G.ph[b], 1u << 24);
+  }
   G.ph[b] ^= 1u;
+  ok = group_and(ok, G.id);
   tc_fence_after();
-  return group_and(ok, G.id);
+  return ok;
 }
 
 // Issue (by the group's first thread, after a group barrier): D += A_chunk * W^T
@@ -78,13 +90,19 @@ __device__ __forceinline__ void group_issue(const MlpGroup& G, uint32_t a_off, u
 // bias + ReLU of this thread's row of the 64 columns at `col`, written as BF16 into H
 __device__ __forceinline__ void group_epilogue(const MlpGroup& G, uint32_t col, uint32_t b_off) {
   const uint32_t lane_base = (uint32_t)((threadIdx.x & 96) << 16);  // warp's TMEM lane quarter
-  const float* bias = reinterpret_cast<const float*>(G.sm + b_off);
+  const float4* bias = reinterpret_cast<const float4*>(G.sm + b_off);  // 16-byte aligned
 #pragma unroll
   for (int c = 0; c < 64; c += 16) {
     float v[16];
     tc_ld16(G.tmem + lane_base + col + c, v);
 #pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i] + bias[c + i], 0.0f);
+    for (int i = 0; i < 16; i += 4) {
+      const float4 b = bias[(c + i) >> 2];
+      v[i] = fmaxf(v[i] + b.x, 0.0f);
+      v[i + 1] = fmaxf(v[i + 1] + b.y, 0.0f);
+      v[i + 2] = fmaxf(v[i + 2] + b.z, 0.0f);
+      v[i + 3] = fmaxf(v[i + 3] + b.w, 0.0f);
+    }
     *reinterpret_cast<uint4*>(G.sm + G.h + tc_chunk_off(G.row, c, 64)) = pack8_bf16(v);
     *reinterpret_cast<uint4*>(G.sm + G.h + tc_chunk_off(G.row, c + 8, 64)) = pack8_bf16(v + 8);
   }
@@ -206,7 +224,7 @@ __device__ __forceinline__ MlpGroup group_init(unsigned char* sm, uint64_t (*gba
   const uint32_t base = kGroupBase + (uint32_t)g * kGroupBytes;
   G.a[0] = base;
   G.a[1] = base + kChunkBytes;
-  G.h = base + 2 * kChunkBytes;
+  G.h = base;  // chunk buffer 0 is free once the first layer has completed
   return G;
 }
 
