@@ -95,6 +95,9 @@ typedef struct t3_mesh {
 #define T3_OP_ATTR 1     /* per-face attribute: a = channel, b = width   (FaceAttr)      */
 #define T3_OP_INPUT 2    /* a = 0 pos, 1 color, 2 normal, 3 texcoord     nodes.py:79-96  */
 #define T3_OP_FRESNEL 3  /* a = metallic, b = albedo, c = specular       material.py:69-83 */
+#define T3_OP_TEXTURE 4  /* a = texcoord node, b = texture slot          nodes.py:99-111 */
+#define T3_OP_CHECKER 5  /* a = texcoord, b = size, c = color0,
+                            (int)v[0] = color1 node                      nodes.py:114-126 */
 /* leaf materials */
 #define T3_OP_LAMBERT 16 /*                                              material.py:387-442 */
 #define T3_OP_PHONG 17   /* a = shineness                                material.py:445-472 */
@@ -110,10 +113,20 @@ typedef struct t3_node {
   float v[4];
 } t3_node;
 
+/* An image texture (advans.py texture_as_field): float32 [w, h, channels],
+ * Tina's field indexing [i, j]; sampled at texcoord * (shape - 1) with
+ * bilerp (common.py:141-150), the +1 neighbour clamped to the image. */
+#define T3_MAX_TEXTURES 4
+typedef struct t3_texture {
+  const float* data;
+  int32_t w, h, channels, _pad; /* channels 1 or 3 */
+} t3_texture;
+
 typedef struct t3_material {
   int32_t nnodes; /* used entries of nodes[]                                 */
   int32_t root;   /* index of the root material node                          */
   t3_node nodes[T3_MAX_NODES];
+  t3_texture textures[T3_MAX_TEXTURES]; /* referenced by T3_OP_TEXTURE nodes  */
 } t3_material;
 
 typedef struct t3_object {

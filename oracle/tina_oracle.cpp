@@ -334,6 +334,36 @@ template <class R> struct MaterialEval {
       if (n.a == 1) return {{R(1), R(1), R(1)}, 3}; // color = V(1,1,1) triangle.py:48
       if (n.a == 2) return {fr->normal, 3};
       return {fr->texcoord, 2};
+    case T3_OP_TEXTURE: {
+      // Texture.__call__ nodes.py:105-111: bilerp(tex, texcoord * (shape - 1)),
+      // bilerp of common.py:141-150 (the +1 texel clamped to the image)
+      const t3_texture& t = m->textures[n.b];
+      const Val<R> uv = value(n.a);
+      const R px = uv.v.x * (R)(t.w - 1), py = uv.v.y * (R)(t.h - 1);
+      const R Ix = std::floor(px), Iy = std::floor(py);
+      const R x0 = px - Ix, x1 = py - Iy, y0 = R(1) - x0, y1 = R(1) - x1;
+      auto texel = [&](int64_t i, int64_t j) {
+        i = i < 0 ? 0 : i >= t.w ? t.w - 1 : i;
+        j = j < 0 ? 0 : j >= t.h ? t.h - 1 : j;
+        const float* p = t.data + (i * t.h + j) * t.channels;
+        return t.channels == 1 ? v3<R>{(R)p[0], (R)p[0], (R)p[0]} : v3<R>{(R)p[0], (R)p[1], (R)p[2]};
+      };
+      const int64_t ix = (int64_t)Ix, iy = (int64_t)Iy;
+      v3<R> r = muls(x0 * x1, texel(ix + 1, iy + 1));
+      r = add(r, muls(x0 * y1, texel(ix + 1, iy)));
+      r = add(r, muls(y0 * y1, texel(ix, iy)));
+      r = add(r, muls(y0 * x1, texel(ix, iy + 1)));
+      return {r, t.channels == 1 ? 1 : 3};
+    }
+    case T3_OP_CHECKER: {
+      // ChessboardTexture nodes.py:114-126: lerp((texcoord // size).sum() % 2, c0, c1)
+      const Val<R> uv = value(n.a);
+      const R size = value(n.b).v.x;
+      const R s = std::floor(uv.v.x / size) + std::floor(uv.v.y / size);
+      const R t = s - R(2) * std::floor(s / R(2));
+      const Val<R> c0 = value(n.c), c1 = value((int)n.v[0]);
+      return vadd(vmul(c0, sval<R>(R(1) - t)), vmul(c1, sval<R>(t)));
+    }
     case T3_OP_FRESNEL: {
       // f0 = metallic * albedo + (1 - metallic) * 0.16 * specular**2  material.py:69-71
       Val<R> met = value(n.a), alb = value(n.b), spc = value(n.c);

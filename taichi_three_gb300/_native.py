@@ -35,7 +35,7 @@ T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED = 0, 1, 2
 T3_MESH_TRANSFORM, T3_MESH_NOCULL, T3_MESH_FLIP_ORDER, T3_MESH_FLIP_NORMAL, T3_MESH_FLAT_NORMAL = \
     1, 2, 4, 8, 16
 
-T3_OP_CONST, T3_OP_ATTR, T3_OP_INPUT, T3_OP_FRESNEL = 0, 1, 2, 3
+T3_OP_CONST, T3_OP_ATTR, T3_OP_INPUT, T3_OP_FRESNEL, T3_OP_TEXTURE, T3_OP_CHECKER = 0, 1, 2, 3, 4, 5
 T3_OP_LAMBERT, T3_OP_PHONG, T3_OP_COOK, T3_OP_EMISSION = 16, 17, 18, 19
 T3_OP_MIX, T3_OP_SCALE, T3_OP_ADD = 32, 33, 34
 
@@ -66,8 +66,17 @@ class t3_node(C.Structure):
                 ("v", C.c_float * 4)]
 
 
+T3_MAX_TEXTURES = 4
+
+
+class t3_texture(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("w", C.c_int32), ("h", C.c_int32), ("channels", C.c_int32),
+                ("_pad", C.c_int32)]
+
+
 class t3_material(C.Structure):
-    _fields_ = [("nnodes", C.c_int32), ("root", C.c_int32), ("nodes", t3_node * T3_MAX_NODES)]
+    _fields_ = [("nnodes", C.c_int32), ("root", C.c_int32), ("nodes", t3_node * T3_MAX_NODES),
+                ("textures", t3_texture * T3_MAX_TEXTURES)]
 
 
 class t3_object(C.Structure):

@@ -18,9 +18,9 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 static int is_leaf(int op) {
   return op == T3_OP_LAMBERT || op == T3_OP_PHONG || op == T3_OP_COOK || op == T3_OP_EMISSION;
 }
-static int is_value(int op) {
-  return op == T3_OP_CONST || op == T3_OP_ATTR || op == T3_OP_INPUT || op == T3_OP_FRESNEL;
-}
+static int is_basic(int op) { return op == T3_OP_CONST || op == T3_OP_ATTR || op == T3_OP_INPUT; }
+static int is_leaf_value(int op) { return is_basic(op) || op == T3_OP_TEXTURE || op == T3_OP_CHECKER; }
+static int is_value(int op) { return is_leaf_value(op) || op == T3_OP_FRESNEL; }
 
 // Walks the material tree from `node`, multiplying factors along the path.
 static int flatten_rec(const t3_material& in, int node, int* fac, int nfac, DevMaterial& out,
@@ -80,19 +80,32 @@ static int flatten_rec(const t3_material& in, int node, int* fac, int nfac, DevM
 int flatten_material(const t3_material& in, DevMaterial& out) {
   std::memset(&out, 0, sizeof(out));
   if (in.nnodes <= 0 || in.nnodes > T3_MAX_NODES) return T3_EINVAL;
-  // value nodes may only reference earlier value nodes (evaluated in order)
+  // value nodes may only reference earlier value nodes: FRESNEL over leaf
+  // values (basic, texture, checker), textures and checkers over basic ones
   for (int i = 0; i < in.nnodes; i++) {
     const t3_node& nd = in.nodes[i];
     if (nd.op == T3_OP_FRESNEL) {
       const int refs[3] = {nd.a, nd.b, nd.c};
       for (int r : refs)
-        if (r < 0 || r >= i || !is_value(in.nodes[r].op)) return T3_EINVAL;
+        if (r < 0 || r >= i || !is_leaf_value(in.nodes[r].op)) return T3_EINVAL;
+    }
+    if (nd.op == T3_OP_TEXTURE) {
+      if (nd.a < 0 || nd.a >= i || !is_basic(in.nodes[nd.a].op)) return T3_EINVAL;
+      if (nd.b < 0 || nd.b >= T3_MAX_TEXTURES) return T3_EINVAL;
+      const t3_texture& t = in.textures[nd.b];
+      if (!t.data || t.w < 1 || t.h < 1 || (t.channels != 1 && t.channels != 3)) return T3_EINVAL;
+    }
+    if (nd.op == T3_OP_CHECKER) {
+      const int refs[4] = {nd.a, nd.b, nd.c, (int)nd.v[0]};
+      for (int r : refs)
+        if (r < 0 || r >= i || !is_basic(in.nodes[r].op)) return T3_EINVAL;
     }
     if (nd.op == T3_OP_ATTR && (nd.a < 0 || (nd.b != 1 && nd.b != 3))) return T3_EINVAL;
     if (nd.op == T3_OP_INPUT && (nd.a < 0 || nd.a > 3)) return T3_EINVAL;
   }
   out.nnodes = in.nnodes;
   for (int i = 0; i < in.nnodes; i++) out.nodes[i] = in.nodes[i];
+  for (int t = 0; t < T3_MAX_TEXTURES; t++) out.textures[t] = in.textures[t];
   int fac[T3_MAX_FACTORS];
   return flatten_rec(in, in.root, fac, 0, out, 0);
 }

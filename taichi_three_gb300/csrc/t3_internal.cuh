@@ -60,6 +60,7 @@ struct DevMaterial {
   int32_t _pad[2];
   t3_node nodes[T3_MAX_NODES];
   DevLobe lobes[T3_MAX_LOBES];
+  t3_texture textures[T3_MAX_TEXTURES];
 };
 
 struct DevObject {

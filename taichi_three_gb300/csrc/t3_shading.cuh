@@ -49,7 +49,7 @@ struct Frag {
 };
 
 // CONST / ATTR / INPUT node value (scalars broadcast to all three lanes)
-__device__ __forceinline__ V3 eval_leaf(const t3_node& nd, const Frag& fg) {
+__device__ __forceinline__ V3 eval_basic(const t3_node& nd, const Frag& fg) {
   switch (nd.op) {
   case T3_OP_CONST:
     return nd.b == 3 ? v3(nd.v[0], nd.v[1], nd.v[2]) : v3(nd.v[0], nd.v[0], nd.v[0]);
@@ -67,15 +67,52 @@ __device__ __forceinline__ V3 eval_leaf(const t3_node& nd, const Frag& fg) {
   }
 }
 
+// Texture.__call__ (nodes.py:105-111): bilerp(texture, texcoord * (shape - 1))
+// (common.py:141-150), indices clamped to the image
+__device__ __forceinline__ V3 tex_texel(const t3_texture& t, int i, int j) {
+  i = min(max(i, 0), t.w - 1);
+  j = min(max(j, 0), t.h - 1);
+  const float* p = t.data + ((int64_t)i * t.h + j) * t.channels;
+  if (t.channels == 1) {
+    const float s = __ldg(p);
+    return v3(s, s, s);
+  }
+  return v3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+__device__ __forceinline__ V3 tex_sample(const t3_texture& t, V3 uv) {
+  const float cx = uv.x * (float)(t.w - 1), cy = uv.y * (float)(t.h - 1);
+  const float fx = floorf(cx), fy = floorf(cy);
+  const int ix = (int)fx, iy = (int)fy;
+  const float x0 = cx - fx, x1 = cy - fy, y0 = 1.0f - x0, y1 = 1.0f - x1;
+  return ((x0 * x1) * tex_texel(t, ix + 1, iy + 1) + (x0 * y1) * tex_texel(t, ix + 1, iy)) +
+         ((y0 * y1) * tex_texel(t, ix, iy) + (y0 * x1) * tex_texel(t, ix, iy + 1));
+}
+
+// basic values, Texture, ChessboardTexture (nodes.py:114-126:
+// lerp((texcoord // size).sum() % 2, color0, color1))
+__device__ __forceinline__ V3 eval_leaf(const DevMaterial& m, const t3_node& nd, const Frag& fg) {
+  if (nd.op == T3_OP_TEXTURE) return tex_sample(m.textures[nd.b], eval_basic(m.nodes[nd.a], fg));
+  if (nd.op == T3_OP_CHECKER) {
+    const V3 uv = eval_basic(m.nodes[nd.a], fg);
+    const float size = eval_basic(m.nodes[nd.b], fg).x;
+    const float s = floorf(uv.x / size) + floorf(uv.y / size);
+    const float t = s - 2.0f * floorf(s * 0.5f);
+    const V3 c0 = eval_basic(m.nodes[nd.c], fg), c1 = eval_basic(m.nodes[(int)nd.v[0]], fg);
+    return (1.0f - t) * c0 + t * c1;
+  }
+  return eval_basic(nd, fg);
+}
+
 // value of node i; FRESNEL f0 = metallic * albedo + (1 - metallic) * 0.16 * specular**2
 __device__ __forceinline__ V3 eval_value(const DevMaterial& m, int i, const Frag& fg) {
   const t3_node nd = m.nodes[i];
   if (nd.op == T3_OP_FRESNEL) {
-    const V3 met = eval_leaf(m.nodes[nd.a], fg), alb = eval_leaf(m.nodes[nd.b], fg);
-    const V3 spc = eval_leaf(m.nodes[nd.c], fg);
+    const V3 met = eval_leaf(m, m.nodes[nd.a], fg), alb = eval_leaf(m, m.nodes[nd.b], fg);
+    const V3 spc = eval_leaf(m, m.nodes[nd.c], fg);
     return met * alb + (one_minus(met) * v3(0.16f, 0.16f, 0.16f)) * (spc * spc);
   }
-  return eval_leaf(nd, fg);
+  return eval_leaf(m, nd, fg);
 }
 
 // NL = lobe slots compiled in (the kernels are instantiated for 1, 2 and 4)

@@ -8,7 +8,7 @@ parents) followed by the material nodes (LAMBERT, PHONG, COOK, EMISSION, MIX,
 SCALE, ADD); the library flattens that tree into weighted lobes for the kernel.
 """
 from . import _native as N
-from .nodes import Const, FaceAttr, Input, Node, Param, Texture
+from .nodes import ChessboardTexture, Const, FaceAttr, Input, Node, Param, Texture
 
 
 class IMaterial(Node):
@@ -119,11 +119,13 @@ class MaterialCompileError(ValueError):
     pass
 
 
-def compile_material(material, attr_stride=0):
-    """Returns (t3_material, uses_face_attrs)."""
+def compile_material(material, attr_stride=0, device=None, keep=None):
+    """Returns (t3_material, uses_face_attrs); texture pointers are placed on
+    `device` (default: the CUDA device), kept alive through `keep`."""
     nodes = []
     index = {}
     uses_attr = [False]
+    textures = []
 
     def emit(op, a=0, b=0, c=0, v=(0.0, 0.0, 0.0, 0.0)):
         if len(nodes) >= N.T3_MAX_NODES:
@@ -161,7 +163,18 @@ def compile_material(material, attr_stride=0):
             s = value(node.params['specular'])
             i = emit(N.T3_OP_FRESNEL, m, a, s)
         elif isinstance(node, Texture):
-            raise MaterialCompileError('Texture nodes are not supported')
+            uv = value(node.params['texcoord'])
+            if node not in textures:
+                if len(textures) >= N.T3_MAX_TEXTURES:
+                    raise MaterialCompileError(f'at most {N.T3_MAX_TEXTURES} textures per material')
+                textures.append(node)
+            i = emit(N.T3_OP_TEXTURE, uv, textures.index(node))
+        elif isinstance(node, ChessboardTexture):
+            uv = value(node.params['texcoord'])
+            size = value(node.params['size'])
+            c0 = value(node.params['color0'])
+            c1 = value(node.params['color1'])
+            i = emit(N.T3_OP_CHECKER, uv, size, c0, (float(c1), 0.0, 0.0, 0.0))
         else:
             raise MaterialCompileError(f'{type(node).__name__} cannot be used as a value')
         index[key] = i
@@ -209,4 +222,11 @@ def compile_material(material, attr_stride=0):
         nd.op, nd.a, nd.b, nd.c = op, a, b, c
         for j in range(4):
             nd.v[j] = v[j]
+    if textures:
+        from ._device import ptr
+        keep = keep if keep is not None else []
+        for k, t in enumerate(textures):
+            out.textures[k].data = ptr(t.data, device or 'cuda', keep)
+            out.textures[k].w, out.textures[k].h = t.shape
+            out.textures[k].channels = t.channels
     return out, uses_attr[0]

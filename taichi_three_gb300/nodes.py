@@ -114,12 +114,37 @@ class FaceAttr(Node):
 
 
 class Texture(Node):
-    """Image texture node (tina/matr/nodes.py:99-111): not part of this build."""
+    """Image texture (tina/matr/nodes.py:99-111, advans.py:8-28): an array
+    [w, h] or [w, h, 3] indexed [i, j] like a Taichi field (uint8 is scaled by
+    1/255), or a .npy path; sampled with bilerp at texcoord * (shape - 1).
+    Image-file decoding is not part of this build (pass the decoded array)."""
+    arguments = ['texcoord']
+    defaults = ['texcoord']
 
     def __init__(self, path, **kwargs):
-        raise NotImplementedError('Texture nodes are not implemented by this rasteriser build')
+        import torch
+        from ._device import default_device
+        if isinstance(path, str):
+            if not path.endswith('.npy'):
+                raise NotImplementedError('image decoding is not available here; pass the image as an '
+                                          'array (or a .npy file)')
+            img = np.load(path)
+        else:
+            img = np.asarray(path.cpu() if hasattr(path, 'cpu') else path)
+        if img.dtype == np.uint8:
+            img = img / 255
+        img = np.asarray(img, np.float32)
+        if img.ndim == 3 and img.shape[2] == 1:
+            img = img[..., 0]
+        if img.ndim not in (2, 3) or (img.ndim == 3 and img.shape[2] != 3):
+            raise ValueError('textures are [w, h] or [w, h, 3] arrays')
+        super().__init__(**kwargs)
+        self.shape = img.shape[:2]
+        self.channels = 1 if img.ndim == 2 else 3
+        self.data = torch.as_tensor(np.ascontiguousarray(img), device=default_device())
 
 
 class ChessboardTexture(Node):
-    def __init__(self, **kwargs):
-        raise NotImplementedError('ChessboardTexture is not implemented by this rasteriser build')
+    """lerp((texcoord // size).sum() % 2, color0, color1) (tina/matr/nodes.py:114-126)."""
+    arguments = ['texcoord', 'size', 'color0', 'color1']
+    defaults = ['texcoord', 0.1, 0.4, 0.9]

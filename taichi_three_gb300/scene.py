@@ -130,7 +130,7 @@ class Shader:
         raster.mesh._t3_fill(ob.mesh, dev, keep)
         ob.nfaces = raster.mesh.get_nfaces()
         ob.face_base = 0
-        mat, _ = compile_material(self.material, raster.mesh.attr_stride())
+        mat, _ = compile_material(self.material, raster.mesh.attr_stride(), dev, keep)
         ob.material = mat
         size = C.c_size_t()
         N.check(lib.t3_workspace_size(C.byref(sc), N.T3_RASTER_DIRECT, 16, 0, C.byref(size)),
@@ -246,7 +246,9 @@ class Scene:
             ob.nfaces = n
             ob.face_base = base
             base += n
-            mat, uses_attr = compile_material(info.material, obj.attr_stride() if hasattr(obj, 'attr_stride') else 0)
+            mat, uses_attr = compile_material(info.material,
+                                              obj.attr_stride() if hasattr(obj, 'attr_stride') else 0,
+                                              device, keep)
             if uses_attr and not ob.mesh.face_attr:
                 raise ValueError('material uses FaceAttr but the mesh has no face attributes '
                                  '(mesh.set_face_attrs)')
