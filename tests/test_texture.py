@@ -79,7 +79,7 @@ def test_texture_parity(cuda, oracle_mod, kind):
         mat = tina.PBR(basecolor=tina.Texture(_img(16, 16, 3, 3)), metallic=tina.Texture(_img(4, 4, 1, 4)),
                        roughness=0.4)
     o = _check(_quad_scene(mat), oracle_mod)
-    assert (o['face_id'] >= 0).sum() > 2000
+    assert (o['face_id'] >= 0).sum() > 1000
     rgb = o['rgb'][o['face_id'] >= 0]
     assert rgb.std(axis=0).max() > 0.02  # the texture shows
 
