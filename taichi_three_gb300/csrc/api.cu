@@ -190,6 +190,13 @@ int max_lobes(const DevScene& sc) {
   return m;
 }
 
+int has_textures(const DevScene& sc) {
+  for (int o = 0; o < sc.nobjects; o++)
+    for (int i = 0; i < sc.obj[o].mat.nnodes; i++)
+      if (sc.obj[o].mat.nodes[i].op == T3_OP_TEXTURE || sc.obj[o].mat.nodes[i].op == T3_OP_CHECKER) return 1;
+  return 0;
+}
+
 static int64_t max_object_faces(const t3_scene& sc) {
   int64_t m = 0;
   for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
@@ -355,7 +362,7 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
   cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
   return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
-                              nullptr, *out, max_lobes(ds), ds.lighting.mode, nullptr, st));
+                              nullptr, *out, max_lobes(ds), ds.lighting.mode, has_textures(ds), nullptr, st));
 }
 
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
@@ -402,7 +409,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
       e = launch_shade(dsc, scene->frame, keys, reinterpret_cast<const float4*>(ws + L.rec), *out,
-                       max_lobes(ds), ds.lighting.mode, status, st);
+                       max_lobes(ds), ds.lighting.mode, has_textures(ds), status, st);
   } else {
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -427,7 +434,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
     if (e == cudaSuccess && b.keys)
-      e = launch_shade(dsc, scene->frame, b.keys, b.rec, *out, b.max_lobes, ds.lighting.mode, status, st);
+      e = launch_shade(dsc, scene->frame, b.keys, b.rec, *out, b.max_lobes, ds.lighting.mode, 1, status, st);
   }
   if (e == cudaSuccess) e = mark(3);
   return cuda_rc(e);

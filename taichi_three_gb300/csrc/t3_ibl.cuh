@@ -109,7 +109,7 @@ struct IblLobes {
   int n;
 };
 
-template <int NL>
+template <int NL, bool TEX = true>
 __device__ __forceinline__ void eval_ibl_lobes(const DevMaterial& mat, const Frag& fg,
                                                IblLobes<NL>& L, V3& emission) {
   L.n = mat.nlobes;
@@ -125,7 +125,7 @@ __device__ __forceinline__ void eval_ibl_lobes(const DevMaterial& mat, const Fra
     float prob = 1.0f;
     for (int j = 0; j < lb.nfac; j++) {
       const int fj = lb.fac[j];
-      const V3 f = eval_value(mat, fj & 0xFFFF, fg);
+      const V3 f = eval_value<TEX>(mat, fj & 0xFFFF, fg);
       const bool om = (fj & T3_FAC_ONE_MINUS) != 0;
       w = w * (om ? one_minus(f) : f);
       if (fj & T3_FAC_MIX) {
@@ -140,11 +140,11 @@ __device__ __forceinline__ void eval_ibl_lobes(const DevMaterial& mat, const Fra
     L.kind[k] = lb.kind;
     L.w[k] = prob > 0.0f ? (1.0f / prob) * w : v3(0.f, 0.f, 0.f);
     if (lb.kind == T3_OP_COOK) {
-      const float r = eval_value(mat, lb.p0, fg).x;
+      const float r = eval_value<TEX>(mat, lb.p0, fg).x;
       L.r2[k] = r * r;
-      L.f0[k] = eval_value(mat, lb.p1, fg);
+      L.f0[k] = eval_value<TEX>(mat, lb.p1, fg);
     } else if (lb.kind == T3_OP_PHONG) {
-      L.r2[k] = eval_value(mat, lb.p0, fg).x;
+      L.r2[k] = eval_value<TEX>(mat, lb.p0, fg).x;
     }
     c += prob;
     L.cdf[k] = c;  // upper edge of lobe k's interval

@@ -88,11 +88,12 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
                          const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
-                         int32_t* status, cudaStream_t st);
+                         int textured, int32_t* status, cudaStream_t st);
 cudaError_t launch_shade_mlp(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
                              const float4* rec, const t3_outputs& out, int max_lobes, int32_t* status,
                              cudaStream_t st);
 int max_lobes(const DevScene& sc);
+int has_textures(const DevScene& sc);  // any Texture / ChessboardTexture node
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,
                         cudaStream_t st);

@@ -35,11 +35,12 @@ __device__ __forceinline__ void load_record(const float4* __restrict__ rec, uint
   s.botx = p0 & 0xFFFF; s.boty = p0 >> 16; s.topx = p1 & 0xFFFF; s.topy = p1 >> 16;
 }
 
+// A warp's 32 face setups, one 64-byte record per face (four 16-byte loads per
+// tested pixel; lanes testing pixels of the same face read it as a broadcast),
+// plus the bbox heights and inclusive prefix sums of the bbox areas.
 struct WarpFaces {
-  float bx[32], by[32], cx[32], cy[32], bcnx[32], bcny[32], canx[32], cany[32];
-  float wsa[32], wsb[32], wsc[32], Az[32], Bz[32], Cz[32];
-  int x0[32], y0[32], h[32], incl[32];
-  uint32_t id[32];
+  float4 rec[32][4];  // (bx, by, cx, cy) (bcn, can) (wsa, wsb, wsc, Az) (Bz, Cz, x0 | y0 << 16, id)
+  int h[32], incl[32];
 };
 
 // One pixel's exact inside / depth test (triangle.py:115-125) against setup t.
@@ -74,11 +75,11 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
   const float biasx = fr.bias[0], biasy = fr.bias[1];
   if (!__any_sync(FULL, area > 0)) return;
   if (area > 0) {
-    wf.bx[lane] = s.bx; wf.by[lane] = s.by; wf.cx[lane] = s.cx; wf.cy[lane] = s.cy;
-    wf.bcnx[lane] = s.bcnx; wf.bcny[lane] = s.bcny; wf.canx[lane] = s.canx; wf.cany[lane] = s.cany;
-    wf.wsa[lane] = s.wsa; wf.wsb[lane] = s.wsb; wf.wsc[lane] = s.wsc;
-    wf.Az[lane] = s.Az; wf.Bz[lane] = s.Bz; wf.Cz[lane] = s.Cz;
-    wf.x0[lane] = x0; wf.y0[lane] = y0; wf.h[lane] = y1 - y0 + 1; wf.id[lane] = id;
+    wf.rec[lane][0] = make_float4(s.bx, s.by, s.cx, s.cy);
+    wf.rec[lane][1] = make_float4(s.bcnx, s.bcny, s.canx, s.cany);
+    wf.rec[lane][2] = make_float4(s.wsa, s.wsb, s.wsc, s.Az);
+    wf.rec[lane][3] = make_float4(s.Bz, s.Cz, __int_as_float(x0 | (y0 << 16)), __uint_as_float(id));
+    wf.h[lane] = y1 - y0 + 1;
   }
   int incl = area;
 #pragma unroll
@@ -102,12 +103,15 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
       int q = __float2int_rz(__fdividef((float)off + 0.5f, (float)h));
       int r = off - q * h;
       if (r < 0) { q--; r += h; } else if (r >= h) { q++; r -= h; }
+      const float4 r0 = wf.rec[j][0], r1 = wf.rec[j][1], r2 = wf.rec[j][2], r3 = wf.rec[j][3];
       Setup t;
-      t.bx = wf.bx[j]; t.by = wf.by[j]; t.cx = wf.cx[j]; t.cy = wf.cy[j];
-      t.bcnx = wf.bcnx[j]; t.bcny = wf.bcny[j]; t.canx = wf.canx[j]; t.cany = wf.cany[j];
-      t.wsa = wf.wsa[j]; t.wsb = wf.wsb[j]; t.wsc = wf.wsc[j];
-      t.Az = wf.Az[j]; t.Bz = wf.Bz[j]; t.Cz = wf.Cz[j];
-      test_pixel(t, wf.x0[j] + q, wf.y0[j] + r, wf.id[j], biasx, biasy, maxd, fr.maxdepth, sink);
+      t.bx = r0.x; t.by = r0.y; t.cx = r0.z; t.cy = r0.w;
+      t.bcnx = r1.x; t.bcny = r1.y; t.canx = r1.z; t.cany = r1.w;
+      t.wsa = r2.x; t.wsb = r2.y; t.wsc = r2.z; t.Az = r2.w;
+      t.Bz = r3.x; t.Cz = r3.y;
+      const int xy = __float_as_int(r3.z);
+      test_pixel(t, (xy & 0xFFFF) + q, (xy >> 16) + r, __float_as_uint(r3.w), biasx, biasy, maxd,
+                 fr.maxdepth, sink);
     }
   }
   __syncwarp();

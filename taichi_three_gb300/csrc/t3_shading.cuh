@@ -90,29 +90,36 @@ __device__ __forceinline__ V3 tex_sample(const t3_texture& t, V3 uv) {
 }
 
 // basic values, Texture, ChessboardTexture (nodes.py:114-126:
-// lerp((texcoord // size).sum() % 2, color0, color1))
-__device__ __forceinline__ V3 eval_leaf(const DevMaterial& m, const t3_node& nd, const Frag& fg) {
-  if (nd.op == T3_OP_TEXTURE) return tex_sample(m.textures[nd.b], eval_basic(m.nodes[nd.a], fg));
-  if (nd.op == T3_OP_CHECKER) {
-    const V3 uv = eval_basic(m.nodes[nd.a], fg);
-    const float size = eval_basic(m.nodes[nd.b], fg).x;
-    const float s = floorf(uv.x / size) + floorf(uv.y / size);
-    const float t = s - 2.0f * floorf(s * 0.5f);
-    const V3 c0 = eval_basic(m.nodes[nd.c], fg), c1 = eval_basic(m.nodes[(int)nd.v[0]], fg);
-    return (1.0f - t) * c0 + t * c1;
+// lerp((texcoord // size).sum() % 2, color0, color1)).  TEX = false compiles
+// the texture nodes out (the host picks that instance for untextured scenes:
+// it keeps their registers out of the lamp loop).
+template <bool TEX>
+__device__ __forceinline__ V3 eval_leaf(const DevMaterial& m, int i, const Frag& fg) {
+  const t3_node& nd = m.nodes[i];
+  if constexpr (TEX) {
+    if (nd.op == T3_OP_TEXTURE) return tex_sample(m.textures[nd.b], eval_basic(m.nodes[nd.a], fg));
+    if (nd.op == T3_OP_CHECKER) {
+      const V3 uv = eval_basic(m.nodes[nd.a], fg);
+      const float size = eval_basic(m.nodes[nd.b], fg).x;
+      const float s = floorf(uv.x / size) + floorf(uv.y / size);
+      const float t = s - 2.0f * floorf(s * 0.5f);
+      const V3 c0 = eval_basic(m.nodes[nd.c], fg), c1 = eval_basic(m.nodes[(int)nd.v[0]], fg);
+      return (1.0f - t) * c0 + t * c1;
+    }
   }
   return eval_basic(nd, fg);
 }
 
 // value of node i; FRESNEL f0 = metallic * albedo + (1 - metallic) * 0.16 * specular**2
+template <bool TEX = true>
 __device__ __forceinline__ V3 eval_value(const DevMaterial& m, int i, const Frag& fg) {
   const t3_node nd = m.nodes[i];
   if (nd.op == T3_OP_FRESNEL) {
-    const V3 met = eval_leaf(m, m.nodes[nd.a], fg), alb = eval_leaf(m, m.nodes[nd.b], fg);
-    const V3 spc = eval_leaf(m, m.nodes[nd.c], fg);
+    const V3 met = eval_leaf<TEX>(m, nd.a, fg), alb = eval_leaf<TEX>(m, nd.b, fg);
+    const V3 spc = eval_leaf<TEX>(m, nd.c, fg);
     return met * alb + (one_minus(met) * v3(0.16f, 0.16f, 0.16f)) * (spc * spc);
   }
-  return eval_leaf(m, nd, fg);
+  return eval_leaf<TEX>(m, i, fg);
 }
 
 // NL = lobe slots compiled in (the kernels are instantiated for 1, 2 and 4)
@@ -127,7 +134,7 @@ struct LobeState {
   int n;
 };
 
-template <int NL>
+template <int NL, bool TEX = true>
 __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag& fg, V3 viewdir,
                                               LobeState<NL>& L, V3& ambient, V3& emission) {
   L.n = mat.nlobes;
@@ -141,7 +148,7 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
     const DevLobe& lb = mat.lobes[k];
     V3 w = v3(1.f, 1.f, 1.f);
     for (int j = 0; j < lb.nfac; j++) {
-      const V3 f = eval_value(mat, lb.fac[j] & 0xFFFF, fg);
+      const V3 f = eval_value<TEX>(mat, lb.fac[j] & 0xFFFF, fg);
       w = w * ((lb.fac[j] & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
     }
     L.kind[k] = lb.kind;
@@ -149,16 +156,16 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
     else ambient = ambient + w;
     if (lb.kind == T3_OP_COOK) {
       // per-pixel parts of CookTorrance.sub_brdf (material.py:323-357)
-      const float r = eval_value(mat, lb.p0, fg).x;
+      const float r = eval_value<TEX>(mat, lb.p0, fg).x;
       const float a2 = fmaxf(1e-6f, r * r);
       const float kk = a2 * 0.5f;
       L.a2[k] = a2;
       L.k[k] = kk;
       const float gv = 1.0f / ((NoV * kk + 1.0f) - kk);
       L.gnorm[k] = gv / (1.0f * (1.0f - a2) + 12.566370614359172f * a2);
-      L.f0[k] = eval_value(mat, lb.p1, fg);
+      L.f0[k] = eval_value<TEX>(mat, lb.p1, fg);
     } else if (lb.kind == T3_OP_PHONG) {
-      L.m[k] = eval_value(mat, lb.p0, fg).x;
+      L.m[k] = eval_value<TEX>(mat, lb.p0, fg).x;
       L.ipow[k] = lb.int_pow;
     }
     L.w[k] = w;
@@ -380,7 +387,7 @@ __device__ __forceinline__ void store_rgb(const t3_frame& fr, const t3_outputs& 
 
 // Shades pixel (x, y) from its packed (depth, id) key and writes every output.
 // MODE is the lighting (T3_LIGHT_LAMPS or T3_LIGHT_IBL_MC).
-template <int NL, int MODE, bool COHERENT_REC = false>
+template <int NL, int MODE, bool COHERENT_REC = false, bool TEX = true>
 __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
                                                      const float4* __restrict__ rec,
                                                      unsigned long long key, int x, int y,
@@ -402,20 +409,20 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
   if (MODE == T3_LIGHT_LAMPS) {
     LobeState<NL> L;
     V3 amb, emi;
-    eval_material<NL>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
+    eval_material<NL, TEX>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
     color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
     color = color + lamps_term<NL>(lt, L, g.fg, g.vdir);
   } else {
     // SkyboxLighting.shade_color (lighting.py:20-21): IBL + emission
     IblLobes<NL> L;
     V3 emi;
-    eval_ibl_lobes<NL>(g.ob->mat, g.fg, L, emi);
+    eval_ibl_lobes<NL, TEX>(g.ob->mat, g.fg, L, emi);
     const Env env{lt.env, lt.env_w, lt.env_h, lt.env_half};
     color = emi + ibl_mc<NL>(L, g.fg.normal, g.vdir, env, lt.spp, lt.seed, (uint32_t)g.i);
     if (lt.nlights > 0) {
       LobeState<NL> Ll;
       V3 amb, e2;
-      eval_material<NL>(g.ob->mat, g.fg, g.vdir, Ll, amb, e2);
+      eval_material<NL, TEX>(g.ob->mat, g.fg, g.vdir, Ll, amb, e2);
       color = color + lamps_term<NL>(lt, Ll, g.fg, g.vdir);
     }
   }
@@ -427,7 +434,7 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
 // compacted into a shared list (warp ballot + one shared atomic per warp) so
 // that full warps run the shading.  s_list holds BLOCK * PPT entries; s_count
 // must be zero on entry and is left non-zero (callers reset it after a barrier).
-template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false>
+template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false, bool TEX = true>
 __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
                                             const unsigned long long* __restrict__ keys,
                                             const float4* __restrict__ rec, const t3_outputs& out,
@@ -461,7 +468,7 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
     const int64_t i = base + s_list[j];
     const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
     const unsigned long long key = COHERENT ? __ldcg(keys + i) : keys[i];
-    shade_pixel_from_key<NL, MODE, COHERENT>(sc, rec, key, x, y, out);
+    shade_pixel_from_key<NL, MODE, COHERENT, TEX>(sc, rec, key, x, y, out);
   }
 }
 
