@@ -361,8 +361,8 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
   DevScene* dsc = reinterpret_cast<DevScene*>(ws);
   cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
-  return cuda_rc(launch_shade(dsc, scene->frame, reinterpret_cast<const unsigned long long*>(depth_id),
-                              nullptr, *out, max_lobes(ds), ds.lighting.mode, has_textures(ds), nullptr, st));
+  return cuda_rc(launch_shade(ds, dsc, reinterpret_cast<const unsigned long long*>(depth_id), nullptr, *out,
+                              nullptr, st));
 }
 
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
@@ -408,8 +408,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     }
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
-      e = launch_shade(dsc, scene->frame, keys, reinterpret_cast<const float4*>(ws + L.rec), *out,
-                       max_lobes(ds), ds.lighting.mode, has_textures(ds), status, st);
+      e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st);
   } else {
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -434,7 +433,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
     if (e == cudaSuccess && b.keys)
-      e = launch_shade(dsc, scene->frame, b.keys, b.rec, *out, b.max_lobes, ds.lighting.mode, 1, status, st);
+      e = launch_shade(ds, dsc, b.keys, b.rec, *out, status, st);
   }
   if (e == cudaSuccess) e = mark(3);
   return cuda_rc(e);

@@ -84,8 +84,6 @@ extern "C" int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t
     big.rec = nullptr;
     e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
   }
-  if (e == cudaSuccess) e = launch_shade(dsc, scene->frame, keys, nullptr, *out, max_lobes(ds), ds.lighting.mode,
-                                         has_textures(ds), status,
-                                         st);
+  if (e == cudaSuccess) e = launch_shade(ds, dsc, keys, nullptr, *out, status, st);
   return e == cudaSuccess ? T3_OK : T3_ECUDA;
 }

@@ -36,53 +36,54 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
   return cudaGetLastError();
 }
 
-// Each block owns PPT * BLOCK consecutive pixels (shade_block).
+// Each block owns PPT * BLOCK consecutive pixels (shade_block).  The scene
+// descriptor is a __grid_constant__ kernel parameter: lamps, materials and
+// camera are read through the constant cache (warp-uniform broadcasts), not
+// as per-pixel global loads.
 template <int BLOCK, int PPT, int NL, int MODE, bool TEX>
 __global__ void __launch_bounds__(BLOCK, 3)
-k_shade(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
-        const float4* __restrict__ rec, t3_outputs out, int64_t npix, int H) {
+k_shade(const __grid_constant__ DevScene sc, const unsigned long long* __restrict__ keys,
+        const float4* __restrict__ rec, t3_outputs out, int64_t npix) {
   __shared__ int s_list[BLOCK * PPT];
   __shared__ int s_count;
   if (threadIdx.x == 0) s_count = 0;
   __syncthreads();
-  (void)H;
-  shade_block<BLOCK, PPT, NL, MODE, false, TEX>(sc, keys, rec, out, npix, (int64_t)blockIdx.x * BLOCK * PPT,
+  shade_block<BLOCK, PPT, NL, MODE, false, TEX>(&sc, keys, rec, out, npix, (int64_t)blockIdx.x * BLOCK * PPT,
                                                 s_list, &s_count);
 }
 
 template <int NL, int MODE, bool TEX>
-static void launch_shade_t(const DevScene* sc_dev, const unsigned long long* keys,
-                           const float4* rec, const t3_outputs& out, int64_t npix, int H,
-                           cudaStream_t st) {
+static void launch_shade_t(const DevScene& sc, const unsigned long long* keys, const float4* rec,
+                           const t3_outputs& out, int64_t npix, cudaStream_t st) {
   constexpr int BLOCK = 256, PPT = 4;
   const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
-  k_shade<BLOCK, PPT, NL, MODE, TEX><<<(unsigned)grid, BLOCK, 0, st>>>(sc_dev, keys, rec, out, npix, H);
+  k_shade<BLOCK, PPT, NL, MODE, TEX><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix);
 }
 
 template <int MODE, bool TEX>
-static void launch_shade_m(const DevScene* sc_dev, const unsigned long long* keys,
-                           const float4* rec, const t3_outputs& out, int64_t npix, int H,
-                           int max_lobes, cudaStream_t st) {
-  if (max_lobes <= 1) launch_shade_t<1, MODE, TEX>(sc_dev, keys, rec, out, npix, H, st);
-  else if (max_lobes == 2) launch_shade_t<2, MODE, TEX>(sc_dev, keys, rec, out, npix, H, st);
-  else launch_shade_t<4, MODE, TEX>(sc_dev, keys, rec, out, npix, H, st);
+static void launch_shade_m(const DevScene& sc, const unsigned long long* keys, const float4* rec,
+                           const t3_outputs& out, int64_t npix, int max_lobes, cudaStream_t st) {
+  if (max_lobes <= 1) launch_shade_t<1, MODE, TEX>(sc, keys, rec, out, npix, st);
+  else if (max_lobes == 2) launch_shade_t<2, MODE, TEX>(sc, keys, rec, out, npix, st);
+  else launch_shade_t<4, MODE, TEX>(sc, keys, rec, out, npix, st);
 }
 
-cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                         const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
-                         int textured, int32_t* status, cudaStream_t st) {
+cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
+                         const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st) {
+  const t3_frame& fr = sc_host.frame;
   const int64_t npix = (int64_t)fr.width * fr.height;
-  const int H = fr.height;
+  const int max_lobes = t3::max_lobes(sc_host), light_mode = sc_host.lighting.mode;
+  const bool textured = has_textures(sc_host) != 0;
   if (light_mode == T3_LIGHT_LAMPS && textured)
-    launch_shade_m<T3_LIGHT_LAMPS, true>(sc_dev, keys, rec, out, npix, H, max_lobes, st);
+    launch_shade_m<T3_LIGHT_LAMPS, true>(sc_host, keys, rec, out, npix, max_lobes, st);
   else if (light_mode == T3_LIGHT_LAMPS)
-    launch_shade_m<T3_LIGHT_LAMPS, false>(sc_dev, keys, rec, out, npix, H, max_lobes, st);
+    launch_shade_m<T3_LIGHT_LAMPS, false>(sc_host, keys, rec, out, npix, max_lobes, st);
   else if (light_mode == T3_LIGHT_IBL_MC && textured)
-    launch_shade_m<T3_LIGHT_IBL_MC, true>(sc_dev, keys, rec, out, npix, H, max_lobes, st);
+    launch_shade_m<T3_LIGHT_IBL_MC, true>(sc_host, keys, rec, out, npix, max_lobes, st);
   else if (light_mode == T3_LIGHT_IBL_MC)
-    launch_shade_m<T3_LIGHT_IBL_MC, false>(sc_dev, keys, rec, out, npix, H, max_lobes, st);
+    launch_shade_m<T3_LIGHT_IBL_MC, false>(sc_host, keys, rec, out, npix, max_lobes, st);
   else if (light_mode == T3_LIGHT_IBL_MLP)
-    return launch_shade_mlp(sc_dev, fr, keys, rec, out, max_lobes, status, st);
+    return launch_shade_mlp(sc_host, keys, rec, out, status, st);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

@@ -71,8 +71,9 @@ __device__ __forceinline__ void write_sky(const t3_frame& fr, const Env& env, co
 
 template <int NL>
 __global__ void __launch_bounds__(kMlpGroups * 128, 1)
-k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restrict__ keys,
+k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __restrict__ keys,
             const float4* __restrict__ rec, t3_outputs out, int64_t npix, int32_t* __restrict__ status) {
+  const DevScene* sc = &scene;  // read through the constant cache
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t cta_bar;
   __shared__ __align__(8) uint64_t gbar[kMlpGroups][3];
@@ -175,7 +176,7 @@ k_shade_mlp(const DevScene* __restrict__ sc, const unsigned long long* __restric
 }
 
 template <int NL>
-static cudaError_t launch_shade_mlp_t(const DevScene* sc_dev, const unsigned long long* keys,
+static cudaError_t launch_shade_mlp_t(const DevScene& sc, const unsigned long long* keys,
                                       const float4* rec, const t3_outputs& out, int64_t npix,
                                       int32_t* status, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_shade_mlp<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -189,16 +190,15 @@ static cudaError_t launch_shade_mlp_t(const DevScene* sc_dev, const unsigned lon
   const int64_t want = (nchunks + kMlpGroups - 1) / kMlpGroups;
   const int grid = (int)(want < nsm ? want : nsm);
   if (grid <= 0) return cudaSuccess;
-  k_shade_mlp<NL><<<grid, kMlpGroups * 128, kMlpGroupSmem, st>>>(sc_dev, keys, rec, out, npix, status);
+  k_shade_mlp<NL><<<grid, kMlpGroups * 128, kMlpGroupSmem, st>>>(sc, keys, rec, out, npix, status);
   return cudaGetLastError();
 }
 
-cudaError_t launch_shade_mlp(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                             const float4* rec, const t3_outputs& out, int max_lobes, int32_t* status,
-                             cudaStream_t st) {
-  const int64_t npix = (int64_t)fr.width * fr.height;
-  if (max_lobes <= 2) return launch_shade_mlp_t<2>(sc_dev, keys, rec, out, npix, status, st);
-  return launch_shade_mlp_t<4>(sc_dev, keys, rec, out, npix, status, st);
+cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
+                             const t3_outputs& out, int32_t* status, cudaStream_t st) {
+  const int64_t npix = (int64_t)sc.frame.width * sc.frame.height;
+  if (max_lobes(sc) <= 2) return launch_shade_mlp_t<2>(sc, keys, rec, out, npix, status, st);
+  return launch_shade_mlp_t<4>(sc, keys, rec, out, npix, status, st);
 }
 
 } // namespace t3

@@ -86,12 +86,12 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
                                 int ncounters, int32_t* status, cudaStream_t st);
 cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
-cudaError_t launch_shade(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                         const float4* rec, const t3_outputs& out, int max_lobes, int light_mode,
-                         int textured, int32_t* status, cudaStream_t st);
-cudaError_t launch_shade_mlp(const DevScene* sc_dev, const t3_frame& fr, const unsigned long long* keys,
-                             const float4* rec, const t3_outputs& out, int max_lobes, int32_t* status,
-                             cudaStream_t st);
+// the shading pass; the scene descriptor is passed to the kernels by value
+// (sc_dev, its uploaded copy, is kept for kernels that read it from memory)
+cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
+                         const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st);
+cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
+                             const t3_outputs& out, int32_t* status, cudaStream_t st);
 int max_lobes(const DevScene& sc);
 int has_textures(const DevScene& sc);  // any Texture / ChessboardTexture node
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);

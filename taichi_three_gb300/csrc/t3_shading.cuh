@@ -89,23 +89,27 @@ __device__ __forceinline__ V3 tex_sample(const t3_texture& t, V3 uv) {
          ((y0 * y1) * tex_texel(t, ix, iy) + (y0 * x1) * tex_texel(t, ix, iy + 1));
 }
 
-// basic values, Texture, ChessboardTexture (nodes.py:114-126:
-// lerp((texcoord // size).sum() % 2, color0, color1)).  TEX = false compiles
-// the texture nodes out (the host picks that instance for untextured scenes:
-// it keeps their registers out of the lamp loop).
+// Texture and ChessboardTexture (nodes.py:114-126:
+// lerp((texcoord // size).sum() % 2, color0, color1)), one out-of-line copy.
+static __device__ __noinline__ V3 eval_texture_node(const DevMaterial& m, int i, Frag fg) {
+  const t3_node& nd = m.nodes[i];
+  if (nd.op == T3_OP_TEXTURE) return tex_sample(m.textures[nd.b], eval_basic(m.nodes[nd.a], fg));
+  const V3 uv = eval_basic(m.nodes[nd.a], fg);
+  const float size = eval_basic(m.nodes[nd.b], fg).x;
+  const float s = floorf(uv.x / size) + floorf(uv.y / size);
+  const float t = s - 2.0f * floorf(s * 0.5f);
+  const V3 c0 = eval_basic(m.nodes[nd.c], fg), c1 = eval_basic(m.nodes[(int)nd.v[0]], fg);
+  return (1.0f - t) * c0 + t * c1;
+}
+
+// basic values and (TEX) the texture nodes.  TEX = false compiles the texture
+// nodes out: the host picks that instance for untextured scenes, which keeps
+// the call and its registers out of the lamp loop.
 template <bool TEX>
 __device__ __forceinline__ V3 eval_leaf(const DevMaterial& m, int i, const Frag& fg) {
   const t3_node& nd = m.nodes[i];
   if constexpr (TEX) {
-    if (nd.op == T3_OP_TEXTURE) return tex_sample(m.textures[nd.b], eval_basic(m.nodes[nd.a], fg));
-    if (nd.op == T3_OP_CHECKER) {
-      const V3 uv = eval_basic(m.nodes[nd.a], fg);
-      const float size = eval_basic(m.nodes[nd.b], fg).x;
-      const float s = floorf(uv.x / size) + floorf(uv.y / size);
-      const float t = s - 2.0f * floorf(s * 0.5f);
-      const V3 c0 = eval_basic(m.nodes[nd.c], fg), c1 = eval_basic(m.nodes[(int)nd.v[0]], fg);
-      return (1.0f - t) * c0 + t * c1;
-    }
+    if (nd.op == T3_OP_TEXTURE || nd.op == T3_OP_CHECKER) return eval_texture_node(m, i, fg);
   }
   return eval_basic(nd, fg);
 }
