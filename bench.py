@@ -428,8 +428,8 @@ def main():
     with torch.cuda.graph(graph):
         frame(torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    if args.raster == "direct":  # upload, clear, (raster, big) x objects, shade
-        kernels_per_frame = 2 + 2 * len(scene.objects) + 1
+    if args.raster == "direct":  # clear, (raster, big) x objects, shade
+        kernels_per_frame = 1 + 2 * len(scene.objects) + 1
         stage_names = ("clear", "raster", "shade")
     else:                        # upload, bin x objects, tile (raster + shade)
         kernels_per_frame = 1 + len(scene.objects) + 1

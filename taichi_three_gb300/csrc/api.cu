@@ -356,13 +356,10 @@ int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
   static thread_local DevScene ds;
   int r = make_dev_scene(*scene, ds);
   if (r) return r;
-  cudaStream_t st = (cudaStream_t)stream;
-  uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
-  DevScene* dsc = reinterpret_cast<DevScene*>(ws);
-  cudaError_t e = launch_upload_scene(ds, dsc, nullptr, 0, nullptr, st);
-  if (e != cudaSuccess) return T3_ECUDA;
-  return cuda_rc(launch_shade(ds, dsc, reinterpret_cast<const unsigned long long*>(depth_id), nullptr, *out,
-                              nullptr, st));
+  // the shading kernel takes the scene by value; the workspace is not written
+  return cuda_rc(launch_shade(ds, reinterpret_cast<DevScene*>(workspace),
+                              reinterpret_cast<const unsigned long long*>(depth_id), nullptr, *out, nullptr,
+                              (cudaStream_t)stream));
 }
 
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, void* workspace,
@@ -391,11 +388,12 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     return cudaEventRecord((cudaEvent_t)stage_events[k], st);
   };
   cudaError_t e = mark(0);
-  if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
   if (mode == T3_RASTER_DIRECT) {
+    // the shading kernels take the scene by value: no device copy is needed,
+    // and the clear also zeroes the counters and the status
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
     const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
-    if (e == cudaSuccess) e = launch_clear(keys, npix, st);
+    if (e == cudaSuccess) e = launch_clear(keys, npix, st, counters, L.ncounters, status);
     if (e == cudaSuccess) e = mark(1);
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
       BigQueue big;
@@ -410,6 +408,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess)
       e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st);
   } else {
+    if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
     b.bins = reinterpret_cast<uint32_t*>(ws + L.bins);

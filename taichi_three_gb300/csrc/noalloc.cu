@@ -73,8 +73,7 @@ extern "C" int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t
   DevScene* dsc = reinterpret_cast<DevScene*>(ws + kNoallocScene);
   uint32_t* counters = reinterpret_cast<uint32_t*>(ws + kNoallocCounters);
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + kNoallocKeys);
-  cudaError_t e = launch_upload_scene(ds, dsc, counters, 64, status, st);
-  if (e == cudaSuccess) e = launch_clear(keys, npix, st);
+  cudaError_t e = launch_clear(keys, npix, st, counters, 64, status);
   for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
     BigQueue big;
     big.items = reinterpret_cast<uint32_t*>(ws + kNoallocBig);

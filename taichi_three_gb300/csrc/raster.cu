@@ -19,9 +19,14 @@
 
 namespace t3 {
 
-__global__ void k_clear(unsigned long long* __restrict__ keys, int64_t n) {
+// key buffer <- empty; also zeroes `ncounters` frame counters and the status
+// word (one launch where the frame needs no device copy of the scene)
+__global__ void k_clear(unsigned long long* __restrict__ keys, int64_t n, uint32_t* __restrict__ counters,
+                        int ncounters, int32_t* __restrict__ status) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ncounters) counters[i] = 0u;
+  if (i == 0 && status) *status = 0;
   if ((reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
     ulonglong2* k2 = reinterpret_cast<ulonglong2*>(keys);
     const int64_t n2 = n >> 1;
@@ -107,11 +112,12 @@ k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
   }
 }
 
-cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st) {
+cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, uint32_t* counters,
+                         int ncounters, int32_t* status) {
   const int block = 256;
   int64_t want = ((n >> 1) + block - 1) / block;
   const int grid = (int)(want < 4 * 152 * 8 ? (want > 0 ? want : 1) : 4 * 152 * 8);
-  k_clear<<<grid, block, 0, st>>>(keys, n);
+  k_clear<<<grid, block, 0, st>>>(keys, n, counters, ncounters, status);
   return cudaGetLastError();
 }
 

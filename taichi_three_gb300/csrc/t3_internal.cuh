@@ -81,7 +81,8 @@ struct DevScene {
 int flatten_material(const t3_material& in, DevMaterial& out);
 int make_dev_scene(const t3_scene& sc, DevScene& out);
 
-cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st);
+cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, uint32_t* counters = nullptr,
+                         int ncounters = 0, int32_t* status = nullptr);
 cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
                                 int ncounters, int32_t* status, cudaStream_t st);
 cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
