@@ -16,6 +16,22 @@ from ._device import as_f32, as_i32, default_device, ptr
 MAX = 2**20  # tina/common.py:7
 
 
+def _copy_in_place(dst, src, limit=None):
+    """Updates the device buffer `dst` from a float32 CPU tensor of the same
+    shape (the first `limit` rows): one stream-ordered copy, asynchronous from
+    pinned memory, no allocation (Taichi's field.from_numpy also writes the
+    field in place).  Returns False when the shapes differ."""
+    if dst is None or not isinstance(src, torch.Tensor) or src.device.type != 'cpu':
+        return False
+    if src.dtype != torch.float32 or not src.is_contiguous():
+        return False
+    n = src.shape[0] if limit is None else min(src.shape[0], limit)
+    if tuple(dst.shape) != (n,) + tuple(src.shape[1:]) or not dst.is_cuda:
+        return False
+    dst.copy_(src[:n], non_blocking=src.is_pinned())
+    return True
+
+
 class MeshBase:
     face_attr = None
 
@@ -27,6 +43,8 @@ class MeshBase:
 
     def set_face_attrs(self, attrs):
         """Extension: per-face material attributes [nfaces, C] read by FaceAttr."""
+        if _copy_in_place(self.face_attr, attrs):
+            return
         a = as_f32(attrs)
         if a.dim() == 1:
             a = a[:, None]
@@ -60,6 +78,9 @@ class SimpleMesh(MeshBase):
         return min(self.nfaces, self.maxfaces)
 
     def set_face_verts(self, verts):
+        if _copy_in_place(self.verts, verts, self.maxfaces):
+            self.nfaces = self.verts.shape[0]
+            return
         v = as_f32(verts)
         if v.dim() != 3 or v.shape[1] != 3 or v.shape[2] != 3:
             raise ValueError('verts must have shape [nfaces, 3, 3]')
@@ -67,12 +88,18 @@ class SimpleMesh(MeshBase):
         self.verts = v[:self.nfaces].contiguous()
 
     def set_face_norms(self, norms):
+        if self.norms is not None and self.norms.shape[0] == self.nfaces and \
+                _copy_in_place(self.norms, norms, self.nfaces):
+            return
         n = as_f32(norms)
         if n.dim() != 3 or n.shape[0] < self.nfaces or n.shape[1:] != (3, 3):
             raise ValueError('norms must have shape [>= nfaces, 3, 3]')
         self.norms = n[:self.nfaces].contiguous()
 
     def set_face_coors(self, coors):
+        if self.coors is not None and self.coors.shape[0] == self.nfaces and \
+                _copy_in_place(self.coors, coors, self.nfaces):
+            return
         c = as_f32(coors)
         if c.dim() != 3 or c.shape[0] < self.nfaces or c.shape[1] != 3 or c.shape[2] < 2:
             raise ValueError('coors must have shape [>= nfaces, 3, 2]')
