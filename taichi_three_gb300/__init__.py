@@ -22,6 +22,7 @@ from .scene import Scene, Shader, TriangleRaster
 from .postp import ToneMapping, aces_tonemap
 from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from . import workloads
+from .assimp import readobj
 from .mlp import IBLNet, train_for_skybox
 from . import colour
 from .batch import BatchRenderer
