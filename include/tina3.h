@@ -298,6 +298,20 @@ int t3_event_elapsed_ms(void* start, void* end, float* ms); /* waits for `end` *
  * race and must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
 int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* out, void* stream);
 
+/* ---- post-processing of scene.img (images [W, H, 3] float32, pixel x*H + y) ----
+ * Blooming.apply (tina/postp/blooming.py:52-75): threshold filter, half-res
+ * average, separable Gaussian (radius taps, weights of init_gwei :30-40),
+ * bilinear add-back; workspace: t3_bloom_workspace_floats floats. */
+int64_t t3_bloom_workspace_floats(int width, int height);
+int t3_bloom(float* rgb, int width, int height, float thresh, float factor, float scale, float sigma,
+             int radius, float* workspace, int64_t workspace_floats, void* stream);
+/* FXAA.apply (tina/postp/fxaa.py:25-68); workspace: t3_fxaa_workspace_floats floats. */
+int64_t t3_fxaa_workspace_floats(int width, int height);
+int t3_fxaa(float* rgb, int width, int height, float abs_thresh, float rel_thresh, float factor,
+            float* workspace, int64_t workspace_floats, void* stream);
+/* Accumator.update (tina/util/accumator.py:16-23): acc = acc (1 - 1/count) + src / count. */
+int t3_accumulate(float* acc, const float* src, int64_t n, int count, void* stream);
+
 /* ---- batched multi-view rendering ------------------------------------------
  * No reference counterpart: the reference renders one Scene per call
  * (tina/scene/raster.py:168-207).  Up to T3_BATCH_MAX_SCENES independent

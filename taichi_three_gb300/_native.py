@@ -134,6 +134,12 @@ SIGNATURES = {
     "t3_grid_normals": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
     "t3_tonemap": (C.c_int, [_VP, _I64, _VP]),
     "t3_grid_wave": (C.c_int, [_VP, C.c_int, C.c_int] + [C.c_float] * 6 + [_VP]),
+    "t3_bloom_workspace_floats": (C.c_int64, [C.c_int, C.c_int]),
+    "t3_bloom": (C.c_int, [_VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                           _VP, _I64, _VP]),
+    "t3_fxaa_workspace_floats": (C.c_int64, [C.c_int, C.c_int]),
+    "t3_fxaa": (C.c_int, [_VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _VP, _I64, _VP]),
+    "t3_accumulate": (C.c_int, [_VP, _VP, _I64, C.c_int, _VP]),
     "t3_render_staged": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,
                                    C.POINTER(t3_outputs), _VP, C.POINTER(C.c_void_p)]),
     "t3_render_noalloc": (C.c_int, [C.POINTER(t3_scene), _VP, C.POINTER(t3_outputs), _VP]),

@@ -41,7 +41,10 @@ __global__ void k_tonemap(float* __restrict__ rgb, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float c = rgb[i];
-  rgb[i] = (c * (2.51f * c + 0.03f)) / (c * (2.43f * c + 0.59f) + 0.14f);
+  // source order, no contraction: the same bits as the serial evaluation
+  const float num = xmul(c, xadd(xmul(2.51f, c), 0.03f));
+  const float den = xadd(xmul(c, xadd(xmul(2.43f, c), 0.59f)), 0.14f);
+  rgb[i] = xdiv(num, den);
 }
 } // namespace t3
 

@@ -16,7 +16,7 @@ from .engine import Engine
 from .lighting import Lighting
 from .materials import Diffuse, compile_material
 
-_UNSUPPORTED_OPTIONS = ('taa', 'ssr', 'ssao', 'fxaa', 'blooming')
+_UNSUPPORTED_OPTIONS = ('ssr', 'ssao')
 RASTER_MODES = {'direct': N.T3_RASTER_DIRECT, 'binned': N.T3_RASTER_BINNED}
 
 
@@ -151,12 +151,12 @@ class Scene:
     """Tina's Scene(res, **options) (tina/scene/raster.py:5-258).
 
     Options kept from the reference: smoothing, texturing, culling, clipping,
-    maxfaces, tonemap (default True), bgcolor (default 0).  Extension options:
-    raster ('direct' | 'binned'), tile (8 | 16 | 32), bin_capacity (entries
-    per tile bin, 0 = automatic), check_bins (re-render with doubled bins when
-    a bin overflowed; default True).  taa, ssr,
-    ssao, fxaa and blooming are outside this rasteriser build; ibl selects
-    SkyboxLighting.
+    maxfaces, tonemap (default True), bgcolor (default 0), blooming, fxaa, taa
+    (post-processing in the reference's order), ibl (SkyboxLighting).
+    Extension options: raster ('direct' | 'binned'), tile (8 | 16 | 32),
+    bin_capacity (entries per tile bin, 0 = automatic), check_bins (re-render
+    with doubled bins when a bin overflowed; default True).  ssr and ssao are
+    outside this rasteriser build.
     """
 
     def __init__(self, res_x=512, res_y=None, **options):
@@ -168,6 +168,14 @@ class Scene:
         self.options = options
         self.ibl = options.get('ibl', False)
         self.tonemap = options.get('tonemap', True)
+        # post-processing (raster.py:72-85, :200-207): blooming on the HDR
+        # image, then the tonemap, FXAA, and temporal accumulation
+        from .postp import Accumator, Blooming, FXAA, ToneMapping
+        self.blooming = Blooming(self.res) if options.get('blooming', False) else None
+        self.fxaa = FXAA(self.res) if options.get('fxaa', False) else None
+        self.taa = bool(options.get('taa', False))
+        self.accum = Accumator(self.res) if self.taa else None
+        self._tonemap_pass = ToneMapping(self.res)
         self.bgcolor = options.get('bgcolor', 0)
         self.raster_mode = options.get('raster', 'direct')
         if self.raster_mode not in RASTER_MODES:
@@ -233,7 +241,9 @@ class Scene:
         sc = N.t3_scene()
         keep = []
         raster = self._raster()
-        self.engine._t3_fill_frame(sc.frame, raster.flags(self.tonemap), self.bgcolor)
+        # the tonemap is fused into shading unless blooming needs the HDR image
+        self.engine._t3_fill_frame(sc.frame, raster.flags(self.tonemap and self.blooming is None),
+                                   self.bgcolor)
         self.lighting._t3_fill(sc.lighting)
         if hasattr(self.lighting, '_t3_fill_device'):
             self.lighting._t3_fill_device(sc.lighting, device, keep)
@@ -269,6 +279,8 @@ class Scene:
         require_cuda('Scene.render')
         lib = N.load()
         dev = default_device()
+        if self.taa:
+            self.engine.randomize_bias(self.accum.count == 0)  # raster.py:173-174
         for obj in self.objects:
             obj.pre_compute()
         sc, keep = self.describe(dev)
@@ -303,6 +315,14 @@ class Scene:
                                           C.byref(size)), 't3_workspace_size')
             if self._ws.numel() < size.value:
                 self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+        if self.blooming is not None:
+            self.blooming.apply(self.image)
+            if self.tonemap:
+                self._tonemap_pass.apply(self.image)
+        if self.fxaa is not None:
+            self.fxaa.apply(self.image)
+        if self.taa:
+            self.accum.update(self.image)
         self._keep = keep
         self._last_scene = sc
 
@@ -315,8 +335,14 @@ class Scene:
 
     @property
     def img(self):
-        """The final image (tina/scene/raster.py:209-214): float32 (W, H, 3)."""
-        return self.image
+        """The final image (tina/scene/raster.py:209-214): float32 (W, H, 3);
+        with taa, the running mean of the frames since the last clear()."""
+        return self.accum.img if self.taa else self.image
+
+    def clear(self):
+        """Restarts the temporal accumulation (raster.py:230-232)."""
+        if self.accum is not None:
+            self.accum.clear()
 
     def input(self, gui):
         raise NotImplementedError('GUI camera control is not part of this headless build; '
