@@ -81,6 +81,7 @@ def fxaa(img, abs_thresh=0.0625, rel_thresh=0.063, factor=1.0):
     pl = np.where(is_hori, n, e)
     nl = np.where(is_hori, s, w)
     blend = np.where(np.abs(pl - m) < np.abs(nl - m), -blend, blend)
+    blend = np.where(skip, f32(0), blend)  # skipped pixels keep their colour (their blend is unused)
     px = X.astype(f32) + np.where(is_hori, f32(0), blend)
     py = Y.astype(f32) + np.where(is_hori, blend, f32(0))
     out = _bilerp(img, px, py)

@@ -19,7 +19,7 @@ from .mesh import (MAX, ConnectiveMesh, MeshFlatNormal, MeshFlipCulling, MeshFli
                    MeshModel, MeshNoCulling, MeshTransform, PrimitiveMesh, SimpleMesh)
 from .engine import Engine
 from .scene import Scene, Shader, TriangleRaster
-from .postp import ToneMapping, aces_tonemap
+from .postp import Accumator, Blooming, FXAA, ToneMapping, aces_tonemap
 from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from . import workloads
 from .assimp import readobj
