@@ -169,12 +169,9 @@ def barrier(world):
 
 
 def allmax(x, world):
-    if world == 1:
-        return x
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    """Max over ranks (replicas only: the sole cross-rank exchange)."""
+    from taichi_three_gb300 import replicas
+    return replicas.max_over_ranks(x) if world > 1 else x
 
 
 def graph_of(fn):
