@@ -518,6 +518,34 @@ def main():
                 "frame_alg_bytes": frame_bytes,
                 "frame_frac": frame_bytes / (ms_per_step / 1e3) / 1e9 / peak}
 
+    # atomic work: depth reductions per frame against the measured u64
+    # atomicMin rate on distinct L2-resident addresses
+    atomics = None
+    if args.raster == "direct":
+        nfrag = C.c_int64()
+        N.check(lib.t3_raster_fragments(C.byref(sc), ws.data_ptr(), ws.numel(), C.byref(nfrag),
+                                        torch.cuda.current_stream().cuda_stream), "t3_raster_fragments")
+        probe_n, rounds = 1 << 22, 16  # 32 MB of keys, L2 resident
+        probe = torch.empty(probe_n, dtype=torch.int64, device=dev)
+        rates = []
+        for i in range(6):
+            probe.fill_(-1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            N.check(lib.t3_red_min_rate(probe.data_ptr(), probe_n, rounds,
+                                        torch.cuda.current_stream().cuda_stream), "t3_red_min_rate")
+            e1.record()
+            torch.cuda.synchronize()
+            if i:
+                rates.append(probe_n * rounds / (e0.elapsed_time(e1) / 1e3) / 1e9)
+        peak_red = max(rates)
+        frag_rate = nfrag.value / (stage_ms["raster"] / 1e3) / 1e9
+        atomics = {"fragments_per_frame": nfrag.value, "rate": frag_rate, "peak": peak_red,
+                   "unit": "G reductions/s", "frac": frag_rate / peak_red,
+                   "probe": f"u64 atomicMin, {probe_n} distinct L2-resident addresses x {rounds} rounds, "
+                            "best of 5 (CUDA events)"}
+        del probe
+
     # end to end through the public API: pinned host arrays in, scene.img out
     verts_h = mesh.verts.cpu().pin_memory()
     norms_h = mesh.norms.cpu().pin_memory()
@@ -551,6 +579,7 @@ def main():
                            graph="one CUDA graph per frame"),
             "fps": world * 1e3 / ms_per_step, "mpix_s": world * P / (ms_per_step / 1e3) / 1e6,
             "gpu_launches": kernels_per_frame * args.steps, "e2e": e2e, "roofline": roofline,
+            "atomics": atomics,
             "clocks": clocks, "wall_s_timed": wall}
     if rank == 0 and not args.no_cpu_baseline and args.workload != "ibl1080":
         line["cpu_baseline"] = cpu_baseline(scene, faces, args.cpu_seconds, cfg["workload"])

@@ -243,6 +243,18 @@ int t3_raster(const t3_frame* frame, const t3_object* object,
 int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
              size_t workspace_bytes, const t3_outputs* out, void* stream);
 
+/* Statistics (no reference counterpart): the number of depth reductions
+ * (fragments passing the inside and maxdepth tests) the direct rasteriser
+ * performs for the scene -- the atomic work of a frame.  Runs clear + raster
+ * with a counting instance of the kernels and synchronises the stream.
+ * workspace: t3_workspace_size(scene, T3_RASTER_DIRECT, ...) bytes. */
+int t3_raster_fragments(const t3_scene* scene, void* workspace, size_t workspace_bytes,
+                        int64_t* fragments, void* stream);
+/* u64 atomicMin throughput probe: `rounds` reductions on each of n distinct
+ * addresses of buf (zeroed or filled by the caller; L2-resident when n * 8
+ * is well below the L2 size).  The caller times it. */
+int t3_red_min_rate(uint64_t* buf, int64_t n, int rounds, void* stream);
+
 /* Scene.render (tina/scene/raster.py:168-207) for one frame: clear, raster
  * every object (mode T3_RASTER_*), shade, tonemap. */
 int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,

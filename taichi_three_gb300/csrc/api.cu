@@ -438,6 +438,47 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
   return cuda_rc(e);
 }
 
+int t3_raster_fragments(const t3_scene* scene, void* workspace, size_t workspace_bytes, int64_t* fragments,
+                        void* stream) {
+  if (!scene || !workspace || !fragments) return T3_EINVAL;
+  static thread_local DevScene ds;
+  int r = make_dev_scene(*scene, ds);
+  if (r) return r;
+  Layout L;
+  r = layout_for(*scene, T3_RASTER_DIRECT, 16, 0, L);
+  if (r) return r;
+  if (workspace_bytes < L.end) return T3_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
+  uint32_t* counters = reinterpret_cast<uint32_t*>(ws + L.counters);
+  unsigned long long* count = reinterpret_cast<unsigned long long*>(counters + 62);  // 8-byte aligned
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
+  const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
+  cudaError_t e = launch_clear(keys, npix, st, counters, L.ncounters, nullptr);
+  for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
+    BigQueue big;
+    big.items = reinterpret_cast<uint32_t*>(ws + L.big);
+    big.capacity = L.big_capacity;
+    big.count = counters + o;
+    big.status = reinterpret_cast<int32_t*>(counters + 61);
+    big.rec = nullptr;
+    big.fragments = count;
+    e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
+  }
+  unsigned long long host = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&host, count, sizeof(host), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return T3_ECUDA;
+  *fragments = (int64_t)host;
+  return T3_OK;
+}
+
+int t3_red_min_rate(uint64_t* buf, int64_t n, int rounds, void* stream) {
+  if (!buf || n <= 0 || rounds <= 0) return T3_EINVAL;
+  return cuda_rc(launch_red_min_rate(reinterpret_cast<unsigned long long*>(buf), n, rounds,
+                                     (cudaStream_t)stream));
+}
+
 int t3_bin_counts_max(const t3_scene* scene, int tile, int64_t bin_capacity, const void* workspace,
                       size_t workspace_bytes, int64_t* max_count, void* stream) {
   if (!scene || !workspace || !max_count) return T3_EINVAL;

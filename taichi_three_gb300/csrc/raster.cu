@@ -37,17 +37,20 @@ __global__ void k_clear(unsigned long long* __restrict__ keys, int64_t n, uint32
   }
 }
 
+template <bool COUNT>
 struct GlobalKeySink {
   unsigned long long* keys;
   int64_t H;
+  unsigned long long* fragments;  // COUNT (statistics runs only): every reduction is counted
   __device__ __forceinline__ void operator()(int x, int y, unsigned long long key) const {
+    if constexpr (COUNT) atomicAdd(fragments, 1ull);
     // fire-and-forget reduction (no return value, so no load latency on the
     // fragment path)
     atomicMin(keys + (int64_t)x * H + y, key);
   }
 };
 
-template <int BLOCK>
+template <int BLOCK, bool COUNT>
 __global__ void __launch_bounds__(BLOCK)
 k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t face_base,
                 unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold) {
@@ -73,19 +76,19 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
       vis = false;
     }
   }
-  GlobalKeySink sink{keys, fr.height};
+  GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
   warp_raster(wfs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0, fr.width - 1, 0,
               fr.height - 1, fr, sink);
 }
 
 // Large faces: every CTA walks a slice of every queued face's bbox.
-template <int BLOCK>
+template <int BLOCK, bool COUNT>
 __global__ void __launch_bounds__(BLOCK)
 k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
              unsigned long long* __restrict__ keys, BigQueue big) {
   const uint32_t count = min(*big.count, big.capacity);
   const float maxd = (float)fr.maxdepth;
-  GlobalKeySink sink{keys, fr.height};
+  GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
   const int64_t stride = (int64_t)gridDim.x * BLOCK;
   for (uint32_t e = 0; e < count; e++) {
     const uint32_t n = big.items[e];
@@ -126,13 +129,35 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
   if (ob.nfaces <= 0) return cudaSuccess;
   constexpr int BLOCK = 256;
   const int64_t grid = (ob.nfaces + BLOCK - 1) / BLOCK;
-  // big.count was zeroed by the scene upload at the start of the frame
-  k_raster_direct<BLOCK><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
-                                                          (uint32_t)ob.face_base, keys, big,
-                                                          big_threshold);
+  // big.count was zeroed at the start of the frame
+  if (big.fragments) {
+    k_raster_direct<BLOCK, true><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
+                                                                  (uint32_t)ob.face_base, keys, big,
+                                                                  big_threshold);
+    k_raster_big<BLOCK, true><<<2 * 152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
+    return cudaGetLastError();
+  }
+  k_raster_direct<BLOCK, false><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
+                                                                 (uint32_t)ob.face_base, keys, big,
+                                                                 big_threshold);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_raster_big<BLOCK><<<2 * 152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
+  k_raster_big<BLOCK, false><<<2 * 152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
+  return cudaGetLastError();
+}
+
+// u64 atomicMin throughput: n distinct addresses (L2 resident for n * 8 below
+// the L2 size), `rounds` reductions each, with decreasing values so every
+// reduction changes memory like a winning fragment does
+__global__ void k_red_min_rate(unsigned long long* __restrict__ buf, int64_t n, int rounds) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < rounds; r++)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+      atomicMin(buf + i, (unsigned long long)(rounds - r) << 32 | (unsigned long long)i);
+}
+
+cudaError_t launch_red_min_rate(unsigned long long* buf, int64_t n, int rounds, cudaStream_t st) {
+  k_red_min_rate<<<152 * 8, 256, 0, st>>>(buf, n, rounds);
   return cudaGetLastError();
 }
 

@@ -19,6 +19,7 @@ struct BigQueue {
   uint32_t* count;
   int32_t* status;
   float4* rec;  // setup records per global face id, or nullptr (shading recomputes)
+  unsigned long long* fragments = nullptr;  // statistics runs: count of depth reductions
 };
 
 // Binned rasteriser state (binned.cu).
@@ -81,6 +82,7 @@ struct DevScene {
 int flatten_material(const t3_material& in, DevMaterial& out);
 int make_dev_scene(const t3_scene& sc, DevScene& out);
 
+cudaError_t launch_red_min_rate(unsigned long long* buf, int64_t n, int rounds, cudaStream_t st);
 cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, uint32_t* counters = nullptr,
                          int ncounters = 0, int32_t* status = nullptr);
 cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
