@@ -86,7 +86,7 @@ typedef struct t3_mesh {
   const float* face_attr;   /* per-face material attributes [n, attr_stride]     */
   float trans[16];          /* MeshTransform.trans                                */
   float trans_normal[9];    /* transpose(inv(trans))[:3,:3]                       */
-  int32_t _pad;
+  int32_t nverts;           /* vertex rows of verts (indexed meshes; 0 = unknown)   */
 } t3_mesh;
 
 /* ---- materials: an expression tree (tina/matr/material.py, nodes.py) -------- */

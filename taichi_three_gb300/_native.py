@@ -58,7 +58,7 @@ class t3_mesh(C.Structure):
                 ("slot_vert", C.c_int32), ("slot_coor", C.c_int32), ("slot_norm", C.c_int32),
                 ("grid_nx", C.c_int32), ("grid_ny", C.c_int32), ("attr_stride", C.c_int32),
                 ("face_attr", C.c_void_p), ("trans", C.c_float * 16),
-                ("trans_normal", C.c_float * 9), ("_pad", C.c_int32)]
+                ("trans_normal", C.c_float * 9), ("nverts", C.c_int32)]
 
 
 class t3_node(C.Structure):

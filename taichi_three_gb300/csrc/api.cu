@@ -190,6 +190,12 @@ int max_lobes(const DevScene& sc) {
   return m;
 }
 
+int64_t mesh_vertex_rows(const t3_mesh& m) {
+  if (m.kind == T3_MESH_GRID) return (int64_t)m.grid_nx * m.grid_ny;
+  if (m.kind == T3_MESH_INDEXED) return m.nverts > 0 ? m.nverts : 0;
+  return 0;
+}
+
 int has_textures(const DevScene& sc) {
   for (int o = 0; o < sc.nobjects; o++)
     for (int i = 0; i < sc.obj[o].mat.nnodes; i++)
@@ -219,7 +225,7 @@ static int64_t total_faces(const t3_scene& sc) {
 //   direct:   keys  uint64[W*H] packed (depth, id)
 //   binned:   bins  uint32[ntiles * bin_capacity]
 struct Layout {
-  size_t scene, counters, big, keys, rec, bins, end;
+  size_t scene, counters, big, keys, rec, bins, vtx, end;
   int ncounters;
   uint32_t big_capacity, bin_capacity;
   int tile, tiles_x, tiles_y;
@@ -268,6 +274,12 @@ static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capaci
   } else {
     L.keys = after_rec;
     L.end = align256(L.keys + 8 * (size_t)sc.frame.width * (size_t)sc.frame.height);
+    // vertex stage outputs (float4 per vertex row) of every indexed / grid object
+    L.vtx = L.end;
+    size_t vtx = 0;
+    for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
+      vtx += align256(16 * (size_t)mesh_vertex_rows(sc.objects[o].mesh));
+    L.end += vtx;
   }
   return T3_OK;
 }
@@ -395,6 +407,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
     if (e == cudaSuccess) e = launch_clear(keys, npix, st, counters, L.ncounters, status);
     if (e == cudaSuccess) e = mark(1);
+    size_t vtx = L.vtx;
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
       BigQueue big;
       big.items = reinterpret_cast<uint32_t*>(ws + L.big);
@@ -402,7 +415,14 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
       big.count = counters + o;
       big.status = status;
       big.rec = reinterpret_cast<float4*>(ws + L.rec);
-      e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
+      const int64_t nv = mesh_vertex_rows(scene->objects[o].mesh);
+      if (nv > 0 && scene->objects[o].nfaces > 0) {
+        float4* out = reinterpret_cast<float4*>(ws + vtx);
+        e = launch_vertex_ndc(scene->frame, scene->objects[o].mesh, nv, out, st);
+        big.vndc = out;
+        vtx += align256(16 * (size_t)nv);
+      }
+      if (e == cudaSuccess) e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
     }
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)

@@ -62,9 +62,19 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
   Setup s{};
   bool vis = false;
   if (n < nfaces) {
-    f3 v[3];
-    load_face(mesh, n, staged, sv, v);
-    vis = face_setup(fr, v, s) && s.botx <= s.topx && s.boty <= s.topy;
+    if (big.vndc) {
+      // transformed corners from the vertex stage
+      const FaceRef ref = face_ref(mesh, n);
+      float4 c[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) c[k] = __ldg(big.vndc + corner_vertex(mesh, ref.f, k));
+      vis = face_setup_ndc(fr, ref.flip ? c[2] : c[0], c[1], ref.flip ? c[0] : c[2], s);
+    } else {
+      f3 v[3];
+      load_face(mesh, n, staged, sv, v);
+      vis = face_setup(fr, v, s);
+    }
+    vis = vis && s.botx <= s.topx && s.boty <= s.topy;
   }
   if (vis) {
     if (big.rec) store_record(big.rec, face_base + (uint32_t)n, s);

@@ -207,16 +207,21 @@ __device__ __forceinline__ void tighten_to_centres(float lo, float hi, int32_t& 
   top = t < top ? t : top;
 }
 
-// returns false when the face is culled or clipped
-__device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Setup& s) {
-  const float* W2V = fr.W2V;
-  f3 r; float wa, wb, wc;
-  mapply_x(W2V, v[0], 1.0f, r, wa);
-  const f3 Av = f3{xdiv(r.x, wa), xdiv(r.y, wa), xdiv(r.z, wa)};
-  mapply_x(W2V, v[1], 1.0f, r, wb);
-  const f3 Bv = f3{xdiv(r.x, wb), xdiv(r.y, wb), xdiv(r.z, wb)};
-  mapply_x(W2V, v[2], 1.0f, r, wc);
-  const f3 Cv = f3{xdiv(r.x, wc), xdiv(r.y, wc), xdiv(r.z, wc)};
+// the vertex transform of the setup: NDC position and clip w of one corner
+// (mapply_pos, common.py:170-184)
+__device__ __forceinline__ float4 vertex_ndc(const t3_frame& fr, f3 v) {
+  f3 r;
+  float w;
+  mapply_x(fr.W2V, v, 1.0f, r, w);
+  return make_float4(xdiv(r.x, w), xdiv(r.y, w), xdiv(r.z, w), w);
+}
+
+// setup from the corners' NDC positions and clip w (the rest of
+// render_occup's per-face part); returns false when the face is culled or clipped
+__device__ __forceinline__ bool face_setup_ndc(const t3_frame& fr, float4 A4, float4 B4, float4 C4,
+                                               Setup& s) {
+  const f3 Av = f3{A4.x, A4.y, A4.z}, Bv = f3{B4.x, B4.y, B4.z}, Cv = f3{C4.x, C4.y, C4.z};
+  const float wa = A4.w, wb = B4.w, wc = C4.w;
   const float facing = cross2_x(xsub(Bv.x, Av.x), xsub(Bv.y, Av.y), xsub(Cv.x, Av.x), xsub(Cv.y, Av.y));
   if (facing <= 0.0f && (fr.flags & T3_CULLING)) return false;
   if (fr.flags & T3_CLIPPING) {
@@ -247,6 +252,26 @@ __device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Se
   s.wsc = xrcp(wc);
   s.Az = Av.z; s.Bz = Bv.z; s.Cz = Cv.z;
   return true;
+}
+
+// returns false when the face is culled or clipped
+__device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Setup& s) {
+  return face_setup_ndc(fr, vertex_ndc(fr, v[0]), vertex_ndc(fr, v[1]), vertex_ndc(fr, v[2]), s);
+}
+
+// vertex row of corner k of base face f (GRID and INDEXED meshes; base_ptr's indexing)
+__device__ __forceinline__ int64_t corner_vertex(const t3_mesh& d, int64_t f, int k) {
+  if (d.kind == T3_MESH_GRID) {
+    const uint32_t stride = (uint32_t)d.grid_nx - 1u;
+    const uint32_t m = (uint32_t)(f >> 1);
+    const uint32_t i = m / stride, j = m - i * stride;
+    int c = k;
+    if (f & 1) c = k == 0 ? 0 : k + 1;
+    const uint32_t ii = i + (c == 1 || c == 2 ? 1u : 0u);
+    const uint32_t jj = j + (c >= 2 ? 1u : 0u);
+    return (int64_t)ii * d.grid_ny + jj;
+  }
+  return __ldg(d.faces + f * d.face_stride + k * d.corner_stride + d.slot_vert);
 }
 
 // Unnormalised weights at pixel centre (px, py) and their sum (triangle.py:115-119).

@@ -20,6 +20,7 @@ struct BigQueue {
   int32_t* status;
   float4* rec;  // setup records per global face id, or nullptr (shading recomputes)
   unsigned long long* fragments = nullptr;  // statistics runs: count of depth reductions
+  const float4* vndc = nullptr;  // per-vertex NDC + clip w (indexed meshes and grids), or nullptr
 };
 
 // Binned rasteriser state (binned.cu).
@@ -82,6 +83,9 @@ struct DevScene {
 int flatten_material(const t3_material& in, DevMaterial& out);
 int make_dev_scene(const t3_scene& sc, DevScene& out);
 
+cudaError_t launch_vertex_ndc(const t3_frame& fr, const t3_mesh& mesh, int64_t nverts, float4* out,
+                              cudaStream_t st);
+int64_t mesh_vertex_rows(const t3_mesh& m);  // rows the vertex stage transforms (0: none)
 cudaError_t launch_red_min_rate(unsigned long long* buf, int64_t n, int rounds, cudaStream_t st);
 cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, uint32_t* counters = nullptr,
                          int ncounters = 0, int32_t* status = nullptr);

@@ -79,3 +79,23 @@ extern "C" int t3_grid_wave(float* pos, int nx, int ny, float amp, float fx, flo
       pos, n, amp, fx, fy, wx, wy, t);
   return cudaGetLastError() == cudaSuccess ? T3_OK : T3_ECUDA;
 }
+
+namespace t3 {
+// The vertex stage of indexed meshes and grids: each vertex's NDC position and
+// clip w once (after MeshTransform), instead of once per face corner in the
+// rasteriser's setup (the same operations on the same inputs, so the same bits).
+__global__ void k_vertex_ndc(const t3_frame fr, const t3_mesh mesh, int64_t nverts, float4* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nverts) return;
+  f3 v = ld3(mesh.verts + i * 3);
+  if (mesh.flags & T3_MESH_TRANSFORM) v = mapply_pos_x(mesh.trans, v);
+  out[i] = vertex_ndc(fr, v);
+}
+
+cudaError_t launch_vertex_ndc(const t3_frame& fr, const t3_mesh& mesh, int64_t nverts, float4* out,
+                              cudaStream_t st) {
+  if (nverts <= 0) return cudaSuccess;
+  k_vertex_ndc<<<(unsigned)((nverts + 255) / 256), 256, 0, st>>>(fr, mesh, nverts, out);
+  return cudaGetLastError();
+}
+} // namespace t3

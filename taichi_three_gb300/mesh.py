@@ -292,6 +292,7 @@ class ConnectiveMesh(MeshBase):
         m.kind = N.T3_MESH_INDEXED
         m.nfaces = self.nfaces
         m.verts = ptr(self.verts, device, keep)
+        m.nverts = int(self.verts.shape[0])
         m.norms = ptr(self.norms, device, keep)
         m.coors = ptr(self.coors, device, keep)
         m.faces = ptr(self.faces, device, keep)
@@ -339,6 +340,7 @@ class MeshModel(MeshBase):
         m.kind = N.T3_MESH_INDEXED
         m.nfaces = self.nfaces
         m.verts = ptr(self.verts, device, keep)
+        m.nverts = int(self.verts.shape[0])
         m.norms = ptr(self.norms, device, keep)
         m.coors = ptr(self.coors, device, keep)
         m.faces = ptr(self.faces, device, keep)
