@@ -35,12 +35,13 @@ __device__ __forceinline__ void load_record(const float4* __restrict__ rec, uint
   s.botx = p0 & 0xFFFF; s.boty = p0 >> 16; s.topx = p1 & 0xFFFF; s.topy = p1 >> 16;
 }
 
-// A warp's 32 face setups, one 64-byte record per face (four 16-byte loads per
-// tested pixel; lanes testing pixels of the same face read it as a broadcast),
-// plus the bbox heights and inclusive prefix sums of the bbox areas.
+// A warp's face setups in rank order (faces with a non-empty bbox), one 64-byte
+// record per face (four 16-byte loads per tested pixel; lanes testing pixels
+// of the same face read it as a broadcast), plus the bbox heights and the
+// first index of each face's pixels in the warp's concatenated pixel list.
 struct WarpFaces {
   float4 rec[32][4];  // (bx, by, cx, cy) (bcn, can) (wsa, wsb, wsc, Az) (Bz, Cz, x0 | y0 << 16, id)
-  int h[32], incl[32];
+  int h[32], start[32];
 };
 
 // One pixel's exact inside / depth test (triangle.py:115-125) against setup t.
@@ -61,7 +62,10 @@ __device__ __forceinline__ void test_pixel(const Setup& t, int x, int y, uint32_
 // `s` clipped to [cx0, cx1] x [cy0, cy1]; sink(x, y, key) receives every
 // covered pixel with its packed (depth, id) key.  Every face, however small,
 // goes through the cooperative prefix-sum walk (measured faster than letting
-// faces of a few pixels walk their own bbox per lane).
+// faces of a few pixels walk their own bbox per lane).  Finding a pixel's face:
+// per round of 32 list positions, each face whose first pixel falls in the
+// round sets that position's bit (one warp OR-reduction); a lane's face rank is
+// the faces started before the round plus the set bits up to its position.
 template <class Sink>
 __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool active, uint32_t id,
                                             int cx0, int cx1, int cy0, int cy1,
@@ -73,32 +77,35 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
   const int area = (active && x0 <= x1 && y0 <= y1) ? (x1 - x0 + 1) * (y1 - y0 + 1) : 0;
   const float maxd = (float)fr.maxdepth;
   const float biasx = fr.bias[0], biasy = fr.bias[1];
-  if (!__any_sync(FULL, area > 0)) return;
-  if (area > 0) {
-    wf.rec[lane][0] = make_float4(s.bx, s.by, s.cx, s.cy);
-    wf.rec[lane][1] = make_float4(s.bcnx, s.bcny, s.canx, s.cany);
-    wf.rec[lane][2] = make_float4(s.wsa, s.wsb, s.wsc, s.Az);
-    wf.rec[lane][3] = make_float4(s.Bz, s.Cz, __int_as_float(x0 | (y0 << 16)), __uint_as_float(id));
-    wf.h[lane] = y1 - y0 + 1;
-  }
+  const unsigned live = __ballot_sync(FULL, area > 0);
+  if (!live) return;
   int incl = area;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const int t = __shfl_up_sync(FULL, incl, o);
     if (lane >= o) incl += t;
   }
-  wf.incl[lane] = incl;
+  const int first = incl - area;  // this face's first position in the pixel list
+  if (area > 0) {
+    const int r = __popc(live & ((1u << lane) - 1u));
+    wf.rec[r][0] = make_float4(s.bx, s.by, s.cx, s.cy);
+    wf.rec[r][1] = make_float4(s.bcnx, s.bcny, s.canx, s.cany);
+    wf.rec[r][2] = make_float4(s.wsa, s.wsb, s.wsc, s.Az);
+    wf.rec[r][3] = make_float4(s.Bz, s.Cz, __int_as_float(x0 | (y0 << 16)), __uint_as_float(id));
+    wf.h[r] = y1 - y0 + 1;
+    wf.start[r] = first;
+  }
   const int total = __shfl_sync(FULL, incl, 31);
+  const unsigned upto = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
   __syncwarp();
+  int before = 0;  // faces whose first pixel precedes this round
   for (int base = 0; base < total; base += 32) {
+    const unsigned bit = (area > 0 && first >= base && first < base + 32) ? 1u << (first - base) : 0u;
+    const unsigned starts = __reduce_or_sync(FULL, bit);
     const int idx = base + lane;
     if (idx < total) {
-      // first face j with incl[j] > idx
-      int j = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1)
-        if (wf.incl[j + step - 1] <= idx) j += step;
-      const int off = idx - (j ? wf.incl[j - 1] : 0);
+      const int j = before + __popc(starts & upto) - 1;
+      const int off = idx - wf.start[j];
       const int h = wf.h[j];
       int q = __float2int_rz(__fdividef((float)off + 0.5f, (float)h));
       int r = off - q * h;
@@ -113,6 +120,7 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
       test_pixel(t, (xy & 0xFFFF) + q, (xy >> 16) + r, __float_as_uint(r3.w), biasx, biasy, maxd,
                  fr.maxdepth, sink);
     }
+    before += __popc(starts);
   }
   __syncwarp();
 }
