@@ -16,7 +16,6 @@
 // rasterised by k_raster_big, where every CTA takes a slice of each queued
 // face's bbox.
 #include "t3_raster.cuh"
-#include "t3_tc.cuh"
 
 namespace t3 {
 
@@ -51,96 +50,45 @@ struct GlobalKeySink {
   }
 };
 
-// Persistent: each CTA takes chunks of BLOCK faces (chunk c = blockIdx.x,
-// + gridDim.x, ...).  Face-soup positions are staged into shared memory by a
-// bulk copy (cp.async.bulk, completion on an mbarrier) issued one chunk ahead,
-// so the next chunk's 9 KB are in flight while the current one is set up and
-// rasterised.  Chunks whose byte count is not a multiple of 16 (a partial last
-// chunk) and unaligned soups use plain vector loads.
 template <int BLOCK, bool COUNT>
-__global__ void __launch_bounds__(BLOCK, 6)
+__global__ void __launch_bounds__(BLOCK)
 k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t face_base,
                 unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold) {
-  __shared__ __align__(128) float sv[2][BLOCK * 9];
+  __shared__ __align__(16) float sv[BLOCK * 9];
   __shared__ WarpFaces wfs[BLOCK / 32];
-  __shared__ __align__(8) uint64_t bar[2];
-  const int64_t nchunks = (nfaces + BLOCK - 1) / BLOCK;
-  const bool soup = mesh.kind == T3_MESH_SOUP && !(mesh.flags & T3_MESH_NOCULL) && !big.vndc;
-  const bool bulk = soup && (reinterpret_cast<uintptr_t>(mesh.verts) & 15) == 0;
-  auto chunk_faces = [&](int64_t c) { return (int)min((int64_t)BLOCK, nfaces - c * BLOCK); };
-  auto by_copy = [&](int64_t c) { return bulk && (chunk_faces(c) & 3) == 0; };  // 36 * nf % 16 == 0
-  auto issue = [&](int64_t c, int b) {  // one thread
-    const uint32_t bytes = (uint32_t)chunk_faces(c) * 36u;
-    const uint32_t mb = smem_addr(&bar[b]);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mb), "r"(bytes) : "memory");
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        :: "r"(smem_addr(sv[b])), "l"(mesh.verts + c * BLOCK * 9), "r"(bytes), "r"(mb) : "memory");
-  };
-  if (threadIdx.x == 0) {
-    mbar_init(smem_addr(&bar[0]), 1);
-    mbar_init(smem_addr(&bar[1]), 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  uint32_t phases = 0u;  // bit b: parity of buffer b's next completion
-  int64_t c = blockIdx.x;
-  if (threadIdx.x == 0 && c < nchunks && by_copy(c)) issue(c, 0);
-  GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
-  for (int b = 0; c < nchunks; c += gridDim.x, b ^= 1) {
-    const int64_t next = c + gridDim.x;
-    // sv[b ^ 1] was last read before the previous iteration's closing barrier
-    if (threadIdx.x == 0 && next < nchunks && by_copy(next)) issue(next, b ^ 1);
-    const int64_t f0 = c * BLOCK;
-    if (by_copy(c)) {
-      bool ok = mbar_wait_bounded(smem_addr(&bar[b]), (phases >> b) & 1u, 1u << 22);
-      phases ^= 1u << b;
-      if (!__syncthreads_and(ok)) {
-        // give up on the frame; let this CTA's copy in flight land first
-        if (threadIdx.x == 0) atomicOr(big.status, T3_STATUS_TIMEOUT);
-        if (next < nchunks && by_copy(next))
-          mbar_wait_bounded(smem_addr(&bar[b ^ 1]), (phases >> (b ^ 1)) & 1u, 1u << 22);
-        return;
-      }
-    } else if (soup) {
-      const int nflt = chunk_faces(c) * 9;
-      const float* src = mesh.verts + f0 * 9;
-      for (int i = threadIdx.x; i < nflt; i += BLOCK) sv[b][i] = __ldg(src + i);
-      __syncthreads();
-    }
-    const int64_t n = f0 + threadIdx.x;
-    Setup s{};
-    bool vis = false;
-    if (n < nfaces) {
-      if (big.vndc) {
-        // transformed corners from the vertex stage
-        const FaceRef ref = face_ref(mesh, n);
-        float4 cv[3];
+  const int64_t f0 = (int64_t)blockIdx.x * BLOCK;
+  const bool staged = stage_soup<BLOCK>(mesh, nfaces, f0, sv);
+  const int64_t n = f0 + threadIdx.x;
+  Setup s{};
+  bool vis = false;
+  if (n < nfaces) {
+    if (big.vndc) {
+      // transformed corners from the vertex stage
+      const FaceRef ref = face_ref(mesh, n);
+      float4 c[3];
 #pragma unroll
-        for (int k = 0; k < 3; k++) cv[k] = __ldg(big.vndc + corner_vertex(mesh, ref.f, k));
-        vis = face_setup_ndc(fr, ref.flip ? cv[2] : cv[0], cv[1], ref.flip ? cv[0] : cv[2], s);
-      } else {
-        f3 v[3];
-        load_face(mesh, n, soup, sv[b], v);
-        vis = face_setup(fr, v, s);
-      }
-      vis = vis && s.botx <= s.topx && s.boty <= s.topy;
+      for (int k = 0; k < 3; k++) c[k] = __ldg(big.vndc + corner_vertex(mesh, ref.f, k));
+      vis = face_setup_ndc(fr, ref.flip ? c[2] : c[0], c[1], ref.flip ? c[0] : c[2], s);
+    } else {
+      f3 v[3];
+      load_face(mesh, n, staged, sv, v);
+      vis = face_setup(fr, v, s);
     }
-    if (vis) {
-      if (big.rec) store_record(big.rec, face_base + (uint32_t)n, s);
-      const int64_t area = (int64_t)(s.topx - s.botx + 1) * (int64_t)(s.topy - s.boty + 1);
-      if (area > big_threshold) {
-        const uint32_t slot = atomicAdd(big.count, 1u);
-        if (slot < big.capacity) big.items[slot] = (uint32_t)n;
-        else atomicOr(big.status, T3_STATUS_BIG_OVERFLOW);
-        vis = false;
-      }
-    }
-    warp_raster(wfs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0, fr.width - 1, 0,
-                fr.height - 1, fr, sink);
-    __syncthreads();  // sv[b] and the warps' face records are rewritten next
+    vis = vis && s.botx <= s.topx && s.boty <= s.topy;
   }
+  if (vis) {
+    if (big.rec) store_record(big.rec, face_base + (uint32_t)n, s);
+    const int64_t area = (int64_t)(s.topx - s.botx + 1) * (int64_t)(s.topy - s.boty + 1);
+    if (area > big_threshold) {
+      const uint32_t slot = atomicAdd(big.count, 1u);
+      if (slot < big.capacity) big.items[slot] = (uint32_t)n;
+      else atomicOr(big.status, T3_STATUS_BIG_OVERFLOW);
+      vis = false;
+    }
+  }
+  GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
+  warp_raster(wfs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0, fr.width - 1, 0,
+              fr.height - 1, fr, sink);
 }
 
 // Large faces: every CTA walks a slice of every queued face's bbox.
@@ -190,23 +138,7 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st) {
   if (ob.nfaces <= 0) return cudaSuccess;
   constexpr int BLOCK = 256;
-  // persistent grid: every resident CTA slot once, at most one CTA per chunk
-  static int per_sm[2] = {0, 0}, nsm = 0;
-  const int ci = big.fragments ? 1 : 0;
-  if (!per_sm[ci]) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm[ci], ci ? (const void*)k_raster_direct<BLOCK, true> : (const void*)k_raster_direct<BLOCK, false>,
-          BLOCK, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm[ci] < 1) per_sm[ci] = 1;
-  }
-  const int64_t nchunks = (ob.nfaces + BLOCK - 1) / BLOCK;
-  const int64_t slots = (int64_t)nsm * per_sm[ci];
-  const int64_t grid = nchunks < slots ? nchunks : slots;
+  const int64_t grid = (ob.nfaces + BLOCK - 1) / BLOCK;
   // big.count was zeroed at the start of the frame
   if (big.fragments) {
     k_raster_direct<BLOCK, true><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
