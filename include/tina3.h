@@ -61,6 +61,10 @@ typedef struct t3_frame {
 #define T3_MESH_SOUP 0    /* SimpleMesh: verts [n,3,3], norms [n,3,3], coors [n,3,2]   */
 #define T3_MESH_GRID 1    /* MeshGrid:   pos [nx,ny,3], nrm [nx,ny,3], tex [nx,ny,2]   */
 #define T3_MESH_INDEXED 2 /* MeshModel / ConnectiveMesh: per-vertex arrays + face indices */
+#define T3_MESH_PARTICLES 3 /* SimpleParticles (tina/pars/simple.py) for ParticleRaster
+                               (tina/core/particle.py): nfaces = particles,
+                               verts = positions [n,3], coors = radii [n],
+                               norms = colours [n,3] (nullptr: white); direct raster only */
 
 /* mesh flags (mesh-edit nodes) */
 #define T3_MESH_TRANSFORM 1   /* MeshTransform        tina/mesh/trans.py:23-40 */

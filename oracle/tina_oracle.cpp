@@ -314,6 +314,7 @@ template <class R> inline Val<R> one_minus(Val<R> a) { return {{R(1) - a.v.x, R(
 template <class R> struct Frag {
   v3<R> pos, normal, texcoord;
   const float* attr; // per-face attributes of this fragment's face
+  v3<R> color = {R(1), R(1), R(1)};  // Input('color'): white on triangles, the particle's colour
 };
 
 template <class R> struct MaterialEval {
@@ -331,7 +332,7 @@ template <class R> struct MaterialEval {
     }
     case T3_OP_INPUT:
       if (n.a == 0) return {fr->pos, 3};
-      if (n.a == 1) return {{R(1), R(1), R(1)}, 3}; // color = V(1,1,1) triangle.py:48
+      if (n.a == 1) return {fr->color, 3};  // V(1,1,1) on triangles (triangle.py:48), particle colour
       if (n.a == 2) return {fr->normal, 3};
       return {fr->texcoord, 2};
     case T3_OP_TEXTURE: {
@@ -736,10 +737,92 @@ template <class R> struct Ctx {
 };
 
 // render_color for one pixel of one object (triangle.py:134-153 -> shader.py:119-131)
+// ---------------------------------------------------------------------------
+// Particles (tina/core/particle.py, SimpleParticles tina/pars/simple.py):
+// verts = positions, coors = radii, norms = colours (nullable).
+// ---------------------------------------------------------------------------
+template <class R> inline v3<R> mapply_dir(const mat4<R>& M, v3<R> d) {
+  v3<R> r;
+  R w;
+  mapply(M, d, R(0), r, w);
+  return r;
+}
+
+template <class R> struct ParS {
+  v3<R> A;
+  R Rl, r2, vz;
+  int32_t depth;
+  int32_t botx, boty, topx, topy;
+};
+
+// render_occup's per-particle part (particle.py:77-101); false when clipped or empty
+template <class R> bool particle_setup(const Ctx<R>& cx, const t3_mesh& m, int64_t n, ParS<R>& p) {
+  const t3_frame& fr = cx.sc->frame;
+  p.A = ld3<R>(m.verts + n * 3);
+  p.Rl = (R)m.coors[n];
+  const v3<R> Av = mapply_pos(cx.W2V, p.A);
+  if ((fr.flags & T3_CLIPPING) && !(R(-1) <= Av.z && Av.z <= R(1))) return false;
+  const v3<R> DX = normalized(mapply_dir(cx.V2W, v3<R>{R(1), R(0), R(0)}));
+  const v3<R> DY = normalized(mapply_dir(cx.V2W, v3<R>{R(0), R(1), R(0)}));
+  const R rx = mapply_pos(cx.W2V, add(p.A, mulv(DX, p.Rl))).x - Av.x;
+  const R ry = mapply_pos(cx.W2V, add(p.A, mulv(DY, p.Rl))).y - Av.y;
+  const v2<R> b0 = to_viewport(v3<R>{Av.x - rx, Av.y - R(0), Av.z}, fr.width, fr.height);
+  const v2<R> b1 = to_viewport(v3<R>{Av.x + rx, Av.y + R(0), Av.z}, fr.width, fr.height);
+  const v2<R> b2 = to_viewport(v3<R>{Av.x - R(0), Av.y - ry, Av.z}, fr.width, fr.height);
+  const v2<R> b3 = to_viewport(v3<R>{Av.x + R(0), Av.y + ry, Av.z}, fr.width, fr.height);
+  const int32_t lox = trunc_i32(std::floor(fmin_(b0.x, b2.x))), loy = trunc_i32(std::floor(fmin_(b0.y, b2.y)));
+  const int32_t hix = trunc_i32(std::ceil(fmax_(b1.x, b3.x))), hiy = trunc_i32(std::ceil(fmax_(b1.y, b3.y)));
+  p.botx = lox > 0 ? lox : 0;
+  p.boty = loy > 0 ? loy : 0;
+  p.topx = hix < fr.width - 1 ? hix : fr.width - 1;
+  p.topy = hiy < fr.height - 1 ? hiy : fr.height - 1;
+  p.r2 = p.Rl * p.Rl;
+  p.vz = Av.z;
+  p.depth = trunc_i32(Av.z * (R)fr.maxdepth);
+  return p.botx <= p.topx && p.boty <= p.topy;
+}
+
+// Pl = mapply_pos(V2W, (from_viewport(P + bias), Av.z)) (particle.py:103-105)
+template <class R> v3<R> particle_pixel_world(const Ctx<R>& cx, const ParS<R>& p, int32_t x, int32_t y) {
+  const t3_frame& fr = cx.sc->frame;
+  const R px = (R)x + (R)fr.bias[0], py = (R)y + (R)fr.bias[1];
+  const v3<R> Pv = {(px / (R)fr.width) * R(2) - R(1), (py / (R)fr.height) * R(2) - R(1), p.vz};
+  return mapply_pos(cx.V2W, Pv);
+}
+
+template <class R> bool particle_covers(const ParS<R>& p, v3<R> Pl) {
+  const v3<R> d = sub(Pl, p.A);
+  return !(((d.x * d.x + d.y * d.y) + d.z * d.z) > p.r2);
+}
+
+// render_color's particle geometry (particle.py:118-146): normal and position
+template <class R> void particle_frag(const Ctx<R>& cx, const t3_mesh& m, int64_t n, int32_t x, int32_t y,
+                                      v3<R>& pos, v3<R>& normal, v3<R>& color, R& depth_f) {
+  ParS<R> p;
+  p.A = ld3<R>(m.verts + n * 3);
+  p.Rl = (R)m.coors[n];
+  p.vz = mapply_pos(cx.W2V, p.A).z;
+  depth_f = p.vz;
+  const v3<R> Pl = particle_pixel_world(cx, p, x, y);
+  v3<R> D = divs(sub(Pl, p.A), p.Rl);
+  const v3<R> Z = normalized(mapply_dir(cx.V2W, v3<R>{R(0), R(0), R(1)}));
+  D = sub(D, mulv(Z, std::sqrt(R(1) - dot(D, D))));
+  D = normalized(D);
+  normal = D;
+  pos = add(p.A, mulv(D, p.Rl));
+  color = m.norms ? ld3<R>(m.norms + n * 3) : v3<R>{R(1), R(1), R(1)};
+}
+
 template <class R>
 v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, int64_t f,
                   int32_t x, int32_t y, R* depth_f_out) {
   const t3_frame& fr = cx.sc->frame;
+  v3<R> pos, normal, tex = {R(0), R(0), R(0)}, color = {R(1), R(1), R(1)};
+  if (ob.mesh.kind == T3_MESH_PARTICLES) {
+    R df;
+    particle_frag(cx, ob.mesh, f, x, y, pos, normal, color, df);
+    if (depth_f_out) *depth_f_out = df;
+  } else {
   v3<R> v[3];
   mesh.verts(f, v);
   Setup<R> s;
@@ -747,8 +830,7 @@ v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, in
   v3<R> wei = face_weights(s, fr, x, y);
   if (depth_f_out) *depth_f_out = face_depth(s, wei);
   // interpolate (triangle.py:32-49)
-  v3<R> pos = add(add(muls(wei.x, v[0]), muls(wei.y, v[1])), muls(wei.z, v[2]));
-  v3<R> normal;
+  pos = add(add(muls(wei.x, v[0]), muls(wei.y, v[1])), muls(wei.z, v[2]));
   if (fr.flags & T3_SMOOTHING) {
     v3<R> n[3];
     mesh.norms(f, n);
@@ -757,12 +839,12 @@ v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, in
     normal = cross(sub(v[1], v[0]), sub(v[2], v[0]));
   }
   normal = normalized(normal);
-  v3<R> tex = {R(0), R(0), R(0)};
   if (fr.flags & T3_TEXTURING) {
     v3<R> t[3];
     mesh.coors(f, t);
     tex = add(add(muls(wei.x, t[0]), muls(wei.y, t[1])), muls(wei.z, t[2]));
     tex.z = R(0);
+  }
   }
   // calc_viewdir (shader.py:82-93)
   R px = (R)x + (R)fr.bias[0], py = (R)y + (R)fr.bias[1];
@@ -774,8 +856,8 @@ v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, in
   v3<R> viewdir = neg(rd);
 
   Frag<R> fg;
-  fg.pos = pos; fg.normal = normal; fg.texcoord = tex;
-  int64_t bf = mesh.base_face(f);
+  fg.pos = pos; fg.normal = normal; fg.texcoord = tex; fg.color = color;
+  int64_t bf = ob.mesh.kind == T3_MESH_PARTICLES ? f : mesh.base_face(f);
   fg.attr = ob.mesh.face_attr ? ob.mesh.face_attr + bf * ob.mesh.attr_stride : nullptr;
   MaterialEval<R> me{&ob.material, &fg};
   const t3_lighting& L = cx.sc->lighting;
@@ -834,6 +916,40 @@ inline void raster_face(const Ctx<R>& cx, const Setup<R>& s, uint64_t id,
   }
 }
 
+// one object into the packed (depth, global id) minimum, in parallel
+template <class R>
+void raster_object_keys(const Ctx<R>& cx, const t3_object& ob, std::atomic<uint64_t>* keys) {
+  const t3_frame& fr = cx.sc->frame;
+  const int H = fr.height;
+  if (ob.mesh.kind == T3_MESH_PARTICLES) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t f = 0; f < ob.nfaces; f++) {
+      ParS<R> p;
+      if (!particle_setup(cx, ob.mesh, f, p) || p.depth >= fr.maxdepth) continue;
+      const uint64_t key = pack_key(p.depth, (uint32_t)(ob.face_base + f));
+      for (int32_t x = p.botx; x <= p.topx; x++)
+        for (int32_t y = p.boty; y <= p.topy; y++) {
+          if (!particle_covers(p, particle_pixel_world(cx, p, x, y))) continue;
+          const int64_t P_ = (int64_t)x * H + y;
+          uint64_t cur = keys[P_].load(std::memory_order_relaxed);
+          while (key < cur && !keys[P_].compare_exchange_weak(cur, key)) {
+          }
+        }
+    }
+    return;
+  }
+  Mesh<R> mesh(&ob.mesh);
+#pragma omp parallel for schedule(dynamic, 2048)
+  for (int64_t f = 0; f < ob.nfaces; f++) {
+    v3<R> v[3];
+    mesh.verts(f, v);
+    Setup<R> s;
+    face_setup(cx.W2V, fr, v, s);
+    if (s.culled) continue;
+    raster_face(cx, s, (uint64_t)(ob.face_base + f), keys);
+  }
+}
+
 template <class R>
 int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb64,
            int32_t* id_out, int32_t* depth_out, float* depth_f_out, int nthreads) {
@@ -857,9 +973,27 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
     for (int o = 0; o < sc->nobjects; o++) {
       const t3_object& ob = sc->objects[o];
       Mesh<R> mesh(&ob.mesh);
-      // render_occup (triangle.py:89-131)
+      // render_occup (triangle.py:89-131; particle.py:74-114 for particles)
       std::fill(occup.begin(), occup.end(), -1);
-      for (int64_t f = 0; f < ob.nfaces; f++) {
+      if (ob.mesh.kind == T3_MESH_PARTICLES) {
+        for (int64_t f = 0; f < ob.nfaces; f++) {
+          ParS<R> p;
+          if (!particle_setup(cx, ob.mesh, f, p)) continue;
+          for (int32_t x = p.botx; x <= p.topx; x++) {
+            for (int32_t y = p.boty; y <= p.topy; y++) {
+              if (!particle_covers(p, particle_pixel_world(cx, p, x, y))) continue;
+              const int32_t d = p.depth;
+              int64_t P_ = (int64_t)x * H + y;
+              int32_t old = depth[P_];
+              if (d < old) depth[P_] = d;
+              if (old > d) {
+                if (depth[P_] >= d) { occup[P_] = f; gid[P_] = ob.face_base + f; }
+              }
+            }
+          }
+        }
+      }
+      for (int64_t f = 0; f < ob.nfaces && ob.mesh.kind != T3_MESH_PARTICLES; f++) {
         v3<R> v[3];
         mesh.verts(f, v);
         Setup<R> s;
@@ -896,15 +1030,7 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
     for (int o = 0; o < sc->nobjects; o++) {
       const t3_object& ob = sc->objects[o];
       Mesh<R> mesh(&ob.mesh);
-#pragma omp parallel for schedule(dynamic, 2048)
-      for (int64_t f = 0; f < ob.nfaces; f++) {
-        v3<R> v[3];
-        mesh.verts(f, v);
-        Setup<R> s;
-        face_setup(cx.W2V, fr, v, s);
-        if (s.culled) continue;
-        raster_face(cx, s, (uint64_t)(ob.face_base + f), keys.data());
-      }
+      raster_object_keys(cx, ob, keys.data());
     }
 #pragma omp parallel for schedule(dynamic, 1024)
     for (int64_t i = 0; i < P; i++) {
@@ -945,6 +1071,10 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
         const t3_object& ob = sc->objects[o];
         if (gid[i] >= ob.face_base && gid[i] < ob.face_base + ob.nfaces) {
           // the winning fragment's float depth, recomputed as render_color does
+          if (ob.mesh.kind == T3_MESH_PARTICLES) {
+            df = (float)mapply_pos(cx.W2V, ld3<R>(ob.mesh.verts + (gid[i] - ob.face_base) * 3)).z;
+            continue;
+          }
           Mesh<R> mesh(&ob.mesh);
           v3<R> v[3];
           mesh.verts(gid[i] - ob.face_base, v);
@@ -971,17 +1101,7 @@ inline std::vector<int64_t> raster_gids_f32(const t3_scene* sc) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < P; i++) keys[i].store(~0ull, std::memory_order_relaxed);
   for (int o = 0; o < sc->nobjects; o++) {
-    const t3_object& ob = sc->objects[o];
-    Mesh<float> mesh(&ob.mesh);
-#pragma omp parallel for schedule(dynamic, 2048)
-    for (int64_t f = 0; f < ob.nfaces; f++) {
-      v3<float> v[3];
-      mesh.verts(f, v);
-      Setup<float> s;
-      face_setup(cx.W2V, fr, v, s);
-      if (s.culled) continue;
-      raster_face(cx, s, (uint64_t)(ob.face_base + f), keys.data());
-    }
+    raster_object_keys(cx, sc->objects[o], keys.data());
   }
   std::vector<int64_t> gid(P);
 #pragma omp parallel for schedule(static)

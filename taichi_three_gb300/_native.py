@@ -31,7 +31,7 @@ T3_NOALLOC_MAX_PIXELS = 1 << 21
 T3_NOALLOC_MAX_BIG_FACES = 1 << 16
 
 T3_CULLING, T3_CLIPPING, T3_SMOOTHING, T3_TEXTURING, T3_TONEMAP = 1, 2, 4, 8, 16
-T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED = 0, 1, 2
+T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED, T3_MESH_PARTICLES = 0, 1, 2, 3
 T3_MESH_TRANSFORM, T3_MESH_NOCULL, T3_MESH_FLIP_ORDER, T3_MESH_FLIP_NORMAL, T3_MESH_FLAT_NORMAL = \
     1, 2, 4, 8, 16
 

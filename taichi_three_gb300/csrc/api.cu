@@ -114,6 +114,7 @@ static int check_mesh(const t3_mesh& m, int flags, int64_t nfaces) {
   if (nfaces < 0) return T3_EINVAL;
   if (nfaces == 0) return T3_OK;
   if (!m.verts) return T3_EINVAL;
+  if (m.kind == T3_MESH_PARTICLES) return m.coors ? T3_OK : T3_EINVAL;  // positions, radii
   if ((flags & T3_SMOOTHING) && !(m.flags & T3_MESH_FLAT_NORMAL) && !m.norms) return T3_EINVAL;
   if ((flags & T3_TEXTURING) && !m.coors) return T3_EINVAL;
   if (m.kind == T3_MESH_GRID) {
@@ -188,6 +189,12 @@ int max_lobes(const DevScene& sc) {
   int m = 1;
   for (int o = 0; o < sc.nobjects; o++) m = sc.obj[o].mat.nlobes > m ? sc.obj[o].mat.nlobes : m;
   return m;
+}
+
+static int has_particles(const t3_scene& sc) {
+  for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
+    if (sc.objects[o].mesh.kind == T3_MESH_PARTICLES && sc.objects[o].nfaces > 0) return 1;
+  return 0;
 }
 
 int64_t mesh_vertex_rows(const t3_mesh& m) {
@@ -346,6 +353,9 @@ int t3_raster(const t3_frame* frame, const t3_object* object, uint64_t* depth_id
   const size_t need = 256 + sizeof(uint32_t) * (size_t)(object->nfaces > 0 ? object->nfaces : 1);
   if (workspace_bytes < need) return T3_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
+  if (object->mesh.kind == T3_MESH_PARTICLES)  // ParticleRaster.render_occup
+    return cuda_rc(launch_raster_particles(*frame, *object, reinterpret_cast<unsigned long long*>(depth_id),
+                                           nullptr, st));
   uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
   BigQueue big;
   big.count = reinterpret_cast<uint32_t*>(ws);
@@ -422,12 +432,17 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
         big.vndc = out;
         vtx += align256(16 * (size_t)nv);
       }
+      if (scene->objects[o].mesh.kind == T3_MESH_PARTICLES) {
+        if (e == cudaSuccess) e = launch_raster_particles(scene->frame, scene->objects[o], keys, nullptr, st);
+        continue;
+      }
       if (e == cudaSuccess) e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
     }
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
       e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st);
   } else {
+    if (has_particles(*scene)) return T3_EUNSUPPORTED;  // particles rasterise in the direct path
     if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -483,7 +498,10 @@ int t3_raster_fragments(const t3_scene* scene, void* workspace, size_t workspace
     big.status = reinterpret_cast<int32_t*>(counters + 61);
     big.rec = nullptr;
     big.fragments = count;
-    e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
+    if (scene->objects[o].mesh.kind == T3_MESH_PARTICLES)
+      e = launch_raster_particles(scene->frame, scene->objects[o], keys, count, st);
+    else
+      e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
   }
   unsigned long long host = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&host, count, sizeof(host), cudaMemcpyDeviceToHost, st);

@@ -81,7 +81,10 @@ extern "C" int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t
     big.count = counters + o;
     big.status = status;
     big.rec = nullptr;
-    e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
+    if (scene->objects[o].mesh.kind == T3_MESH_PARTICLES)
+      e = launch_raster_particles(scene->frame, scene->objects[o], keys, nullptr, st);
+    else
+      e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
   }
   if (e == cudaSuccess) e = launch_shade(ds, dsc, keys, nullptr, *out, status, st);
   return e == cudaSuccess ? T3_OK : T3_ECUDA;

@@ -156,6 +156,89 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
   return cudaGetLastError();
 }
 
+// ---- particles (ParticleRaster.render_occup, tina/core/particle.py:74-114) ----
+// One thread per particle computes its screen bbox; the warp then walks the
+// 32 particles' bbox pixels cooperatively (as warp_raster does for faces) and
+// keeps the pixels whose world point at the particle's depth lies within the
+// radius; every pixel of a particle has the particle's depth.
+struct WarpPars {
+  float4 rec[32][2];  // (ax, ay, az, r2) (vz, depth, x0 | y0 << 16, id)
+  int h[32];
+  long long start[32];
+};
+
+template <int BLOCK, bool COUNT>
+__global__ void __launch_bounds__(BLOCK)
+k_raster_particles(const t3_frame fr, const t3_mesh mesh, int64_t npars, uint32_t face_base,
+                   unsigned long long* __restrict__ keys, unsigned long long* fragments) {
+  __shared__ WarpPars wps[BLOCK / 32];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  WarpPars& wp = wps[threadIdx.x >> 5];
+  GlobalKeySink<COUNT> sink{keys, fr.height, fragments};
+  const int64_t n = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  ParSetup p{};
+  bool live = false;
+  if (n < npars) {
+    live = particle_setup(fr, ld3(mesh.verts + n * 3), __ldg(mesh.coors + n), p) && p.depth < fr.maxdepth;
+  }
+  const long long area = live ? (long long)(p.topx - p.botx + 1) * (p.topy - p.boty + 1) : 0;
+  const unsigned lm = __ballot_sync(FULL, area > 0);
+  if (!lm) return;
+  long long incl = area;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const long long first = incl - area;
+  if (area > 0) {
+    const int r = __popc(lm & ((1u << lane) - 1u));
+    wp.rec[r][0] = make_float4(p.ax, p.ay, p.az, p.r2);
+    wp.rec[r][1] = make_float4(p.vz, __int_as_float(p.depth), __int_as_float(p.botx | (p.boty << 16)),
+                               __uint_as_float(face_base + (uint32_t)n));
+    wp.h[r] = p.topy - p.boty + 1;
+    wp.start[r] = first;
+  }
+  const long long total = __shfl_sync(FULL, incl, 31);
+  const unsigned upto = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+  __syncwarp();
+  int before = 0;
+  for (long long base = 0; base < total; base += 32) {
+    const unsigned bit = (area > 0 && first >= base && first < base + 32) ? 1u << (int)(first - base) : 0u;
+    const unsigned starts = __reduce_or_sync(FULL, bit);
+    const long long idx = base + lane;
+    if (idx < total) {
+      const int j = before + __popc(starts & upto) - 1;
+      const long long off = idx - wp.start[j];
+      const int h = wp.h[j];
+      const int q = (int)(off / h), r = (int)(off - (long long)q * h);
+      const float4 a = wp.rec[j][0], b = wp.rec[j][1];
+      ParSetup t;
+      t.ax = a.x; t.ay = a.y; t.az = a.z; t.r2 = a.w;
+      const int xy = __float_as_int(b.z);
+      const int x = (xy & 0xFFFF) + q, y = (xy >> 16) + r;
+      const f3 Pl = particle_pixel_world(fr, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1]), b.x);
+      if (particle_covers(t, Pl)) sink(x, y, pack_key(__float_as_int(b.y), __float_as_uint(b.w)));
+    }
+    before += __popc(starts);
+  }
+}
+
+cudaError_t launch_raster_particles(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
+                                    unsigned long long* fragments, cudaStream_t st) {
+  if (ob.nfaces <= 0) return cudaSuccess;
+  constexpr int BLOCK = 128;
+  const unsigned grid = (unsigned)((ob.nfaces + BLOCK - 1) / BLOCK);
+  if (fragments)
+    k_raster_particles<BLOCK, true><<<grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces, (uint32_t)ob.face_base,
+                                                            keys, fragments);
+  else
+    k_raster_particles<BLOCK, false><<<grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces, (uint32_t)ob.face_base,
+                                                             keys, nullptr);
+  return cudaGetLastError();
+}
+
 // u64 atomicMin throughput: n distinct addresses (L2 resident for n * 8 below
 // the L2 size), `rounds` reductions each, with decreasing values so every
 // reduction changes memory like a winning fragment does

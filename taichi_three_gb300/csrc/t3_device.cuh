@@ -308,4 +308,70 @@ __device__ __forceinline__ uint64_t pack_key(int32_t depth, uint32_t id) {
   return ((uint64_t)((uint32_t)depth ^ 0x80000000u) << 32) | (uint64_t)id;
 }
 
+// ---- particles (tina/core/particle.py) -----------------------------------------
+
+// mapply_dir (common.py:186-189): mapply with w = 0, in source order
+__device__ __forceinline__ f3 mapply_dir_x(const float* m, f3 d) {
+  f3 r;
+  float w;
+  mapply_x(m, d, 0.0f, r, w);
+  return r;
+}
+
+// from_viewport (engine.py:63-65): p / res * 2 - 1
+__device__ __forceinline__ float from_viewport_x(float p, float res) {
+  return xsub(xmul(xdiv(p, res), 2.0f), 1.0f);
+}
+
+struct ParSetup {
+  float ax, ay, az, r2;  // world centre, radius**2
+  float vz;              // NDC depth of the centre (the depth of every pixel)
+  int32_t depth;         // int(vz * maxdepth)
+  int32_t botx, boty, topx, topy;
+};
+
+// ParticleRaster.render_occup's per-particle part (particle.py:77-101); false
+// when clipped away or the bbox is empty
+__device__ __forceinline__ bool particle_setup(const t3_frame& fr, f3 A, float R, ParSetup& p) {
+  const f3 Av = mapply_pos_x(fr.W2V, A);
+  if ((fr.flags & T3_CLIPPING) && !(-1.0f <= Av.z && Av.z <= 1.0f)) return false;
+  const f3 DX = normalized_x(mapply_dir_x(fr.V2W, f3{1.0f, 0.0f, 0.0f}));
+  const f3 DY = normalized_x(mapply_dir_x(fr.V2W, f3{0.0f, 1.0f, 0.0f}));
+  const f3 AX = f3{xadd(A.x, xmul(DX.x, R)), xadd(A.y, xmul(DX.y, R)), xadd(A.z, xmul(DX.z, R))};
+  const f3 AY = f3{xadd(A.x, xmul(DY.x, R)), xadd(A.y, xmul(DY.y, R)), xadd(A.z, xmul(DY.z, R))};
+  const float rvx = xsub(mapply_pos_x(fr.W2V, AX).x, Av.x);
+  const float rvy = xsub(mapply_pos_x(fr.W2V, AY).y, Av.y);
+  const float W = (float)fr.width, H = (float)fr.height;
+  auto vp = [](float c, float res) { return xmul(xadd(xmul(c, 0.5f), 0.5f), res); };
+  // b = viewport of (Av - (rx,0)), (Av + (rx,0)), (Av - (0,ry)), (Av + (0,ry))
+  const float b0x = vp(xsub(Av.x, rvx), W), b0y = vp(xsub(Av.y, 0.0f), H);
+  const float b1x = vp(xadd(Av.x, rvx), W), b1y = vp(xadd(Av.y, 0.0f), H);
+  const float b2x = vp(xsub(Av.x, 0.0f), W), b2y = vp(xsub(Av.y, rvy), H);
+  const float b3x = vp(xadd(Av.x, 0.0f), W), b3y = vp(xadd(Av.y, rvy), H);
+  const int32_t lox = trunc_i32(floorf(fminf(b0x, b2x))), loy = trunc_i32(floorf(fminf(b0y, b2y)));
+  const int32_t hix = trunc_i32(ceilf(fmaxf(b1x, b3x))), hiy = trunc_i32(ceilf(fmaxf(b1y, b3y)));
+  p.botx = lox > 0 ? lox : 0;
+  p.boty = loy > 0 ? loy : 0;
+  p.topx = hix < fr.width - 1 ? hix : fr.width - 1;
+  p.topy = hiy < fr.height - 1 ? hiy : fr.height - 1;
+  p.ax = A.x; p.ay = A.y; p.az = A.z;
+  p.r2 = xmul(R, R);
+  p.vz = Av.z;
+  p.depth = trunc_i32(xmul(Av.z, (float)fr.maxdepth));
+  return p.botx <= p.topx && p.boty <= p.topy;
+}
+
+// the world point of pixel centre (px, py) at the particle's depth
+// (particle.py:103-105): mapply_pos(V2W, (from_viewport(p), Av.z))
+__device__ __forceinline__ f3 particle_pixel_world(const t3_frame& fr, float px, float py, float vz) {
+  const f3 Pv = f3{from_viewport_x(px, (float)fr.width), from_viewport_x(py, (float)fr.height), vz};
+  return mapply_pos_x(fr.V2W, Pv);
+}
+
+// (Pl - Al).norm_sqr() <= Rl**2
+__device__ __forceinline__ bool particle_covers(const ParSetup& p, f3 Pl) {
+  const float dx = xsub(Pl.x, p.ax), dy = xsub(Pl.y, p.ay), dz = xsub(Pl.z, p.az);
+  return !(xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz)) > p.r2);
+}
+
 } // namespace t3

@@ -83,6 +83,8 @@ struct DevScene {
 int flatten_material(const t3_material& in, DevMaterial& out);
 int make_dev_scene(const t3_scene& sc, DevScene& out);
 
+cudaError_t launch_raster_particles(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
+                                    unsigned long long* fragments, cudaStream_t st);
 cudaError_t launch_vertex_ndc(const t3_frame& fr, const t3_mesh& mesh, int64_t nverts, float4* out,
                               cudaStream_t st);
 int64_t mesh_vertex_rows(const t3_mesh& m);  // rows the vertex stage transforms (0: none)

@@ -46,6 +46,7 @@ struct Frag {
   V3 pos, normal;
   f2 tex;
   const float* attr;
+  V3 color;  // Input('color'): white on triangles (triangle.py:48), the particle's colour
 };
 
 // CONST / ATTR / INPUT node value (scalars broadcast to all three lanes)
@@ -60,7 +61,7 @@ __device__ __forceinline__ V3 eval_basic(const t3_node& nd, const Frag& fg) {
     }
     return v3(__ldg(fg.attr + nd.a), __ldg(fg.attr + nd.a + 1), __ldg(fg.attr + nd.a + 2));
   case T3_OP_INPUT:
-    return nd.a == 0 ? fg.pos : nd.a == 1 ? v3(1.f, 1.f, 1.f) : nd.a == 2 ? fg.normal
+    return nd.a == 0 ? fg.pos : nd.a == 1 ? fg.color : nd.a == 2 ? fg.normal
                                                                         : v3(fg.tex.x, fg.tex.y, 0.f);
   default:
     return v3(0.f, 0.f, 0.f);
@@ -295,6 +296,30 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   g.ob = &ob;
   const t3_mesh& mesh = ob.mesh;
   const int64_t n = (int64_t)gid - ob.face_base;
+  if (mesh.kind == T3_MESH_PARTICLES) {
+    // ParticleRaster.render_color (particle.py:116-146)
+    const f3 A = ld3(mesh.verts + n * 3);
+    const float Rl = __ldg(mesh.coors + n);
+    const float vz = mapply_pos_x(fr.W2V, A).z;
+    if (out.face_id) out.face_id[i] = (int32_t)gid;
+    if (out.depth) out.depth[i] = (int32_t)((uint32_t)(key >> 32) ^ 0x80000000u);
+    if (out.depth_f) out.depth_f[i] = vz;
+    const float px = xadd((float)x, fr.bias[0]), py = xadd((float)y, fr.bias[1]);
+    const f3 Pl = particle_pixel_world(fr, px, py, vz);
+    f3 D = f3{xdiv(xsub(Pl.x, A.x), Rl), xdiv(xsub(Pl.y, A.y), Rl), xdiv(xsub(Pl.z, A.z), Rl)};
+    const f3 Z = normalized_x(mapply_dir_x(fr.V2W, f3{0.0f, 0.0f, 1.0f}));
+    const float h = __fsqrt_rn(xsub(1.0f, dot_x(D, D)));
+    D = normalized_x(f3{xsub(D.x, xmul(Z.x, h)), xsub(D.y, xmul(Z.y, h)), xsub(D.z, xmul(Z.z, h))});
+    Frag& fp = g.fg;
+    fp.normal = tov(D);
+    fp.pos = v3(xadd(A.x, xmul(D.x, Rl)), xadd(A.y, xmul(D.y, Rl)), xadd(A.z, xmul(D.z, Rl)));
+    fp.tex = f2{0.f, 0.f};
+    fp.attr = mesh.face_attr ? mesh.face_attr + n * mesh.attr_stride : nullptr;
+    fp.color = mesh.norms ? tov(ld3(mesh.norms + n * 3)) : v3(1.f, 1.f, 1.f);
+    const V3 rd = view_ray(fr, px, py);
+    g.vdir = v3(-rd.x, -rd.y, -rd.z);
+    return true;
+  }
   const FaceRef ref = face_ref(mesh, n);
   // start every gather of this face now: normals and material attributes are
   // needed only after the weights, but their DRAM latency overlaps from here
@@ -351,6 +376,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
                 (wei.x * t[0].y + wei.y * t[1].y) + wei.z * t[2].y};
   }
   fg.attr = mesh.face_attr ? mesh.face_attr + ref.f * mesh.attr_stride : nullptr;
+  fg.color = v3(1.f, 1.f, 1.f);
   const V3 rd = view_ray(fr, px, py);
   g.vdir = v3(-rd.x, -rd.y, -rd.z);
   return true;

@@ -440,3 +440,59 @@ class MeshNoCulling(MeshEditBase):
         self.mesh._t3_fill(m, device, keep)
         self._check_inner(m, N.T3_MESH_NOCULL)
         m.flags |= N.T3_MESH_NOCULL
+
+
+class SimpleParticles:
+    """Particles (tina/pars/simple.py): positions [n, 3], radii [n] (default
+    `radius`), colours [n, 3] (default white), rasterised as shaded spheres by
+    the particle rasteriser (tina/core/particle.py); Input('color') of the
+    material reads the particle's colour."""
+
+    def __init__(self, maxpars=65536, radius=0.02):
+        dev = default_device()
+        self.maxpars = int(maxpars)
+        self.radius = float(radius)
+        self.npars = 0
+        self.verts = torch.zeros((0, 3), dtype=torch.float32, device=dev)
+        self.sizes = torch.zeros((0,), dtype=torch.float32, device=dev)
+        self.colors = torch.zeros((0, 3), dtype=torch.float32, device=dev)
+
+    def get_npars(self):
+        return min(self.npars, self.maxpars)
+
+    def pre_compute(self):
+        pass
+
+    def set_particles(self, verts):
+        v = as_f32(verts)
+        if v.dim() != 2 or v.shape[1] != 3:
+            raise ValueError('particle positions must have shape [n, 3]')
+        n = min(v.shape[0], self.maxpars)
+        self.npars = n
+        self.verts = v[:n].contiguous()
+        if self.sizes.shape[0] != n:
+            self.sizes = torch.full((n,), self.radius, dtype=torch.float32, device=self.verts.device)
+        if self.colors.shape[0] != n:
+            self.colors = torch.ones((n, 3), dtype=torch.float32, device=self.verts.device)
+
+    def set_particle_radii(self, sizes):
+        s = as_f32(sizes).reshape(-1)
+        if s.shape[0] < self.npars:
+            raise ValueError('need one radius per particle')
+        self.sizes = s[:self.npars].contiguous()
+
+    def set_particle_colors(self, colors):
+        c = as_f32(colors)
+        if c.dim() != 2 or c.shape[0] < self.npars or c.shape[1] != 3:
+            raise ValueError('particle colours must have shape [n, 3]')
+        self.colors = c[:self.npars].contiguous()
+
+    def attr_stride(self):
+        return 0
+
+    def _t3_fill(self, m, device, keep):
+        m.kind = N.T3_MESH_PARTICLES
+        m.nfaces = self.get_npars()
+        m.verts = ptr(self.verts, device, keep)
+        m.coors = ptr(self.sizes, device, keep)
+        m.norms = ptr(self.colors, device, keep)

@@ -107,6 +107,25 @@ class TriangleRaster:
         shader.shade_from_keys(self, self.keys)
 
 
+class ParticleRaster:
+    """ParticleRaster (tina/core/particle.py): particles rasterised as shaded
+    spheres into the same depth buffer as the triangles (the scene's frame is
+    rendered by t3_render; particles take the direct rasteriser).  Options
+    kept: maxpars, coloring, clipping."""
+
+    def __init__(self, engine, maxpars=None, coloring=True, clipping=True, **extra_options):
+        self.engine = engine
+        self.maxpars = maxpars
+        self.coloring = coloring
+        self.clipping = clipping
+
+    def check_faces(self, pars):
+        n = pars.get_npars()
+        if self.maxpars is not None and n > self.maxpars:
+            raise ValueError(f'{n} particles, more than maxpars={self.maxpars}')
+        return n
+
+
 class Shader:
     """Shader(img, lighting, material) (tina/core/shader.py:112-135): shades the
     winning fragments of one raster into `img`."""
@@ -219,8 +238,14 @@ class Scene:
                 if self.triangle_raster is None:
                     self.triangle_raster = TriangleRaster(self.engine, **self.raster_options)
                 raster = self.triangle_raster
-            elif hasattr(object, 'get_npars') or hasattr(object, 'sample_volume'):
-                raise NotImplementedError('particle / volume rasterisation is not part of this build')
+            elif hasattr(object, 'get_npars'):
+                if getattr(self, 'particle_raster', None) is None:
+                    self.particle_raster = ParticleRaster(
+                        self.engine, **{k: self.options[k] for k in ('maxpars', 'coloring', 'clipping')
+                                        if k in self.options})
+                raster = self.particle_raster
+            elif hasattr(object, 'sample_volume'):
+                raise NotImplementedError('volume rasterisation is not part of this build')
             else:
                 raise ValueError(f'cannot determine raster type of object: {object}')
         if len(self.objects) >= N.T3_MAX_OBJECTS:
@@ -252,6 +277,8 @@ class Scene:
         for o, (obj, info) in enumerate(self.objects.items()):
             ob = sc.objects[o]
             obj._t3_fill(ob.mesh, device, keep)
+            if isinstance(info.raster, ParticleRaster) and not info.raster.coloring:
+                ob.mesh.norms = None  # white particles (ParticleRaster(coloring=False))
             n = info.raster.check_faces(obj)
             ob.nfaces = n
             ob.face_base = base
