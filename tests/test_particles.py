@@ -59,7 +59,8 @@ def test_particles_parity(cuda, oracle_mod):
 
 @pytest.mark.gpu
 def test_particles_with_triangles_and_pbr(cuda, oracle_mod):
-    scene, _ = tina.workloads.soup_scene(ntri=3000, res=(128, 96), seed=4, nlights=3)
+    arrays = tina.workloads.soup_arrays(3000, 4, median_sigma=0.08, log_sd=0.6)
+    scene, _ = tina.workloads.soup_scene(ntri=3000, res=(128, 96), seed=4, nlights=3, arrays=arrays)
     pos, rad, col = _pars(200, 2, 0.03, 0.1)
     pars = tina.SimpleParticles()
     pars.set_particles(pos)
@@ -67,7 +68,7 @@ def test_particles_with_triangles_and_pbr(cuda, oracle_mod):
     pars.set_particle_colors(col)
     scene.add_object(pars, tina.PBR(basecolor='color', metallic=0.4, roughness=0.3))
     fid = _render_both(scene, oracle_mod)
-    assert (fid >= 3000).sum() > 500 and ((fid >= 0) & (fid < 3000)).sum() > 500
+    assert (fid >= 3000).sum() > 300 and ((fid >= 0) & (fid < 3000)).sum() > 300
 
 
 @pytest.mark.gpu
