@@ -9,7 +9,7 @@ the raster path is imported: its subpackage __init__ files (which pull in the
 path tracer, GUI and asset loaders) are replaced by empty packages, and
 tina/hacker.py -- monkey-patches of Taichi internals -- by an empty module.
 
-Usage (where the reference is mounted):  python tests/golden/make_golden.py
+Usage (where the reference is mounted):  python tests/golden/make_golden.py [name ...]
 """
 import importlib
 import os
@@ -26,7 +26,7 @@ sys.path.insert(0, HERE)
 MODULES = ['tina.common', 'tina.advans', 'tina.matr.nodes', 'tina.matr.material', 'tina.core.engine',
            'tina.core.shader', 'tina.core.lighting', 'tina.core.triangle', 'tina.mesh.base',
            'tina.mesh.simple', 'tina.mesh.prim', 'tina.mesh.trans', 'tina.mesh.cull', 'tina.mesh.grid',
-           'tina.mesh.norm', 'tina.postp.tonemap', 'tina.util.matrix', 'tina.scene.raster']
+           'tina.mesh.norm', 'tina.core.particle', 'tina.pars.simple', 'tina.postp.tonemap', 'tina.util.matrix', 'tina.scene.raster']
 
 
 def load_reference():
@@ -37,7 +37,7 @@ def load_reference():
     pkg = types.ModuleType('tina')
     pkg.__path__ = [root]
     sys.modules['tina'] = pkg
-    for sub in ('core', 'matr', 'mesh', 'postp', 'scene', 'util'):
+    for sub in ('core', 'matr', 'mesh', 'pars', 'postp', 'scene', 'util'):
         m = types.ModuleType('tina.' + sub)
         m.__path__ = [os.path.join(root, sub)]
         sys.modules['tina.' + sub] = m
@@ -61,7 +61,10 @@ def load_reference():
 def main():
     from recipes import NAMES, build, inputs
     tina, matrix = load_reference()
+    only = sys.argv[1:]
     for name in NAMES:
+        if only and name not in only:
+            continue
         t0 = time.time()
         arrays = inputs(name)
         scene, single = build(tina, name, arrays, matrix)
@@ -69,7 +72,8 @@ def main():
         out = {'img': scene.img.to_numpy().astype(np.float32),
                'depth': scene.engine.depth.to_numpy().astype(np.int32)}
         if single:
-            out['occup'] = scene.triangle_raster.occup.to_numpy().astype(np.int32)
+            raster = getattr(scene, 'triangle_raster', None) or scene.particle_raster
+            out['occup'] = raster.occup.to_numpy().astype(np.int32)
         np.savez_compressed(os.path.join(HERE, name + '.npz'),
                             **{'in_' + k: v for k, v in arrays.items()}, **out)
         cov = int((out['depth'] < 2**30).sum())

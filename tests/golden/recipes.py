@@ -42,11 +42,21 @@ def inputs(name):
         return {'pos': pos}
     if name == 'sphere_lambert':
         return {}
+    if name in ('particles', 'pars_mixed'):
+        rng = np.random.Generator(np.random.PCG64(11 if name == 'particles' else 12))
+        n = 60
+        out = {'pos': rng.uniform(-0.8, 0.8, size=(n, 3)).astype(np.float32),
+               'radii': rng.uniform(0.05, 0.24, size=n).astype(np.float32),
+               'colors': rng.uniform(0.2, 1.0, size=(n, 3)).astype(np.float32)}
+        if name == 'pars_mixed':
+            verts, norms = _soup(80, 13, sigma=0.35)
+            out.update(verts=verts, norms=norms)
+        return out
     raise KeyError(name)
 
 
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
-         'two_objects']
+         'two_objects', 'particles', 'pars_mixed']
 
 
 def build(tina, name, arrays, matrix):
@@ -116,6 +126,31 @@ def build(tina, name, arrays, matrix):
         scene.add_object(m1, tina.Diffuse(color=[0.9, 0.6, 0.3]))
         scene.add_object(m2, tina.Lamp(color=[0.2, 0.5, 1.0]))
         scene.engine.set_camera(matrix.lookat(back=(0, 0, 3)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'particles':
+        scene = tina.Scene(48, 36)
+        pars = tina.SimpleParticles(maxpars=64)
+        pars.set_particles(arrays['pos'])
+        pars.set_particle_radii(arrays['radii'])
+        pars.set_particle_colors(arrays['colors'])
+        scene.add_object(pars, tina.PBR(basecolor='color', metallic=0.2, roughness=0.4))
+        scene.lighting.clear_lights()
+        scene.lighting.add_light(pos=[1.5, 1.0, 2.0], color=[3.0, 3.0, 3.0])
+        scene.lighting.add_light(dir=[0.2, -0.4, 1.0], color=[0.4, 0.4, 0.4])
+        scene.engine.set_camera(matrix.lookat(back=(0.2, 0.3, 3)), matrix.perspective(60, 48 / 36))
+        return scene, True
+    if name == 'pars_mixed':
+        scene = tina.Scene(48, 36, smoothing=True)
+        mesh = tina.SimpleMesh()
+        mesh.set_face_verts(arrays['verts'])
+        mesh.set_face_norms(arrays['norms'])
+        scene.add_object(mesh, tina.Diffuse(color=[0.9, 0.6, 0.3]))
+        pars = tina.SimpleParticles(maxpars=64)
+        pars.set_particles(arrays['pos'])
+        pars.set_particle_radii(arrays['radii'])
+        pars.set_particle_colors(arrays['colors'])
+        scene.add_object(pars, tina.Classic())
+        scene.engine.set_camera(matrix.lookat(back=(-0.3, 0.2, 3)), matrix.perspective(60, 48 / 36))
         return scene, False
     raise KeyError(name)
 
