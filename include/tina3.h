@@ -45,6 +45,7 @@ extern "C" {
 #define T3_SMOOTHING 4  /* interpolate vertex normals     triangle.py:36-38 */
 #define T3_TEXTURING 8  /* interpolate texcoords          triangle.py:44-46 */
 #define T3_TONEMAP 16   /* ACES after shading             scene/raster.py:202-203 */
+#define T3_WIRE_CLIPPING 32 /* WireframeRaster(clipping=True) wireframe.py:78-81 */
 
 typedef struct t3_frame {
   int32_t width, height; /* Engine.res                                      */
@@ -54,7 +55,8 @@ typedef struct t3_frame {
   float V2W[16];         /* inv(proj @ view), float32                       */
   float bias[2];         /* pixel-centre offset, (0.5, 0.5) by default      */
   float bgcolor[3];      /* Scene(bgcolor=...) image.fill value             */
-  int32_t _pad;
+  float linecolor[3];    /* WireframeRaster(linecolor=...), wireframe.py:6-20 */
+  int32_t _pad[2];       /* 184 bytes: keeps t3_scene.lighting.lights 16-byte aligned */
 } t3_frame;
 
 /* ---- meshes (the mesh protocol of the tina.mesh package) ----------------------------- */
@@ -65,6 +67,9 @@ typedef struct t3_frame {
                                (tina/core/particle.py): nfaces = particles,
                                verts = positions [n,3], coors = radii [n],
                                norms = colours [n,3] (nullptr: white); direct raster only */
+#define T3_MESH_LINES 4   /* SimpleMesh(npolygon=2) (tina/mesh/simple.py): verts [n,2,3];
+                             drawn by the wireframe rasteriser (tina/core/wireframe.py);
+                             direct raster only, flags: TRANSFORM, WIREFRAME            */
 
 /* mesh flags (mesh-edit nodes) */
 #define T3_MESH_TRANSFORM 1   /* MeshTransform        tina/mesh/trans.py:23-40 */
@@ -72,6 +77,12 @@ typedef struct t3_frame {
 #define T3_MESH_FLIP_ORDER 4  /* MeshFlipCulling      tina/mesh/cull.py:5-28   */
 #define T3_MESH_FLIP_NORMAL 8 /* MeshFlipNormal       tina/mesh/cull.py:61-66  */
 #define T3_MESH_FLAT_NORMAL 16/* MeshFlatNormal       tina/mesh/norm.py:5-14   */
+#define T3_MESH_WIREFRAME 32  /* MeshToWire           tina/mesh/wire.py:5-40:
+                                 the object is the polygon edges of the mesh as
+                                 lines: line n = corners (n % p, (n+1) % p) of
+                                 face n / p, p = 3 (2 for T3_MESH_LINES), over
+                                 the faces after the other edits (NOCULL doubles
+                                 them); object nfaces = lines; direct raster only */
 
 typedef struct t3_mesh {
   int32_t kind;        /* T3_MESH_*                                              */

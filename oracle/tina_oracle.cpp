@@ -813,10 +813,96 @@ template <class R> void particle_frag(const Ctx<R>& cx, const t3_mesh& m, int64_
   color = m.norms ? ld3<R>(m.norms + n * 3) : v3<R>{R(1), R(1), R(1)};
 }
 
+// ---------------------------------------------------------------------------
+// Wireframe (tina/core/wireframe.py; lines of SimpleMesh(npolygon=2),
+// tina/mesh/simple.py, or MeshToWire, tina/mesh/wire.py).
+// ---------------------------------------------------------------------------
+inline bool is_wire(const t3_mesh& m) { return m.kind == T3_MESH_LINES || (m.flags & T3_MESH_WIREFRAME) != 0; }
+inline bool is_point_or_line(const t3_mesh& m) { return m.kind == T3_MESH_PARTICLES || is_wire(m); }
+
+// world endpoints of line n: MeshToWire._get_face_props (wire.py:20-27) takes
+// corners n % p and (n + 1) % p of face n // p
+template <class R> void wire_endpoints(const t3_mesh& m, int64_t n, v3<R>& A, v3<R>& B) {
+  if (m.kind == T3_MESH_LINES) {
+    const int p = (m.flags & T3_MESH_WIREFRAME) ? 2 : 1;
+    const int64_t l = n / p;
+    const int e = (int)(n % p);
+    v3<R> c[2] = {ld3<R>(m.verts + l * 6), ld3<R>(m.verts + l * 6 + 3)};
+    if (m.flags & T3_MESH_TRANSFORM) {
+      mat4<R> T;
+      for (int i = 0; i < 16; i++) T.m[i] = (R)m.trans[i];
+      c[0] = mapply_pos(T, c[0]);
+      c[1] = mapply_pos(T, c[1]);
+    }
+    A = c[e];
+    B = c[(e + 1) % 2];
+    return;
+  }
+  Mesh<R> mesh(&m);
+  v3<R> v[3];
+  mesh.verts(n / 3, v);
+  A = v[n % 3];
+  B = v[(n % 3 + 1) % 3];
+}
+
+template <class R> struct WireS {
+  v2<R> a, k;     // viewport start, step (draw_line, wireframe.py:49-64)
+  R az, bz;       // NDC depths of the endpoints
+  R wsa, wsb;     // wscale = 1 / clip w
+  int32_t siz;
+};
+
+// render_color's per-line part (wireframe.py:72-83); false when clipped or
+// when range(siz + 1) is empty in int32 (siz < 0, or siz + 1 overflowing)
+template <class R> bool wire_setup(const Ctx<R>& cx, v3<R> A, v3<R> B, WireS<R>& s) {
+  const t3_frame& fr = cx.sc->frame;
+  v3<R> ra, rb;
+  R wa, wb;
+  mapply(cx.W2V, A, R(1), ra, wa);
+  mapply(cx.W2V, B, R(1), rb, wb);
+  const v3<R> Av = divs(ra, wa), Bv = divs(rb, wb);
+  if ((fr.flags & T3_WIRE_CLIPPING) && !inside_clip(Av) && !inside_clip(Bv)) return false;
+  s.a = to_viewport(Av, fr.width, fr.height);
+  const v2<R> b = to_viewport(Bv, fr.width, fr.height);
+  s.az = Av.z;
+  s.bz = Bv.z;
+  s.wsa = R(1) / wa;
+  s.wsb = R(1) / wb;
+  const v2<R> d = {b.x - s.a.x, b.y - s.a.y};
+  if (std::fabs(d.x) >= std::fabs(d.y)) {
+    s.k.x = d.x >= R(0) ? R(1) : R(-1);
+    s.k.y = s.k.x * d.y / d.x;
+    s.siz = trunc_i32(std::fabs(d.x));
+  } else {
+    s.k.y = d.y >= R(0) ? R(1) : R(-1);
+    s.k.x = s.k.y * d.x / d.y;
+    s.siz = trunc_i32(std::fabs(d.y));
+  }
+  return s.siz >= 0 && s.siz != INT32_MAX;
+}
+
+// step i (wireframe.py:84-92): pixel and int depth; false outside the frame
+template <class R> bool wire_step(const t3_frame& fr, const WireS<R>& s, int32_t i, int32_t& x, int32_t& y,
+                                  int32_t& depth) {
+  const R fi = (R)i;
+  x = trunc_i32(std::floor((s.a.x + s.k.x * fi) + (R)fr.bias[0]));
+  y = trunc_i32(std::floor((s.a.y + s.k.y * fi) + (R)fr.bias[1]));
+  if (!(0 <= x && x < fr.width && 0 <= y && y < fr.height)) return false;
+  const R cor = fi / (R)s.siz;
+  R w0 = (R(1) - cor) * s.wsa, w1 = cor * s.wsb;
+  const R sum = w0 + w1;
+  w0 = w0 / sum;
+  w1 = w1 / sum;
+  depth = trunc_i32((w0 * s.az + w1 * s.bz) * (R)fr.maxdepth);
+  return true;
+}
+
 template <class R>
 v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, int64_t f,
                   int32_t x, int32_t y, R* depth_f_out) {
   const t3_frame& fr = cx.sc->frame;
+  // Shader.blend_color(..., factor=1, linecolor) (wireframe.py:93-97, shader.py:133-135)
+  if (is_wire(ob.mesh)) return {(R)fr.linecolor[0], (R)fr.linecolor[1], (R)fr.linecolor[2]};
   v3<R> pos, normal, tex = {R(0), R(0), R(0)}, color = {R(1), R(1), R(1)};
   if (ob.mesh.kind == T3_MESH_PARTICLES) {
     R df;
@@ -938,6 +1024,25 @@ void raster_object_keys(const Ctx<R>& cx, const t3_object& ob, std::atomic<uint6
     }
     return;
   }
+  if (is_wire(ob.mesh)) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t f = 0; f < ob.nfaces; f++) {
+      v3<R> A, B;
+      wire_endpoints<R>(ob.mesh, f, A, B);
+      WireS<R> s;
+      if (!wire_setup(cx, A, B, s)) continue;
+      for (int32_t i = 0; i <= s.siz; i++) {
+        int32_t x, y, d;
+        if (!wire_step(fr, s, i, x, y, d) || d >= fr.maxdepth) continue;
+        const uint64_t key = pack_key(d, (uint32_t)(ob.face_base + f));
+        const int64_t P_ = (int64_t)x * H + y;
+        uint64_t cur = keys[P_].load(std::memory_order_relaxed);
+        while (key < cur && !keys[P_].compare_exchange_weak(cur, key)) {
+        }
+      }
+    }
+    return;
+  }
   Mesh<R> mesh(&ob.mesh);
 #pragma omp parallel for schedule(dynamic, 2048)
   for (int64_t f = 0; f < ob.nfaces; f++) {
@@ -993,7 +1098,27 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
           }
         }
       }
-      for (int64_t f = 0; f < ob.nfaces && ob.mesh.kind != T3_MESH_PARTICLES; f++) {
+      if (is_wire(ob.mesh)) {
+        // WireframeRaster.render_color (wireframe.py:69-97): lines in order,
+        // steps in order, each through the depth test
+        for (int64_t f = 0; f < ob.nfaces; f++) {
+          v3<R> A, B;
+          wire_endpoints<R>(ob.mesh, f, A, B);
+          WireS<R> s;
+          if (!wire_setup(cx, A, B, s)) continue;
+          for (int32_t i = 0; i <= s.siz; i++) {
+            int32_t x, y, d;
+            if (!wire_step(fr, s, i, x, y, d)) continue;
+            int64_t P_ = (int64_t)x * H + y;
+            int32_t old = depth[P_];
+            if (d < old) depth[P_] = d;
+            if (old > d) {
+              if (depth[P_] >= d) { occup[P_] = f; gid[P_] = ob.face_base + f; }
+            }
+          }
+        }
+      }
+      for (int64_t f = 0; f < ob.nfaces && !is_point_or_line(ob.mesh); f++) {
         v3<R> v[3];
         mesh.verts(f, v);
         Setup<R> s;
@@ -1073,6 +1198,10 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
           // the winning fragment's float depth, recomputed as render_color does
           if (ob.mesh.kind == T3_MESH_PARTICLES) {
             df = (float)mapply_pos(cx.W2V, ld3<R>(ob.mesh.verts + (gid[i] - ob.face_base) * 3)).z;
+            continue;
+          }
+          if (is_wire(ob.mesh)) {  // a line pixel: its int depth over maxdepth
+            df = (float)((R)depth[i] / (R)fr.maxdepth);
             continue;
           }
           Mesh<R> mesh(&ob.mesh);

@@ -31,9 +31,11 @@ T3_NOALLOC_MAX_PIXELS = 1 << 21
 T3_NOALLOC_MAX_BIG_FACES = 1 << 16
 
 T3_CULLING, T3_CLIPPING, T3_SMOOTHING, T3_TEXTURING, T3_TONEMAP = 1, 2, 4, 8, 16
-T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED, T3_MESH_PARTICLES = 0, 1, 2, 3
+T3_WIRE_CLIPPING = 32
+T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED, T3_MESH_PARTICLES, T3_MESH_LINES = 0, 1, 2, 3, 4
 T3_MESH_TRANSFORM, T3_MESH_NOCULL, T3_MESH_FLIP_ORDER, T3_MESH_FLIP_NORMAL, T3_MESH_FLAT_NORMAL = \
     1, 2, 4, 8, 16
+T3_MESH_WIREFRAME = 32
 
 T3_OP_CONST, T3_OP_ATTR, T3_OP_INPUT, T3_OP_FRESNEL, T3_OP_TEXTURE, T3_OP_CHECKER = 0, 1, 2, 3, 4, 5
 T3_OP_LAMBERT, T3_OP_PHONG, T3_OP_COOK, T3_OP_EMISSION = 16, 17, 18, 19
@@ -48,7 +50,8 @@ T3_RASTER_DIRECT, T3_RASTER_BINNED = 0, 1
 class t3_frame(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("flags", C.c_int32),
                 ("maxdepth", C.c_int32), ("W2V", C.c_float * 16), ("V2W", C.c_float * 16),
-                ("bias", C.c_float * 2), ("bgcolor", C.c_float * 3), ("_pad", C.c_int32)]
+                ("bias", C.c_float * 2), ("bgcolor", C.c_float * 3), ("linecolor", C.c_float * 3),
+                ("_pad", C.c_int32 * 2)]
 
 
 class t3_mesh(C.Structure):

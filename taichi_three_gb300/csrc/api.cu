@@ -115,6 +115,16 @@ static int check_mesh(const t3_mesh& m, int flags, int64_t nfaces) {
   if (nfaces == 0) return T3_OK;
   if (!m.verts) return T3_EINVAL;
   if (m.kind == T3_MESH_PARTICLES) return m.coors ? T3_OK : T3_EINVAL;  // positions, radii
+  if (m.kind == T3_MESH_LINES) {
+    // line soup: only MeshTransform / MeshToWire edits apply, one or two lines per entry
+    if (m.flags & ~(T3_MESH_TRANSFORM | T3_MESH_WIREFRAME)) return T3_EINVAL;
+    return nfaces <= m.nfaces * ((m.flags & T3_MESH_WIREFRAME) ? 2 : 1) ? T3_OK : T3_EINVAL;
+  }
+  if (m.flags & T3_MESH_WIREFRAME) {
+    // MeshToWire: three lines per face of the (NOCULL-doubled) mesh
+    if (nfaces > m.nfaces * ((m.flags & T3_MESH_NOCULL) ? 2 : 1) * 3) return T3_EINVAL;
+    flags &= ~(T3_SMOOTHING | T3_TEXTURING);  // lines read positions only
+  }
   if ((flags & T3_SMOOTHING) && !(m.flags & T3_MESH_FLAT_NORMAL) && !m.norms) return T3_EINVAL;
   if ((flags & T3_TEXTURING) && !m.coors) return T3_EINVAL;
   if (m.kind == T3_MESH_GRID) {
@@ -191,9 +201,9 @@ int max_lobes(const DevScene& sc) {
   return m;
 }
 
-static int has_particles(const t3_scene& sc) {
+static int has_points_or_lines(const t3_scene& sc) {
   for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
-    if (sc.objects[o].mesh.kind == T3_MESH_PARTICLES && sc.objects[o].nfaces > 0) return 1;
+    if (is_point_or_line(sc.objects[o].mesh) && sc.objects[o].nfaces > 0) return 1;
   return 0;
 }
 
@@ -353,9 +363,9 @@ int t3_raster(const t3_frame* frame, const t3_object* object, uint64_t* depth_id
   const size_t need = 256 + sizeof(uint32_t) * (size_t)(object->nfaces > 0 ? object->nfaces : 1);
   if (workspace_bytes < need) return T3_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
-  if (object->mesh.kind == T3_MESH_PARTICLES)  // ParticleRaster.render_occup
-    return cuda_rc(launch_raster_particles(*frame, *object, reinterpret_cast<unsigned long long*>(depth_id),
-                                           nullptr, st));
+  if (is_point_or_line(object->mesh))  // ParticleRaster / WireframeRaster
+    return cuda_rc(launch_raster_point_or_line(*frame, *object,
+                                               reinterpret_cast<unsigned long long*>(depth_id), nullptr, st));
   uint8_t* ws = reinterpret_cast<uint8_t*>(workspace);
   BigQueue big;
   big.count = reinterpret_cast<uint32_t*>(ws);
@@ -425,6 +435,10 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
       big.count = counters + o;
       big.status = status;
       big.rec = reinterpret_cast<float4*>(ws + L.rec);
+      if (is_point_or_line(scene->objects[o].mesh)) {
+        e = launch_raster_point_or_line(scene->frame, scene->objects[o], keys, nullptr, st);
+        continue;
+      }
       const int64_t nv = mesh_vertex_rows(scene->objects[o].mesh);
       if (nv > 0 && scene->objects[o].nfaces > 0) {
         float4* out = reinterpret_cast<float4*>(ws + vtx);
@@ -432,17 +446,13 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
         big.vndc = out;
         vtx += align256(16 * (size_t)nv);
       }
-      if (scene->objects[o].mesh.kind == T3_MESH_PARTICLES) {
-        if (e == cudaSuccess) e = launch_raster_particles(scene->frame, scene->objects[o], keys, nullptr, st);
-        continue;
-      }
       if (e == cudaSuccess) e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
     }
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
       e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st);
   } else {
-    if (has_particles(*scene)) return T3_EUNSUPPORTED;  // particles rasterise in the direct path
+    if (has_points_or_lines(*scene)) return T3_EUNSUPPORTED;  // particles and lines: direct path only
     if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -498,8 +508,8 @@ int t3_raster_fragments(const t3_scene* scene, void* workspace, size_t workspace
     big.status = reinterpret_cast<int32_t*>(counters + 61);
     big.rec = nullptr;
     big.fragments = count;
-    if (scene->objects[o].mesh.kind == T3_MESH_PARTICLES)
-      e = launch_raster_particles(scene->frame, scene->objects[o], keys, count, st);
+    if (is_point_or_line(scene->objects[o].mesh))
+      e = launch_raster_point_or_line(scene->frame, scene->objects[o], keys, count, st);
     else
       e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
   }

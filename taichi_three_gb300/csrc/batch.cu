@@ -259,7 +259,7 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
     if (r) return r;
     if (ds.lighting.mode != T3_LIGHT_LAMPS) return T3_EUNSUPPORTED;
     for (int o = 0; o < scenes[s].nobjects; o++)
-      if (scenes[s].objects[o].mesh.kind == T3_MESH_PARTICLES) return T3_EUNSUPPORTED;
+      if (is_point_or_line(scenes[s].objects[o].mesh)) return T3_EUNSUPPORTED;
     if (!outs[s].rgb) return T3_EINVAL;
     nl = max_lobes(ds) > nl ? max_lobes(ds) : nl;
     DevScene* dst = reinterpret_cast<DevScene*>(ws + L.scenes + align256b(sizeof(DevScene)) * (size_t)s);

@@ -81,8 +81,8 @@ extern "C" int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t
     big.count = counters + o;
     big.status = status;
     big.rec = nullptr;
-    if (scene->objects[o].mesh.kind == T3_MESH_PARTICLES)
-      e = launch_raster_particles(scene->frame, scene->objects[o], keys, nullptr, st);
+    if (is_point_or_line(scene->objects[o].mesh))
+      e = launch_raster_point_or_line(scene->frame, scene->objects[o], keys, nullptr, st);
     else
       e = launch_raster_direct(scene->frame, scene->objects[o], keys, big, 4096, st);
   }

@@ -239,6 +239,91 @@ cudaError_t launch_raster_particles(const t3_frame& fr, const t3_object& ob, uns
   return cudaGetLastError();
 }
 
+// ---- wireframe (WireframeRaster.render_color, tina/core/wireframe.py:69-97) ----
+// One thread per line runs the setup and finds, by bisection, the steps whose
+// pixel lies inside the frame; the warp then walks the 32 lines' steps
+// cooperatively.  Every step is the reference's DDA step with its own depth
+// interpolation, folded into the packed key like a triangle fragment (the
+// shading pass writes the raster's line colour where a line wins).
+struct WarpWires {
+  float4 rec[32][2];  // (ax, ay, kx, ky) (az, bz, wsa, wsb)
+  int4 meta[32];      // (siz, lo, id, -)
+  long long start[32];
+};
+
+template <int BLOCK, bool COUNT>
+__global__ void __launch_bounds__(BLOCK)
+k_raster_wires(const t3_frame fr, const t3_mesh mesh, int64_t nwires, uint32_t face_base,
+               unsigned long long* __restrict__ keys, unsigned long long* fragments) {
+  __shared__ WarpWires wws[BLOCK / 32];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  WarpWires& ww = wws[threadIdx.x >> 5];
+  GlobalKeySink<COUNT> sink{keys, fr.height, fragments};
+  const int64_t n = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  WireSetup s{};
+  bool live = false;
+  if (n < nwires) {
+    f3 A, B;
+    wire_endpoints(mesh, n, A, B);
+    live = wire_setup(fr, A, B, s);
+  }
+  const long long cnt = live ? (long long)s.hi - s.lo + 1 : 0;
+  const unsigned lm = __ballot_sync(FULL, cnt > 0);
+  if (!lm) return;
+  long long incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const long long first = incl - cnt;
+  if (cnt > 0) {
+    const int r = __popc(lm & ((1u << lane) - 1u));
+    ww.rec[r][0] = make_float4(s.ax, s.ay, s.kx, s.ky);
+    ww.rec[r][1] = make_float4(s.az, s.bz, s.wsa, s.wsb);
+    ww.meta[r] = make_int4(s.siz, s.lo, (int)(face_base + (uint32_t)n), 0);
+    ww.start[r] = first;
+  }
+  const long long total = __shfl_sync(FULL, incl, 31);
+  const unsigned upto = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+  __syncwarp();
+  int before = 0;
+  for (long long base = 0; base < total; base += 32) {
+    const unsigned bit = (cnt > 0 && first >= base && first < base + 32) ? 1u << (int)(first - base) : 0u;
+    const unsigned starts = __reduce_or_sync(FULL, bit);
+    const long long idx = base + lane;
+    if (idx < total) {
+      const int j = before + __popc(starts & upto) - 1;
+      const float4 a = ww.rec[j][0], b = ww.rec[j][1];
+      const int4 m = ww.meta[j];
+      WireSetup t;
+      t.ax = a.x; t.ay = a.y; t.kx = a.z; t.ky = a.w;
+      t.az = b.x; t.bz = b.y; t.wsa = b.z; t.wsb = b.w;
+      t.siz = m.x;
+      const int32_t i = m.y + (int32_t)(idx - ww.start[j]);
+      int x, y;
+      int32_t depth;
+      if (wire_step(fr, t, i, x, y, depth)) sink(x, y, pack_key(depth, (uint32_t)m.z));
+    }
+    before += __popc(starts);
+  }
+}
+
+cudaError_t launch_raster_wires(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
+                                unsigned long long* fragments, cudaStream_t st) {
+  if (ob.nfaces <= 0) return cudaSuccess;
+  constexpr int BLOCK = 128;
+  const unsigned grid = (unsigned)((ob.nfaces + BLOCK - 1) / BLOCK);
+  if (fragments)
+    k_raster_wires<BLOCK, true><<<grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces, (uint32_t)ob.face_base,
+                                                        keys, fragments);
+  else
+    k_raster_wires<BLOCK, false><<<grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces, (uint32_t)ob.face_base,
+                                                         keys, nullptr);
+  return cudaGetLastError();
+}
+
 // u64 atomicMin throughput: n distinct addresses (L2 resident for n * 8 below
 // the L2 size), `rounds` reductions each, with decreasing values so every
 // reduction changes memory like a winning fragment does

@@ -133,7 +133,10 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
       pix = list[G.row];
       const int x = (int)(pix / H), y = (int)(pix - (int64_t)x * H);
       PixelGeom pg;
-      if (pixel_geometry(sc, rec, keys[pix], x, y, out, pg)) {
+      const bool hit = pixel_geometry(sc, rec, keys[pix], x, y, out, pg);
+      if (hit && pg.flat) {
+        store_rgb(fr, out, pix, pg.fg.color);  // a line pixel
+      } else if (hit) {
         mine = true;
         eval_mlp_coeffs<NL>(pg.ob->mat, pg.fg, q);
         if (lt.nlights > 0) {

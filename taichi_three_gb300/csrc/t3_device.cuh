@@ -374,4 +374,127 @@ __device__ __forceinline__ bool particle_covers(const ParSetup& p, f3 Pl) {
   return !(xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz)) > p.r2);
 }
 
+// ---- wireframe (WireframeRaster, tina/core/wireframe.py) ----------------------
+__device__ __forceinline__ bool is_wire(const t3_mesh& d) {
+  return d.kind == T3_MESH_LINES || (d.flags & T3_MESH_WIREFRAME) != 0;
+}
+
+// world endpoints of line n of a wire object: SimpleMesh(npolygon=2) lines, or
+// MeshToWire's corners (n % p, (n + 1) % p) of face n / p (wire.py:20-27)
+__device__ __forceinline__ void wire_endpoints(const t3_mesh& d, int64_t n, f3& A, f3& B) {
+  if (d.kind == T3_MESH_LINES) {
+    int64_t l = n;
+    bool swap = false;
+    if (d.flags & T3_MESH_WIREFRAME) { l = n >> 1; swap = (n & 1) != 0; }
+    f3 p0 = ld3(d.verts + l * 6), p1 = ld3(d.verts + l * 6 + 3);
+    if (d.flags & T3_MESH_TRANSFORM) { p0 = mapply_pos_x(d.trans, p0); p1 = mapply_pos_x(d.trans, p1); }
+    A = swap ? p1 : p0;
+    B = swap ? p0 : p1;
+    return;
+  }
+  const int64_t f = n / 3;
+  const int e = (int)(n - f * 3);
+  f3 v[3];
+  face_verts(d, face_ref(d, f), v);
+  A = e == 0 ? v[0] : e == 1 ? v[1] : v[2];
+  B = e == 0 ? v[1] : e == 1 ? v[2] : v[0];
+}
+
+struct WireSetup {
+  float ax, ay;    // viewport start a
+  float kx, ky;    // per-step increment k (draw_line)
+  float az, bz;    // NDC depth of the endpoints
+  float wsa, wsb;  // 1 / clip w of the endpoints
+  int32_t siz;     // the line's last step (steps 0..siz)
+  int32_t lo, hi;  // the steps whose pixel lies inside the frame
+};
+
+// the pixel coordinate of step i along one axis (pos = src + k * i + bias)
+__device__ __forceinline__ float wire_coord(float a, float k, float bias, int32_t i) {
+  return xadd(xadd(a, xmul(k, (float)i)), bias);
+}
+
+// first i in [lo, hi + 1) where pred, for a predicate false..false true..true
+template <class Pred>
+__device__ __forceinline__ int32_t wire_first(int32_t lo, int32_t hi, Pred pred) {
+  int64_t a = lo, b = (int64_t)hi + 1;
+  while (a < b) {
+    const int64_t m = a + ((b - a) >> 1);
+    if (pred((int32_t)m)) b = m; else a = m + 1;
+  }
+  return (int32_t)a;
+}
+
+// the steps of [0, siz] whose coordinate lies in [0, res): every operation of
+// wire_coord is monotone in i (k * float(i) for a fixed k, then two roundings
+// of a sum), so the in-range steps form one interval, found by bisection
+__device__ __forceinline__ void wire_axis_range(float a, float k, float bias, int32_t res, int32_t siz,
+                                                int32_t& lo, int32_t& hi) {
+  const float r = (float)res;
+  if (k >= 0.0f) {
+    lo = wire_first(0, siz, [&](int32_t i) { return wire_coord(a, k, bias, i) >= 0.0f; });
+    hi = wire_first(0, siz, [&](int32_t i) { return !(wire_coord(a, k, bias, i) < r); }) - 1;
+  } else {
+    lo = wire_first(0, siz, [&](int32_t i) { return wire_coord(a, k, bias, i) < r; });
+    hi = wire_first(0, siz, [&](int32_t i) { return !(wire_coord(a, k, bias, i) >= 0.0f); }) - 1;
+  }
+}
+
+// WireframeRaster.render_color's per-line part (wireframe.py:72-83, draw_line
+// :49-64); false when clipped or no step lands in the frame
+__device__ __forceinline__ bool wire_setup(const t3_frame& fr, f3 A, f3 B, WireSetup& s) {
+  f3 ra, rb;
+  float wa, wb;
+  mapply_x(fr.W2V, A, 1.0f, ra, wa);
+  mapply_x(fr.W2V, B, 1.0f, rb, wb);
+  const f3 Av = f3{xdiv(ra.x, wa), xdiv(ra.y, wa), xdiv(ra.z, wa)};
+  const f3 Bv = f3{xdiv(rb.x, wb), xdiv(rb.y, wb), xdiv(rb.z, wb)};
+  if ((fr.flags & T3_WIRE_CLIPPING) && !inside_clip(Av) && !inside_clip(Bv)) return false;
+  auto vp = [](float c, float res) { return xmul(xadd(xmul(c, 0.5f), 0.5f), res); };
+  s.ax = vp(Av.x, (float)fr.width);
+  s.ay = vp(Av.y, (float)fr.height);
+  const float bx = vp(Bv.x, (float)fr.width), by = vp(Bv.y, (float)fr.height);
+  s.az = Av.z;
+  s.bz = Bv.z;
+  s.wsa = xdiv(1.0f, wa);
+  s.wsb = xdiv(1.0f, wb);
+  const float dx = xsub(bx, s.ax), dy = xsub(by, s.ay);
+  const float adx = fabsf(dx), ady = fabsf(dy);
+  if (adx >= ady) {
+    s.kx = dx >= 0.0f ? 1.0f : -1.0f;
+    s.ky = xdiv(xmul(s.kx, dy), dx);
+    s.siz = trunc_i32(adx);
+  } else {
+    s.ky = dy >= 0.0f ? 1.0f : -1.0f;
+    s.kx = xdiv(xmul(s.ky, dx), dy);
+    s.siz = trunc_i32(ady);
+  }
+  // range(siz + 1) in int32: empty for siz < 0 and for siz = INT32_MAX (overflow)
+  if (s.siz < 0 || s.siz == INT32_MAX) return false;
+  int32_t lx, hx, ly, hy;
+  wire_axis_range(s.ax, s.kx, fr.bias[0], fr.width, s.siz, lx, hx);
+  wire_axis_range(s.ay, s.ky, fr.bias[1], fr.height, s.siz, ly, hy);
+  s.lo = lx > ly ? lx : ly;
+  s.hi = hx < hy ? hx : hy;
+  return s.lo <= s.hi;
+}
+
+// step i of the line (wireframe.py:84-92): its pixel and int depth; false when
+// the pixel is outside the frame or the depth cannot pass the depth test
+__device__ __forceinline__ bool wire_step(const t3_frame& fr, const WireSetup& s, int32_t i, int& x, int& y,
+                                          int32_t& depth) {
+  const float fi = (float)i;
+  x = trunc_i32(floorf(xadd(xadd(s.ax, xmul(s.kx, fi)), fr.bias[0])));
+  y = trunc_i32(floorf(xadd(xadd(s.ay, xmul(s.ky, fi)), fr.bias[1])));
+  if (!(0 <= x && x < fr.width && 0 <= y && y < fr.height)) return false;
+  const float cor = xdiv(fi, (float)s.siz);
+  float w0 = xmul(xsub(1.0f, cor), s.wsa), w1 = xmul(cor, s.wsb);
+  const float sum = xadd(w0, w1);
+  w0 = xdiv(w0, sum);
+  w1 = xdiv(w1, sum);
+  const float df = xadd(xmul(w0, s.az), xmul(w1, s.bz));
+  depth = trunc_i32(xmul(df, (float)fr.maxdepth));
+  return depth < fr.maxdepth;
+}
+
 } // namespace t3

@@ -3,6 +3,8 @@
 // the workspace layout, status bits and the launchers.
 #pragma once
 
+#include <cstddef>
+
 #include "t3_device.cuh"
 
 namespace t3 {
@@ -78,6 +80,10 @@ struct DevScene {
   int32_t _pad;
   DevObject obj[T3_MAX_OBJECTS];
 };
+// the shading kernels read each lamp as two float4 loads
+static_assert((offsetof(DevScene, lighting) + offsetof(t3_lighting, lights)) % 16 == 0,
+              "lamps must be 16-byte aligned inside DevScene");
+static_assert(sizeof(t3_light) % 16 == 0, "t3_light must be a multiple of 16 bytes");
 
 
 int flatten_material(const t3_material& in, DevMaterial& out);
@@ -85,6 +91,17 @@ int make_dev_scene(const t3_scene& sc, DevScene& out);
 
 cudaError_t launch_raster_particles(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                     unsigned long long* fragments, cudaStream_t st);
+cudaError_t launch_raster_wires(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
+                                unsigned long long* fragments, cudaStream_t st);
+// objects of the particle and wireframe rasterisers (direct path only)
+inline bool is_point_or_line(const t3_mesh& m) {
+  return m.kind == T3_MESH_PARTICLES || m.kind == T3_MESH_LINES || (m.flags & T3_MESH_WIREFRAME) != 0;
+}
+inline cudaError_t launch_raster_point_or_line(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
+                                               unsigned long long* fragments, cudaStream_t st) {
+  return ob.mesh.kind == T3_MESH_PARTICLES ? launch_raster_particles(fr, ob, keys, fragments, st)
+                                           : launch_raster_wires(fr, ob, keys, fragments, st);
+}
 cudaError_t launch_vertex_ndc(const t3_frame& fr, const t3_mesh& mesh, int64_t nverts, float4* out,
                               cudaStream_t st);
 int64_t mesh_vertex_rows(const t3_mesh& m);  // rows the vertex stage transforms (0: none)

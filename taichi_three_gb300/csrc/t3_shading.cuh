@@ -255,6 +255,7 @@ __device__ __forceinline__ V3 view_ray(const t3_frame& fr, float px, float py) {
 // Everything shading needs about one covered pixel.
 struct PixelGeom {
   int64_t i;          // pixel index x*H + y
+  bool flat;          // a line pixel: fg.color is its final colour, nothing to shade
   const DevObject* ob;
   Frag fg;
   V3 vdir;            // calc_viewdir
@@ -276,6 +277,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   const int H = fr.height;
   const int64_t i = (int64_t)x * H + y;
   g.i = i;
+  g.flat = false;
   // the object owning this face id (-1: empty pixel, or an id no object owns)
   int o = -1;
   if (key != T3_EMPTY_KEY) {
@@ -296,6 +298,17 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   g.ob = &ob;
   const t3_mesh& mesh = ob.mesh;
   const int64_t n = (int64_t)gid - ob.face_base;
+  if (is_wire(mesh)) {
+    // WireframeRaster: the raster's line colour, blended with factor 1 by
+    // Shader.blend_color (wireframe.py:93-97, shader.py:133-135)
+    const int32_t d = (int32_t)((uint32_t)(key >> 32) ^ 0x80000000u);
+    if (out.face_id) out.face_id[i] = (int32_t)gid;
+    if (out.depth) out.depth[i] = d;
+    if (out.depth_f) out.depth_f[i] = xdiv((float)d, (float)fr.maxdepth);
+    g.flat = true;
+    g.fg.color = v3(fr.linecolor[0], fr.linecolor[1], fr.linecolor[2]);
+    return true;
+  }
   if (mesh.kind == T3_MESH_PARTICLES) {
     // ParticleRaster.render_color (particle.py:116-146)
     const f3 A = ld3(mesh.verts + n * 3);
@@ -433,6 +446,10 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
       bg = env_sample(env, view_ray(fr, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1])));
     }
     store_rgb(fr, out, (int64_t)x * fr.height + y, bg);
+    return;
+  }
+  if (g.flat) {
+    store_rgb(fr, out, g.i, g.fg.color);
     return;
   }
   V3 color;

@@ -60,19 +60,23 @@ class MeshBase:
 
 
 class SimpleMesh(MeshBase):
-    """A face soup (tina/mesh/simple.py): verts [n, 3, 3], norms [n, 3, 3],
-    coors [n, 3, 2]; nfaces = min(n, maxfaces)."""
+    """A face soup (tina/mesh/simple.py): verts [n, p, 3], norms [n, p, 3],
+    coors [n, p, 2] with p = npolygon, 3 (triangles) or 2 (lines, drawn by the
+    wireframe rasteriser); nfaces = min(n, maxfaces)."""
 
     def __init__(self, maxfaces=MAX, npolygon=3):
-        if npolygon != 3:
-            raise NotImplementedError('only triangle meshes (npolygon=3) are rasterised by this build')
+        if npolygon not in (2, 3):
+            raise NotImplementedError('SimpleMesh takes npolygon=3 (triangles) or 2 (lines) in this build')
         self.maxfaces = maxfaces
         self.npolygon = npolygon
         self.nfaces = 0
         dev = default_device()
-        self.verts = torch.zeros((0, 3, 3), dtype=torch.float32, device=dev)
+        self.verts = torch.zeros((0, npolygon, 3), dtype=torch.float32, device=dev)
         self.norms = None
         self.coors = None
+
+    def get_npolygon(self):
+        return self.npolygon
 
     def get_nfaces(self):
         return min(self.nfaces, self.maxfaces)
@@ -81,9 +85,10 @@ class SimpleMesh(MeshBase):
         if _copy_in_place(self.verts, verts, self.maxfaces):
             self.nfaces = self.verts.shape[0]
             return
+        p = self.npolygon
         v = as_f32(verts)
-        if v.dim() != 3 or v.shape[1] != 3 or v.shape[2] != 3:
-            raise ValueError('verts must have shape [nfaces, 3, 3]')
+        if v.dim() != 3 or v.shape[1] != p or v.shape[2] != 3:
+            raise ValueError(f'verts must have shape [nfaces, {p}, 3]')
         self.nfaces = min(v.shape[0], self.maxfaces)
         self.verts = v[:self.nfaces].contiguous()
 
@@ -91,22 +96,24 @@ class SimpleMesh(MeshBase):
         if self.norms is not None and self.norms.shape[0] == self.nfaces and \
                 _copy_in_place(self.norms, norms, self.nfaces):
             return
+        p = self.npolygon
         n = as_f32(norms)
-        if n.dim() != 3 or n.shape[0] < self.nfaces or n.shape[1:] != (3, 3):
-            raise ValueError('norms must have shape [>= nfaces, 3, 3]')
+        if n.dim() != 3 or n.shape[0] < self.nfaces or n.shape[1:] != (p, 3):
+            raise ValueError(f'norms must have shape [>= nfaces, {p}, 3]')
         self.norms = n[:self.nfaces].contiguous()
 
     def set_face_coors(self, coors):
         if self.coors is not None and self.coors.shape[0] == self.nfaces and \
                 _copy_in_place(self.coors, coors, self.nfaces):
             return
+        p = self.npolygon
         c = as_f32(coors)
-        if c.dim() != 3 or c.shape[0] < self.nfaces or c.shape[1] != 3 or c.shape[2] < 2:
-            raise ValueError('coors must have shape [>= nfaces, 3, 2]')
+        if c.dim() != 3 or c.shape[0] < self.nfaces or c.shape[1] != p or c.shape[2] < 2:
+            raise ValueError(f'coors must have shape [>= nfaces, {p}, 2]')
         self.coors = c[:self.nfaces, :, :2].contiguous()
 
     def _t3_fill(self, m, device, keep):
-        m.kind = N.T3_MESH_SOUP
+        m.kind = N.T3_MESH_SOUP if self.npolygon == 3 else N.T3_MESH_LINES
         m.nfaces = self.get_nfaces()
         m.verts = ptr(self.verts, device, keep)
         m.norms = ptr(self.norms, device, keep)
@@ -391,7 +398,8 @@ class MeshTransform(MeshEditBase):
 
     def _t3_fill(self, m, device, keep):
         self.mesh._t3_fill(m, device, keep)
-        self._check_inner(m, 0xFF)
+        # a transform commutes with MeshToWire (both act per vertex)
+        self._check_inner(m, 0xFF & ~N.T3_MESH_WIREFRAME)
         m.flags |= N.T3_MESH_TRANSFORM
         t = self.trans.reshape(-1)
         tn = self.trans_normal.reshape(-1)
@@ -407,7 +415,7 @@ class MeshFlatNormal(MeshEditBase):
     def _t3_fill(self, m, device, keep):
         self.mesh._t3_fill(m, device, keep)
         self._check_inner(m, N.T3_MESH_FLAT_NORMAL | N.T3_MESH_FLIP_ORDER | N.T3_MESH_FLIP_NORMAL
-                          | N.T3_MESH_NOCULL)
+                          | N.T3_MESH_NOCULL | N.T3_MESH_WIREFRAME)
         m.flags |= N.T3_MESH_FLAT_NORMAL
 
 
@@ -416,7 +424,7 @@ class MeshFlipCulling(MeshEditBase):
 
     def _t3_fill(self, m, device, keep):
         self.mesh._t3_fill(m, device, keep)
-        self._check_inner(m, N.T3_MESH_FLIP_NORMAL | N.T3_MESH_NOCULL)
+        self._check_inner(m, N.T3_MESH_FLIP_NORMAL | N.T3_MESH_NOCULL | N.T3_MESH_WIREFRAME)
         m.flags ^= N.T3_MESH_FLIP_ORDER
 
 
@@ -425,7 +433,7 @@ class MeshFlipNormal(MeshEditBase):
 
     def _t3_fill(self, m, device, keep):
         self.mesh._t3_fill(m, device, keep)
-        self._check_inner(m, N.T3_MESH_NOCULL)
+        self._check_inner(m, N.T3_MESH_NOCULL | N.T3_MESH_WIREFRAME)
         m.flags ^= N.T3_MESH_FLIP_NORMAL
 
 
@@ -438,8 +446,30 @@ class MeshNoCulling(MeshEditBase):
 
     def _t3_fill(self, m, device, keep):
         self.mesh._t3_fill(m, device, keep)
-        self._check_inner(m, N.T3_MESH_NOCULL)
+        self._check_inner(m, N.T3_MESH_NOCULL | N.T3_MESH_WIREFRAME)
         m.flags |= N.T3_MESH_NOCULL
+
+
+class MeshToWire(MeshEditBase):
+    """The polygon edges of a mesh as lines for the wireframe rasteriser
+    (tina/mesh/wire.py:5-40): line n joins corners n % p and (n + 1) % p of
+    face n // p, p the wrapped mesh's npolygon; applies outside every other
+    edit except MeshTransform."""
+
+    def __init__(self, mesh):
+        super().__init__(mesh)
+        self.src_npolygon = mesh.get_npolygon() if hasattr(mesh, 'get_npolygon') else 3
+
+    def get_npolygon(self):
+        return 2
+
+    def get_nfaces(self):
+        return self.mesh.get_nfaces() * self.src_npolygon
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        self._check_inner(m, N.T3_MESH_WIREFRAME)
+        m.flags |= N.T3_MESH_WIREFRAME
 
 
 class SimpleParticles:

@@ -8,6 +8,7 @@ float32 tensor of shape (W, H, 3) indexed [x, y] like Tina's Taichi field.
 """
 import ctypes as C
 
+import numpy as np
 import torch
 
 from . import _native as N
@@ -126,6 +127,36 @@ class ParticleRaster:
         return n
 
 
+class WireframeRaster:
+    """WireframeRaster (tina/core/wireframe.py): each line is walked one pixel
+    per step along its major axis (draw_line), with the depth interpolated
+    perspective-correctly between the endpoints, through the same depth buffer
+    as the triangles; a pixel a line wins takes the raster's line colour.
+    Options kept: maxwires, linewidth (stored: the reference draws one-pixel
+    lines whatever its value), linecolor, clipping (default False: a line is
+    dropped only when both endpoints leave the clip cube)."""
+
+    def __init__(self, engine, maxwires=None, linewidth=1.5, linecolor=(.9, .6, 0), clipping=False,
+                 **extra_options):
+        self.engine = engine
+        self.maxwires = maxwires
+        self.linewidth = linewidth
+        self.linecolor = tuple(float(c) for c in np.broadcast_to(np.asarray(linecolor, np.float32), (3,)))
+        self.clipping = clipping
+
+    def check_faces(self, mesh):
+        n = mesh.get_nfaces()
+        if self.maxwires is not None and n > self.maxwires:
+            raise ValueError(f'{n} lines, more than maxwires={self.maxwires}')
+        return n
+
+    def _t3_fill(self, fr):
+        for k in range(3):
+            fr.linecolor[k] = self.linecolor[k]
+        if self.clipping:
+            fr.flags |= N.T3_WIRE_CLIPPING
+
+
 class Shader:
     """Shader(img, lighting, material) (tina/core/shader.py:112-135): shades the
     winning fragments of one raster into `img`."""
@@ -234,10 +265,16 @@ class Scene:
         if raster is None:
             if hasattr(object, 'get_nfaces'):
                 if hasattr(object, 'get_npolygon') and object.get_npolygon() == 2:
-                    raise NotImplementedError('wireframe rasterisation is not part of this build')
-                if self.triangle_raster is None:
-                    self.triangle_raster = TriangleRaster(self.engine, **self.raster_options)
-                raster = self.triangle_raster
+                    if getattr(self, 'wireframe_raster', None) is None:
+                        self.wireframe_raster = WireframeRaster(
+                            self.engine, **{k: self.options[k] for k in
+                                            ('maxwires', 'linewidth', 'linecolor', 'clipping')
+                                            if k in self.options})
+                    raster = self.wireframe_raster
+                else:
+                    if self.triangle_raster is None:
+                        self.triangle_raster = TriangleRaster(self.engine, **self.raster_options)
+                    raster = self.triangle_raster
             elif hasattr(object, 'get_npars'):
                 if getattr(self, 'particle_raster', None) is None:
                     self.particle_raster = ParticleRaster(
@@ -269,6 +306,8 @@ class Scene:
         # the tonemap is fused into shading unless blooming needs the HDR image
         self.engine._t3_fill_frame(sc.frame, raster.flags(self.tonemap and self.blooming is None),
                                    self.bgcolor)
+        if getattr(self, 'wireframe_raster', None) is not None:
+            self.wireframe_raster._t3_fill(sc.frame)
         self.lighting._t3_fill(sc.lighting)
         if hasattr(self.lighting, '_t3_fill_device'):
             self.lighting._t3_fill_device(sc.lighting, device, keep)

@@ -52,11 +52,30 @@ def inputs(name):
             verts, norms = _soup(80, 13, sigma=0.35)
             out.update(verts=verts, norms=norms)
         return out
+    if name == 'wire_soup':
+        verts, norms = _soup(40, 21, sigma=0.3)
+        return {'verts': verts, 'norms': norms}
+    if name == 'lines':
+        rng = np.random.Generator(np.random.PCG64(22))
+        ends = rng.uniform(-1.3, 1.3, size=(70, 2, 3)).astype(np.float32)
+        ends[:, :, 2] *= 0.5
+        ends[0] = [[-0.5, 0.2, 0.1], [-0.5, 0.2, 0.1]]          # zero length: no step in the frame
+        ends[1] = [[0.1, 0.1, 0.0], [0.12, 0.105, 0.0]]         # under a pixel: one step, 0/0 weight
+        ends[2] = [[-0.9, -0.4, 0.2], [0.9, -0.4, 0.2]]         # horizontal
+        ends[3] = [[0.3, -0.95, -0.1], [0.3, 0.95, 0.3]]        # vertical
+        ends[4] = [[-4.0, -3.0, 0.0], [4.0, 2.5, 0.0]]          # both ends far outside the frame
+        return {'verts': ends}
+    if name == 'wire_grid':
+        n = 7
+        u = np.linspace(0, 1, n)
+        x, y = np.meshgrid(u * 2 - 1, u * 2 - 1, indexing='ij')
+        pos = np.stack([x, y, 0.2 * np.cos(2 * x) * np.sin(3 * y + 0.3)], -1).astype(np.float32)
+        return {'pos': pos}
     raise KeyError(name)
 
 
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
-         'two_objects', 'particles', 'pars_mixed']
+         'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid']
 
 
 def build(tina, name, arrays, matrix):
@@ -151,6 +170,36 @@ def build(tina, name, arrays, matrix):
         pars.set_particle_colors(arrays['colors'])
         scene.add_object(pars, tina.Classic())
         scene.engine.set_camera(matrix.lookat(back=(-0.3, 0.2, 3)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'wire_soup':
+        # a mesh's wireframe drawn over the mesh (the reference's wireframe example)
+        scene = tina.Scene(48, 36, smoothing=True)
+        mesh = tina.SimpleMesh()
+        mesh.set_face_verts(arrays['verts'])
+        mesh.set_face_norms(arrays['norms'])
+        scene.add_object(tina.MeshToWire(mesh))
+        inner = tina.MeshTransform(mesh)
+        inner.set_transform(matrix.scale([0.9, 0.9, 0.9]))
+        scene.add_object(inner, tina.Diffuse(color=[0.4, 0.6, 0.9]))
+        scene.engine.set_camera(matrix.lookat(back=(0.2, 0.1, 3)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'lines':
+        scene = tina.Scene(40, 30, tonemap=False, bgcolor=0.05, clipping=True,
+                           linecolor=(0.2, 0.9, 0.5))
+        lines = tina.SimpleMesh(npolygon=2)
+        lines.set_face_verts(arrays['verts'])
+        scene.add_object(lines)
+        scene.engine.set_camera(matrix.lookat(back=(0, 0, 3)), matrix.perspective(60, 40 / 30))
+        return scene, False
+    if name == 'wire_grid':
+        scene = tina.Scene(48, 36, smoothing=True)
+        grid = tina.MeshGrid(7)
+        _set_grid(grid, arrays['pos'])
+        # the wireframe first: where a line and the surface tie in depth the
+        # earlier object keeps the pixel
+        scene.add_object(tina.MeshToWire(grid))
+        scene.add_object(grid, tina.PBR(metallic=0.3, roughness=0.4))
+        scene.engine.set_camera(matrix.lookat(back=(0.3, -1.2, 2.2)), matrix.perspective(60, 48 / 36))
         return scene, False
     raise KeyError(name)
 

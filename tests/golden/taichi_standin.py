@@ -485,8 +485,18 @@ def _truediv(a, b):
         with np.errstate(all='ignore'):
             return np.float32(np.float32(a) / np.float32(b))
     if isinstance(a, int) and isinstance(b, int) and not isinstance(a, bool):
-        return np.float32(a / b) if b != 0 else np.float32(np.inf)
+        # int / int in a kernel: both operands become float32, then an IEEE
+        # float32 division (0 / 0 is NaN, x / 0 an infinity)
+        with np.errstate(all='ignore'):
+            return np.float32(np.float32(a) / np.float32(b))
     return a / b
+
+
+def _ti_div(a, b):
+    """`a / b` inside kernels and funcs (Taichi's truediv)."""
+    if isinstance(a, Matrix) or isinstance(b, Matrix):
+        return Matrix._elementwise(_truediv, a, b)
+    return _truediv(a, b)
 
 
 def _floordiv(a, b):
@@ -679,6 +689,9 @@ class _Rewrite(ast.NodeTransformer):
         if isinstance(node.op, ast.Pow):
             return ast.Call(func=ast.Name(id='_ti_pow', ctx=ast.Load()), args=[node.left, node.right],
                             keywords=[])
+        if isinstance(node.op, ast.Div):
+            return ast.Call(func=ast.Name(id='_ti_div', ctx=ast.Load()), args=[node.left, node.right],
+                            keywords=[])
         return node
 
     def visit_AugAssign(self, node):
@@ -706,7 +719,7 @@ class _Env(dict):
 
 
 _HELPERS = {'_ti_int': _ti_int, '_ti_float': _ti_float, '_ti_min': _ti_min, '_ti_max': _ti_max,
-            '_ti_pow': _ti_pow}
+            '_ti_pow': _ti_pow, '_ti_div': _ti_div}
 
 
 def _recompile(fn):

@@ -32,6 +32,9 @@ def test_struct_layouts_match():
     N.check_layout(lib)
     n = lib.t3_struct_sizes(None, 0)
     assert n == len(N.STRUCTS)
+    # lamps are read as float4 pairs: 16-byte aligned inside the scene
+    assert (N.t3_scene.lighting.offset + N.t3_lighting.lights.offset) % 16 == 0
+    assert C.sizeof(N.t3_light) % 16 == 0
 
 
 def test_null_arguments_are_rejected_without_touching_the_device():

@@ -1,0 +1,164 @@
+"""Wireframes (WireframeRaster, tina/core/wireframe.py; MeshToWire,
+tina/mesh/wire.py; SimpleMesh(npolygon=2)): one-pixel DDA lines in the shared
+depth buffer, against the oracle -- line id, int32 depth and float depth
+bit-exact, RGB within 1e-4 (line pixels carry the raster's line colour)."""
+import numpy as np
+import pytest
+import torch
+
+import taichi_three_gb300 as tina
+from taichi_three_gb300 import _native as N
+
+
+def _lines(n, seed, spread=1.2, zscale=0.5):
+    rng = np.random.default_rng(seed)
+    ends = rng.uniform(-spread, spread, (n, 2, 3)).astype(np.float32)
+    ends[:, :, 2] *= zscale
+    return ends
+
+
+def test_describe_wires():
+    verts, _, _ = tina.workloads.soup_arrays(50, 0)
+    mesh = tina.SimpleMesh()
+    mesh.set_face_verts(verts)
+    wire = tina.MeshToWire(mesh)
+    assert wire.get_npolygon() == 2 and wire.get_nfaces() == 150
+    lines = tina.SimpleMesh(npolygon=2)
+    lines.set_face_verts(_lines(20, 1))
+    assert lines.get_npolygon() == 2 and lines.get_nfaces() == 20
+    with pytest.raises(ValueError):
+        lines.set_face_verts(np.zeros((3, 3, 3), np.float32))
+    scene = tina.Scene(32, linecolor=(0.1, 0.2, 0.3), clipping=True)
+    scene.add_object(mesh)
+    scene.add_object(wire)
+    scene.add_object(tina.MeshTransform(lines, tina.translate([0, 0, 0.1])))
+    assert isinstance(scene.objects[wire].raster, tina.WireframeRaster)
+    assert isinstance(scene.objects[mesh].raster, tina.TriangleRaster)
+    sc, keep = scene.describe('cpu')
+    assert sc.frame.flags & N.T3_WIRE_CLIPPING
+    assert [round(c, 6) for c in sc.frame.linecolor] == [0.1, 0.2, 0.3]
+    assert sc.objects[1].mesh.flags & N.T3_MESH_WIREFRAME and sc.objects[1].nfaces == 150
+    assert sc.objects[2].mesh.kind == N.T3_MESH_LINES and sc.objects[2].nfaces == 20
+    assert sc.objects[2].mesh.flags == N.T3_MESH_TRANSFORM
+    assert (sc.objects[1].face_base, sc.objects[2].face_base) == (50, 200)
+    # an edge order flip around the wireframe is not a wireframe of the flipped mesh
+    with pytest.raises(NotImplementedError):
+        tina.MeshNoCulling(tina.MeshToWire(mesh))._t3_fill(N.t3_mesh(), 'cpu', [])
+
+
+def test_default_wire_options():
+    scene = tina.Scene(16)
+    lines = tina.SimpleMesh(npolygon=2)
+    lines.set_face_verts(_lines(4, 2))
+    scene.add_object(lines)
+    sc, _ = scene.describe('cpu')
+    assert not (sc.frame.flags & N.T3_WIRE_CLIPPING)          # WireframeRaster(clipping=False)
+    assert sc.frame.flags & N.T3_CLIPPING                      # TriangleRaster(clipping=True)
+    assert np.allclose(list(sc.frame.linecolor), [0.9, 0.6, 0.0])
+
+
+def _render_both(scene, oracle_mod, mode=0):
+    scene.render()
+    torch.cuda.synchronize()
+    o = oracle_mod.render(scene, mode=mode)
+    fid = scene.face_id.cpu().numpy()
+    assert np.array_equal(fid, o['face_id'])
+    assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
+    assert np.array_equal(scene.depth_f.cpu().numpy().view(np.uint32), o['depth_f'].view(np.uint32))
+    g = scene.img.cpu().numpy()
+    ok = np.isfinite(o['rgb'])
+    assert np.array_equal(np.isfinite(g), ok)
+    assert np.abs(g[ok] - o['rgb'][ok]).max() <= 1e-4
+    return fid
+
+
+@pytest.mark.gpu
+def test_wireframe_over_soup(cuda, oracle_mod):
+    arrays = tina.workloads.soup_arrays(4000, 5, median_sigma=0.06, log_sd=0.6)
+    scene, mesh = tina.workloads.soup_scene(ntri=4000, res=(200, 150), seed=5, nlights=2, arrays=arrays)
+    wire = tina.MeshToWire(mesh)
+    scene.add_object(wire)
+    fid = _render_both(scene, oracle_mod)
+    assert (fid >= 4000).sum() > 2000 and ((fid >= 0) & (fid < 4000)).sum() > 2000
+
+
+@pytest.mark.gpu
+def test_lines_clipping_and_far_endpoints(cuda, oracle_mod):
+    ends = _lines(600, 6, spread=3.0, zscale=1.5)
+    ends[:20, 1] = ends[:20, 0]                         # zero-length lines
+    ends[20:40, 1] = ends[20:40, 0] + 1e-3              # under a pixel: one step with 0/0 weights
+    ends[40:60, :, 0] *= 40.0                           # far outside the frame on both sides
+    lines = tina.SimpleMesh(npolygon=2)
+    lines.set_face_verts(ends)
+    for clipping in (False, True):
+        scene = tina.Scene(180, 130, clipping=clipping, linecolor=(0.3, 1.0, 0.2), bgcolor=0.1)
+        scene.add_object(lines)
+        scene.engine.set_camera(tina.lookat(back=(0.2, 0.1, 3)), tina.perspective(60, 180 / 130))
+        fid = _render_both(scene, oracle_mod)
+        assert (fid >= 0).sum() > 3000
+
+
+@pytest.mark.gpu
+def test_wire_of_edited_and_indexed_meshes(cuda, oracle_mod):
+    # MeshToWire over MeshNoCulling (doubled faces, odd copies reversed), over
+    # an indexed mesh, over a grid, and a transform outside a line soup
+    verts, _, _ = tina.workloads.soup_arrays(300, 7, median_sigma=0.1)
+    soup = tina.SimpleMesh()
+    soup.set_face_verts(verts)
+    sphere = tina.PrimitiveMesh.sphere(lons=16, lats=10)
+    v = sphere.verts.cpu().numpy().reshape(-1, 3)
+    uniq, inv = np.unique(v.round(6), axis=0, return_inverse=True)
+    conn = tina.ConnectiveMesh()
+    conn.set_vertices(uniq.astype(np.float32))
+    conn.set_faces(inv.reshape(-1, 3).astype(np.int32))
+    grid = tina.MeshGrid(12)
+    lines = tina.SimpleMesh(npolygon=2)
+    lines.set_face_verts(_lines(50, 8))
+    scene = tina.Scene(160, 120, smoothing=False)
+    scene.add_object(tina.MeshToWire(tina.MeshNoCulling(soup)))
+    scene.add_object(tina.MeshToWire(tina.MeshTransform(conn, tina.scale([0.5, 0.5, 0.5]))))
+    scene.add_object(tina.MeshToWire(tina.MeshTransform(grid, tina.translate([0, 0, 0.3]))))
+    scene.add_object(tina.MeshTransform(lines, tina.translate([0.1, 0.0, 0.2])))
+    scene.add_object(tina.MeshToWire(lines))
+    scene.add_object(grid)
+    scene.engine.set_camera(tina.lookat(back=(0.3, 0.4, 2.6)), tina.perspective(60, 160 / 120))
+    fid = _render_both(scene, oracle_mod)
+    sc, _ = scene.describe()
+    bases = [sc.objects[o].face_base for o in range(sc.nobjects)] + [2 ** 31]
+    for o in range(sc.nobjects):
+        assert ((fid >= bases[o]) & (fid < bases[o + 1])).sum() > 20, o
+
+
+@pytest.mark.gpu
+def test_wires_under_ibl(cuda, oracle_mod):
+    # lines under the skybox lighting keep their colour; the sky fills the rest
+    scene, mesh = tina.workloads.ibl_soup_scene(ntri=500, res=(96, 72), seed=9, env_res=32, spp=8,
+                                                arrays=tina.workloads.soup_arrays(500, 9, median_sigma=0.1))
+    scene.add_object(tina.MeshToWire(mesh))
+    _render_both(scene, oracle_mod, mode=1)
+
+
+@pytest.mark.gpu
+def test_wires_large_property(cuda, oracle_mod):
+    # 300k lines at 1920x1080 against the OpenMP oracle: depth and ids bit-exact
+    ends = _lines(300_000, 10, spread=1.5)
+    lines = tina.SimpleMesh(npolygon=2)
+    lines.set_face_verts(ends)
+    scene = tina.Scene(1920, 1080)
+    scene.add_object(lines)
+    scene.engine.set_camera(tina.lookat(back=(0, 0, 3)), tina.perspective(60, 1920 / 1080))
+    scene.render()
+    torch.cuda.synchronize()
+    o = oracle_mod.render(scene, mode=1, want_depth_f=False)
+    assert np.array_equal(scene.face_id.cpu().numpy(), o['face_id'])
+    assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
+
+
+@pytest.mark.gpu
+def test_wires_binned_unsupported(cuda):
+    lines = tina.SimpleMesh(npolygon=2)
+    lines.set_face_verts(_lines(10, 11))
+    scene = tina.Scene(64, raster='binned')
+    scene.add_object(lines)
+    with pytest.raises(RuntimeError):
+        scene.render()
