@@ -281,6 +281,18 @@ int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
  * clamped neighbours, for a [nx, ny, 3] float grid. */
 int t3_grid_normals(const float* pos, float* nrm, int nx, int ny, void* stream);
 
+/* MeshSmoothNormal (tina/mesh/norm.py:17-55) of an indexed mesh (kind
+ * T3_MESH_INDEXED, no edit flags): norms_out[v] = normalized(sum, over the
+ * faces that use vertex v in face order, of normalized(cross(b - a, c - a))),
+ * [nverts, 3] floats, bit-identical to the reference's serial loop; a vertex
+ * no face uses gets NaN (the reference's normalized zero vector).  A mesh
+ * wrapped by MeshSmoothNormal is then described as the indexed mesh with
+ * norms = norms_out and slot_norm = slot_vert.  `workspace` (device, 16-byte
+ * aligned) holds t3_smooth_normals_workspace_size bytes. */
+int t3_smooth_normals_workspace_size(int64_t nfaces, int64_t nverts, size_t* bytes);
+int t3_smooth_normals(const t3_mesh* mesh, int64_t nverts, float* norms_out, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
 /* Height-field animation of a grid's positions [nx, ny, 3] (no reference
  * counterpart; the reference's demos animate grids from Python):
  * pos[i, j].z = amp * sin(fx * x + wx * t) * cos(fy * y + wy * t). */

@@ -30,6 +30,8 @@ def load():
         lib.oracle_aces_f32.restype = C.c_int
         lib.oracle_aces_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         lib.oracle_max_threads.restype = C.c_int
+        lib.oracle_smooth_normals.restype = C.c_int
+        lib.oracle_smooth_normals.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
         lib.oracle_pixels_f64.restype = C.c_int
         lib.oracle_pixels_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_uint32,
                                           C.c_int, C.c_void_p, C.c_void_p]
@@ -111,9 +113,30 @@ def aces(x):
     return y
 
 
+def smooth_normals(mesh_desc, nverts):
+    """MeshSmoothNormal's vertex normals of an indexed t3_mesh (host pointers)."""
+    lib = load()
+    out = np.empty((nverts, 3), np.float32)
+    rc = lib.oracle_smooth_normals(C.addressof(mesh_desc), int(nverts), _p(out))
+    if rc != 0:
+        raise RuntimeError(f'oracle_smooth_normals failed ({rc})')
+    return out
+
+
 def pre_compute_host(obj):
-    """The mesh's pre_compute on the CPU (MeshGrid normals); the device copy of the
-    mesh is left untouched."""
+    """The mesh's pre_compute on the CPU (MeshGrid normals, MeshSmoothNormal
+    vertex normals) for meshes held in host memory; device meshes are left
+    untouched."""
+    node = obj
+    while node is not None:
+        if type(node).__name__ == 'MeshSmoothNormal' and not node.mesh.verts.is_cuda:
+            import torch
+            from taichi_three_gb300 import _native as N
+            m = N.t3_mesh()
+            keep = []
+            node.mesh._t3_fill(m, 'cpu', keep)
+            node.norm = torch.from_numpy(smooth_normals(m, int(node.mesh.verts.shape[0])))
+        node = getattr(node, 'mesh', None)
     base = obj
     while hasattr(base, 'mesh') and not hasattr(base, 'res'):
         base = base.mesh

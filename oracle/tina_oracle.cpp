@@ -1316,6 +1316,30 @@ int oracle_grid_normals(const float* pos, float* nrm, int nx, int ny) {
   return 0;
 }
 
+// MeshSmoothNormal._update_normal (tina/mesh/norm.py:34-46): every face's unit
+// normal added onto its three vertices in face order, then normalised.
+int oracle_smooth_normals(const t3_mesh* m, int64_t nverts, float* out) {
+  std::vector<v3<float>> acc((size_t)nverts, v3<float>{0.0f, 0.0f, 0.0f});
+  for (int64_t n = 0; n < m->nfaces; n++) {
+    int64_t idx[3];
+    v3<float> p[3];
+    for (int k = 0; k < 3; k++) {
+      idx[k] = m->faces[n * m->face_stride + k * m->corner_stride + m->slot_vert];
+      p[k] = ld3<float>(m->verts + idx[k] * 3);
+    }
+    const v3<float> nrm = normalized(cross(sub(p[1], p[0]), sub(p[2], p[0])));
+    for (int k = 0; k < 3; k++)
+      if (idx[k] >= 0 && idx[k] < nverts) acc[(size_t)idx[k]] = add(acc[(size_t)idx[k]], nrm);
+  }
+  for (int64_t v = 0; v < nverts; v++) {
+    const v3<float> r = normalized(acc[(size_t)v]);
+    out[3 * v] = r.x;
+    out[3 * v + 1] = r.y;
+    out[3 * v + 2] = r.z;
+  }
+  return 0;
+}
+
 int oracle_aces_f32(const float* in, float* out, int64_t n) {
   for (int64_t i = 0; i < n; i++) out[i] = aces1<float>(in[i]);
   return 0;

@@ -16,12 +16,13 @@ from .materials import (AddMaterial, Classic, CookTorrance, Diffuse, Emission, F
                         compile_material)
 from .lighting import Lighting
 from .mesh import (MAX, ConnectiveMesh, MeshFlatNormal, MeshFlipCulling, MeshFlipNormal, MeshGrid,
-                   MeshModel, MeshNoCulling, MeshToWire, MeshTransform, PrimitiveMesh, SimpleMesh,
+                   MeshModel, MeshNoCulling, MeshSmoothNormal, MeshToWire, MeshTransform, PrimitiveMesh, SimpleMesh,
                    SimpleParticles)
 from .engine import Engine
 from .scene import ParticleRaster, Scene, Shader, TriangleRaster, WireframeRaster
 from .postp import Accumator, Blooming, FXAA, ToneMapping, aces_tonemap
 from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
+from .pipeline import FramePipeline
 from . import workloads
 from .assimp import readobj
 from .mlp import IBLNet, train_for_skybox

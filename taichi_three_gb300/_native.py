@@ -135,6 +135,8 @@ SIGNATURES = {
                             C.POINTER(t3_outputs), _VP]),
     "t3_read_status": (C.c_int, [_VP, C.POINTER(C.c_int32), _VP]),
     "t3_grid_normals": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
+    "t3_smooth_normals_workspace_size": (C.c_int, [_I64, _I64, C.POINTER(_SZ)]),
+    "t3_smooth_normals": (C.c_int, [C.POINTER(t3_mesh), _I64, _VP, _VP, _SZ, _VP]),
     "t3_tonemap": (C.c_int, [_VP, _I64, _VP]),
     "t3_grid_wave": (C.c_int, [_VP, C.c_int, C.c_int] + [C.c_float] * 6 + [_VP]),
     "t3_bloom_workspace_floats": (C.c_int64, [C.c_int, C.c_int]),

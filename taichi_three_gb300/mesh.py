@@ -450,6 +450,54 @@ class MeshNoCulling(MeshEditBase):
         m.flags |= N.T3_MESH_NOCULL
 
 
+class MeshSmoothNormal(MeshEditBase):
+    """Per-vertex normals of an indexed mesh (tina/mesh/norm.py:17-55): each
+    face's unit normal is summed onto its three vertices in face order, the sums
+    normalised, and every face corner reads its vertex's normal.  cached=True
+    computes them once (at the first render, or by update_normal()),
+    cached=False at every pre_compute.  Wraps a ConnectiveMesh or MeshModel
+    directly; other edits go outside it."""
+
+    def __init__(self, mesh, cached=True):
+        super().__init__(mesh)
+        if not isinstance(mesh, (ConnectiveMesh, MeshModel)):
+            raise NotImplementedError('MeshSmoothNormal wraps a ConnectiveMesh or MeshModel in this build')
+        self.cached = cached
+        self.norm = None
+
+    def pre_compute(self):
+        self.mesh.pre_compute()
+        if not self.cached or self.norm is None:
+            self.update_normal()
+
+    def update_normal(self):
+        """Recomputes the vertex normals from the current vertices (t3_smooth_normals)."""
+        import ctypes as C
+        from ._device import require_cuda
+        require_cuda('MeshSmoothNormal')
+        lib = N.load()
+        dev = default_device()
+        m = N.t3_mesh()
+        keep = []
+        self.mesh._t3_fill(m, dev, keep)
+        nverts = int(self.mesh.verts.shape[0])
+        if self.norm is None or tuple(self.norm.shape) != (nverts, 3) or not self.norm.is_cuda:
+            self.norm = torch.empty((nverts, 3), dtype=torch.float32, device=dev)
+        size = C.c_size_t()
+        N.check(lib.t3_smooth_normals_workspace_size(m.nfaces, nverts, C.byref(size)),
+                't3_smooth_normals_workspace_size')
+        ws = torch.empty(max(size.value, 16), dtype=torch.uint8, device=dev)
+        N.check(lib.t3_smooth_normals(C.byref(m), nverts, self.norm.data_ptr(), ws.data_ptr(), ws.numel(),
+                                      torch.cuda.current_stream().cuda_stream), 't3_smooth_normals')
+
+    def _t3_fill(self, m, device, keep):
+        self.mesh._t3_fill(m, device, keep)
+        if self.norm is None:
+            raise RuntimeError('MeshSmoothNormal: normals not computed yet (pre_compute or update_normal)')
+        m.norms = ptr(self.norm, device, keep)
+        m.slot_norm = m.slot_vert
+
+
 class MeshToWire(MeshEditBase):
     """The polygon edges of a mesh as lines for the wireframe rasteriser
     (tina/mesh/wire.py:5-40): line n joins corners n % p and (n + 1) % p of

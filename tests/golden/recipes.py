@@ -71,11 +71,44 @@ def inputs(name):
         x, y = np.meshgrid(u * 2 - 1, u * 2 - 1, indexing='ij')
         pos = np.stack([x, y, 0.2 * np.cos(2 * x) * np.sin(3 * y + 0.3)], -1).astype(np.float32)
         return {'pos': pos}
+    if name == 'smooth_model':
+        return {'v': _bumpy_sphere(41)[0], 'f': _bumpy_sphere(41)[1],
+                'v2': _bumpy_sphere(42, nlat=6, nlon=9)[0], 'f2': _bumpy_sphere(42, nlat=6, nlon=9)[1]}
     raise KeyError(name)
 
 
+def _bumpy_sphere(seed, nlat=9, nlon=14):
+    """An indexed lat-long sphere with shared, randomly displaced vertices, one
+    degenerate face (a repeated vertex) and one vertex no face uses."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    v = [[0.0, 0.0, 1.0]]
+    for i in range(1, nlat):
+        th = np.pi * i / nlat
+        for j in range(nlon):
+            ph = 2 * np.pi * j / nlon
+            v.append([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
+    v.append([0.0, 0.0, -1.0])
+    v = np.array(v) * rng.uniform(0.85, 1.15, size=(len(v), 1))
+    ring = lambda i, j: 1 + (i - 1) * nlon + j % nlon
+    f = [[0, ring(1, j), ring(1, j + 1)] for j in range(nlon)]
+    for i in range(1, nlat - 1):
+        for j in range(nlon):
+            f.append([ring(i, j), ring(i + 1, j), ring(i + 1, j + 1)])
+            f.append([ring(i, j), ring(i + 1, j + 1), ring(i, j + 1)])
+    last = len(v) - 1
+    f += [[last, ring(nlat - 1, j + 1), ring(nlat - 1, j)] for j in range(nlon)]
+    f.append([ring(2, 0), ring(2, 0), ring(2, 1)])
+    v = np.concatenate([v, [[3.0, 3.0, 3.0]]])
+    return v.astype(np.float32), np.array(f, np.int32)
+
+
+def _obj(v, f):
+    fi = np.stack([f, np.zeros_like(f), np.zeros_like(f)], axis=2)
+    return {'v': v, 'vt': np.zeros((1, 2), np.float32), 'vn': np.zeros((1, 3), np.float32), 'f': fi}
+
+
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
-         'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid']
+         'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid', 'smooth_model']
 
 
 def build(tina, name, arrays, matrix):
@@ -200,6 +233,16 @@ def build(tina, name, arrays, matrix):
         scene.add_object(tina.MeshToWire(grid))
         scene.add_object(grid, tina.PBR(metallic=0.3, roughness=0.4))
         scene.engine.set_camera(matrix.lookat(back=(0.3, -1.2, 2.2)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'smooth_model':
+        scene = tina.Scene(48, 36, smoothing=True)
+        model = tina.MeshSmoothNormal(tina.MeshModel(_obj(arrays['v'], arrays['f'])))
+        scene.add_object(model, tina.PBR(basecolor=[0.6, 0.7, 0.9], metallic=0.1, roughness=0.3))
+        # (the reference's MeshTransform cannot wrap a MeshModel: its getters return tuples)
+        v2 = arrays['v2'] * np.float32(0.45) + np.float32([0.9, 0.5, 0.4])
+        small = tina.MeshSmoothNormal(tina.MeshModel(_obj(v2.astype(np.float32), arrays['f2'])))
+        scene.add_object(small, tina.Classic())
+        scene.engine.set_camera(matrix.lookat(back=(0.4, 0.3, 3.2)), matrix.perspective(60, 48 / 36))
         return scene, False
     raise KeyError(name)
 
