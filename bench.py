@@ -208,6 +208,24 @@ def time_graph(g, reps, flush=None):
     return statistics.median(times)
 
 
+def direct_launches(scene):
+    """Kernels of one direct-mode t3_render: the clear; per object the vertex
+    stage (grids and indexed meshes), then the raster and the large-face pass
+    (one kernel for particles and lines); the shading kernel."""
+    from taichi_three_gb300 import _native as N
+    sc, keep = scene.describe()
+    n = 1
+    for o in range(sc.nobjects):
+        m = sc.objects[o].mesh
+        if m.kind == N.T3_MESH_PARTICLES or m.kind == N.T3_MESH_LINES or (m.flags & N.T3_MESH_WIREFRAME):
+            n += 1
+            continue
+        if m.kind in (N.T3_MESH_GRID, N.T3_MESH_INDEXED):
+            n += 1
+        n += 2
+    return n + 1
+
+
 def stage_times(scene, reps=10):
     """Median ms of the three stages of t3_render_staged for the scene's
     current state (upload+clear | raster | shade)."""
@@ -427,8 +445,8 @@ def main():
     with torch.cuda.graph(graph):
         frame(torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    if args.raster == "direct":  # clear, (raster, big) x objects, shade
-        kernels_per_frame = 1 + 2 * len(scene.objects) + 1
+    if args.raster == "direct":
+        kernels_per_frame = direct_launches(scene)
         stage_names = ("clear", "raster", "shade")
     else:                        # upload, bin x objects, tile (raster + shade)
         kernels_per_frame = 1 + len(scene.objects) + 1

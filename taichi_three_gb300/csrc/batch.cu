@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_batch_raster(const __grid_co
   }
 }
 
-template <int NL>
+template <int NL, bool TEX, int SIG>
 __global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_constant__ BatchArgs a) {
   __shared__ int s_list[kBatchBlock * kBatchPPT];
   __shared__ int s_count;
@@ -163,8 +163,8 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_con
     const BatchView& v = a.v[s];
     const int64_t base = (int64_t)(gs - v.shade_item0) * a.pixels_per_item;
     for (int64_t p0 = base; p0 < base + a.pixels_per_item && p0 < v.npix; p0 += kBatchBlock * kBatchPPT) {
-      shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS>(v.sc, v.keys, v.rec, v.out, v.npix, p0,
-                                                               s_list, &s_count);
+      shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS, false, TEX, SIG>(v.sc, v.keys, v.rec, v.out,
+                                                                                v.npix, p0, s_list, &s_count);
       __syncthreads();
       if (threadIdx.x == 0) s_count = 0;
       __syncthreads();
@@ -251,7 +251,8 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   a.faces_per_item = c.faces_per_item;
   a.pixels_per_item = c.pixels_per_item;
   a.queue = reinterpret_cast<uint32_t*>(ws + L.counters);
-  int nl = 1;
+  int nl = 1, sig = -1;
+  bool textured = false;
   uint32_t item = 0;
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < nscenes && e == cudaSuccess; s++) {
@@ -262,6 +263,9 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
       if (is_point_or_line(scenes[s].objects[o].mesh)) return T3_EUNSUPPORTED;
     if (!outs[s].rgb) return T3_EINVAL;
     nl = max_lobes(ds) > nl ? max_lobes(ds) : nl;
+    textured = textured || has_textures(ds) != 0;
+    const int ssig = lobe_signature(ds);
+    sig = sig < 0 || sig == ssig ? ssig : 0;
     DevScene* dst = reinterpret_cast<DevScene*>(ws + L.scenes + align256b(sizeof(DevScene)) * (size_t)s);
     // the first upload also zeroes the queue counters and the status
     e = launch_upload_scene(ds, dst, s == 0 ? a.queue : nullptr, s == 0 ? 2 : 0, s == 0 ? status : nullptr,
@@ -294,16 +298,24 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   int dev = 0, nsm = 0, occ_r = 0, occ_s = 0;
   e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const void* shade_fn = nl <= 2 ? (const void*)k_batch_shade<2> : (const void*)k_batch_shade<4>;
+  // the shading instance: lobe kinds as constants when every view shares an
+  // untextured signature, texture nodes compiled in only when a view has one
+  const void* shade_fn;
+  if (!textured && sig == T3_SIG_PBR) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_PBR>;
+  else if (!textured && sig == T3_SIG_CLASSIC) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC>;
+  else if (!textured && sig == T3_SIG_DIFFUSE) shade_fn = (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE>;
+  else if (nl <= 2) shade_fn = textured ? (const void*)k_batch_shade<2, true, 0> : (const void*)k_batch_shade<2, false, 0>;
+  else shade_fn = textured ? (const void*)k_batch_shade<4, true, 0> : (const void*)k_batch_shade<4, false, 0>;
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_r, (const void*)k_batch_raster, kBatchBlock, 0);
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, shade_fn, kBatchBlock, 0);
   if (e != cudaSuccess) return T3_ECUDA;
   auto per_sm = [&](int occ) { return c.ctas_per_sm > 0 && c.ctas_per_sm < occ ? c.ctas_per_sm : (occ > 0 ? occ : 1); };
   k_batch_raster<<<nsm * per_sm(occ_r), kBatchBlock, 0, st>>>(a);
-  if (nl <= 2) k_batch_shade<2><<<nsm * per_sm(occ_s), kBatchBlock, 0, st>>>(a);
-  else k_batch_shade<4><<<nsm * per_sm(occ_s), kBatchBlock, 0, st>>>(a);
-  return cudaGetLastError() == cudaSuccess ? T3_OK : T3_ECUDA;
+  void* args[] = {&a};
+  e = cudaLaunchKernel(shade_fn, dim3(nsm * per_sm(occ_s)), dim3(kBatchBlock), args, 0, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? T3_OK : T3_ECUDA;
 }
 
 } // extern "C"

@@ -40,7 +40,7 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
 // descriptor is a __grid_constant__ kernel parameter: lamps, materials and
 // camera are read through the constant cache (warp-uniform broadcasts), not
 // as per-pixel global loads.
-template <int BLOCK, int PPT, int NL, int MODE, bool TEX>
+template <int BLOCK, int PPT, int NL, int MODE, bool TEX, int SIG>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_shade(const __grid_constant__ DevScene sc, const unsigned long long* __restrict__ keys,
         const float4* __restrict__ rec, t3_outputs out, int64_t npix) {
@@ -48,16 +48,41 @@ k_shade(const __grid_constant__ DevScene sc, const unsigned long long* __restric
   __shared__ int s_count;
   if (threadIdx.x == 0) s_count = 0;
   __syncthreads();
-  shade_block<BLOCK, PPT, NL, MODE, false, TEX>(&sc, keys, rec, out, npix, (int64_t)blockIdx.x * BLOCK * PPT,
-                                                s_list, &s_count);
+  shade_block<BLOCK, PPT, NL, MODE, false, TEX, SIG>(&sc, keys, rec, out, npix,
+                                                     (int64_t)blockIdx.x * BLOCK * PPT, s_list, &s_count);
 }
 
-template <int NL, int MODE, bool TEX>
+// the lobe signature shared by every shaded object, when an instance exists
+// for it (lines take the line colour and are not shaded); 0 otherwise
+int lobe_signature(const DevScene& sc) {
+  int sig = -1;
+  for (int o = 0; o < sc.nobjects; o++) {
+    if (is_wire(sc.obj[o].mesh)) continue;
+    const DevMaterial& m = sc.obj[o].mat;
+    if (m.nlobes > 2) return 0;
+    int s = 0;
+    for (int k = 0; k < m.nlobes; k++) s |= m.lobes[k].kind << (8 * k);
+    if (sig >= 0 && s != sig) return 0;
+    sig = s;
+  }
+  return sig == T3_SIG_PBR || sig == T3_SIG_CLASSIC || sig == T3_SIG_DIFFUSE ? sig : 0;
+}
+
+template <int NL, int MODE, bool TEX, int SIG = 0>
 static void launch_shade_t(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                            const t3_outputs& out, int64_t npix, cudaStream_t st) {
   constexpr int BLOCK = 256, PPT = 4;
   const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
-  k_shade<BLOCK, PPT, NL, MODE, TEX><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix);
+  if constexpr (MODE == T3_LIGHT_LAMPS && !TEX && SIG == 0) {
+    // untextured lamp scenes with one common lobe signature
+    const int sig = lobe_signature(sc);
+    if (NL == 2 && sig == T3_SIG_PBR) return launch_shade_t<2, MODE, TEX, T3_SIG_PBR>(sc, keys, rec, out, npix, st);
+    if (NL == 2 && sig == T3_SIG_CLASSIC)
+      return launch_shade_t<2, MODE, TEX, T3_SIG_CLASSIC>(sc, keys, rec, out, npix, st);
+    if (NL == 1 && sig == T3_SIG_DIFFUSE)
+      return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE>(sc, keys, rec, out, npix, st);
+  }
+  k_shade<BLOCK, PPT, NL, MODE, TEX, SIG><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix);
 }
 
 template <int MODE, bool TEX>

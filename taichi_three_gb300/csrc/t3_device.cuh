@@ -375,7 +375,7 @@ __device__ __forceinline__ bool particle_covers(const ParSetup& p, f3 Pl) {
 }
 
 // ---- wireframe (WireframeRaster, tina/core/wireframe.py) ----------------------
-__device__ __forceinline__ bool is_wire(const t3_mesh& d) {
+__host__ __device__ __forceinline__ bool is_wire(const t3_mesh& d) {
   return d.kind == T3_MESH_LINES || (d.flags & T3_MESH_WIREFRAME) != 0;
 }
 

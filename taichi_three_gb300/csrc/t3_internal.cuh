@@ -119,6 +119,9 @@ cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const 
 cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                              const t3_outputs& out, int32_t* status, cudaStream_t st);
 int max_lobes(const DevScene& sc);
+// the lobe kinds (one byte per slot) shared by every shaded object of the
+// scene when a specialised shading instance exists for them, else 0
+int lobe_signature(const DevScene& sc);
 int has_textures(const DevScene& sc);  // any Texture / ChessboardTexture node
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,

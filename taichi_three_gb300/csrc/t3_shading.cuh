@@ -28,7 +28,7 @@ __device__ __forceinline__ V3 one_minus(V3 a) { return v3(1.0f - a.x, 1.0f - a.y
 __device__ __forceinline__ V3 tov(f3 a) { return v3(a.x, a.y, a.z); }
 
 __device__ __forceinline__ float aces(float c) {
-  return (c * (2.51f * c + 0.03f)) / (c * (2.43f * c + 0.59f) + 0.14f);
+  return __fdividef(c * (2.51f * c + 0.03f), c * (2.43f * c + 0.59f) + 0.14f);
 }
 
 __device__ __forceinline__ float ipowf(float x, int n) {
@@ -133,13 +133,22 @@ struct LobeState {
   int kind[NL];
   V3 w[NL];   // lobe weight
   V3 f0[NL];  // COOK fresnel
-  float a2[NL], k[NL], gnorm[NL];
+  float a2[NL], oma2[NL], k[NL], gnorm[NL];
   float m[NL];
   int ipow[NL];
   int n;
 };
 
-template <int NL, bool TEX = true>
+// Lobe signatures: the kinds of a material's flattened lobes, one byte per
+// slot (0 = none).  A kernel instantiated for a signature has the lobe kinds as
+// constants (no per-lamp dispatch); SIG 0 reads them from the material.
+constexpr int T3_SIG_DIFFUSE = T3_OP_LAMBERT;                      // Diffuse, Lambert * c
+constexpr int T3_SIG_PBR = T3_OP_LAMBERT | (T3_OP_COOK << 8);      // PBR
+constexpr int T3_SIG_CLASSIC = T3_OP_LAMBERT | (T3_OP_PHONG << 8); // Classic
+template <int SIG>
+__device__ __forceinline__ constexpr int sig_kind(int k) { return (SIG >> (8 * k)) & 0xFF; }
+
+template <int NL, bool TEX = true, int SIG = 0>
 __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag& fg, V3 viewdir,
                                               LobeState<NL>& L, V3& ambient, V3& emission) {
   L.n = mat.nlobes;
@@ -156,20 +165,21 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
       const V3 f = eval_value<TEX>(mat, lb.fac[j] & 0xFFFF, fg);
       w = w * ((lb.fac[j] & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
     }
-    L.kind[k] = lb.kind;
-    if (lb.kind == T3_OP_EMISSION) emission = emission + w;
+    const int kind = SIG ? sig_kind<SIG>(k) : lb.kind;
+    L.kind[k] = kind;
+    if (kind == T3_OP_EMISSION) emission = emission + w;
     else ambient = ambient + w;
-    if (lb.kind == T3_OP_COOK) {
+    if (kind == T3_OP_COOK) {
       // per-pixel parts of CookTorrance.sub_brdf (material.py:323-357)
       const float r = eval_value<TEX>(mat, lb.p0, fg).x;
       const float a2 = fmaxf(1e-6f, r * r);
       const float kk = a2 * 0.5f;
       L.a2[k] = a2;
       L.k[k] = kk;
-      const float gv = 1.0f / ((NoV * kk + 1.0f) - kk);
-      L.gnorm[k] = gv / (1.0f * (1.0f - a2) + 12.566370614359172f * a2);
+      L.gnorm[k] = __fdividef(1.0f, ((NoV * kk + 1.0f) - kk) * (1.0f * (1.0f - a2) + 12.566370614359172f * a2));
+      L.oma2[k] = 1.0f - a2;
       L.f0[k] = eval_value<TEX>(mat, lb.p1, fg);
-    } else if (lb.kind == T3_OP_PHONG) {
+    } else if (kind == T3_OP_PHONG) {
       L.m[k] = eval_value<TEX>(mat, lb.p0, fg).x;
       L.ipow[k] = lb.int_pow;
     }
@@ -178,20 +188,21 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
 }
 
 // sum_k W_k * brdf_k(n, L, V)
-template <int NL>
+template <int NL, int SIG = 0>
 __device__ __forceinline__ V3 eval_brdf(const LobeState<NL>& L, V3 n, V3 ldir, V3 vdir) {
   V3 acc = v3(0.f, 0.f, 0.f);
 #pragma unroll
   for (int k = 0; k < NL; k++) {
-    if (L.kind[k] == T3_OP_LAMBERT) {
+    const int kind = SIG ? sig_kind<SIG>(k) : L.kind[k];
+    if (kind == T3_OP_LAMBERT) {
       acc = acc + 0.31830988618379067f * L.w[k];
-    } else if (L.kind[k] == T3_OP_COOK) {
+    } else if (kind == T3_OP_COOK) {
       const V3 half = normalized(ldir + vdir);
       const float NoH = fmaxf(1e-10f, dot(half, n));
       const float NoL = fmaxf(1e-10f, dot(ldir, n));
       const float VoH = fminf(1.0f, fmaxf(1e-10f, dot(half, vdir)));
       const float a2 = L.a2[k];
-      const float denom = 1.0f - (NoH * NoH) * (1.0f - a2);
+      const float denom = 1.0f - (NoH * NoH) * L.oma2[k];
       const float ndf = __fdividef(a2, denom * denom);
       const float vdf = __fdividef(L.gnorm[k], (NoL * L.k[k] + 1.0f) - L.k[k]);
       const float om = 1.0f - VoH;
@@ -200,7 +211,7 @@ __device__ __forceinline__ V3 eval_brdf(const LobeState<NL>& L, V3 n, V3 ldir, V
       const V3 f0 = L.f0[k];
       const V3 fdf = f0 + p5 * one_minus(f0);
       acc = acc + (vdf * ndf) * (L.w[k] * fdf);
-    } else if (L.kind[k] == T3_OP_PHONG) {
+    } else if (kind == T3_OP_PHONG) {
       // reflect(-L, n) = -L - 2 (n . -L) n
       const V3 I = v3(-ldir.x, -ldir.y, -ldir.z);
       const V3 rdir = I - (2.0f * dot(n, I)) * n;
@@ -246,7 +257,7 @@ __device__ __forceinline__ V3 view_ray(const t3_frame& fr, float px, float py) {
   const float* M = fr.V2W;
   const float bx = M[3] + M[0] * ux + M[1] * uy, by = M[7] + M[4] * ux + M[5] * uy;
   const float bz = M[11] + M[8] * ux + M[9] * uy, bw = M[15] + M[12] * ux + M[13] * uy;
-  const float w0 = 1.0f / (bw - M[14]), w1 = 1.0f / (bw + M[14]);
+  const float w0 = __fdividef(1.0f, bw - M[14]), w1 = __fdividef(1.0f, bw + M[14]);
   const V3 ro = v3((bx - M[2]) * w0, (by - M[6]) * w0, (bz - M[10]) * w0);
   const V3 ro1 = v3((bx + M[2]) * w1, (by + M[6]) * w1, (bz + M[10]) * w1);
   return normalized(ro1 - ro);
@@ -396,7 +407,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
 }
 
 // Lighting.shade_color's lamp loop (lighting.py:88-97) for the lobes in L
-template <int NL>
+template <int NL, int SIG = 0>
 __device__ __forceinline__ V3 lamps_term(const t3_lighting& lt, const LobeState<NL>& L,
                                          const Frag& fg, V3 vdir) {
   V3 color = v3(0.f, 0.f, 0.f);
@@ -411,7 +422,7 @@ __device__ __forceinline__ V3 lamps_term(const t3_lighting& lt, const LobeState<
     if (cos_i > 0.0f) {
       const float4 lc = *reinterpret_cast<const float4*>(lt.lights[l].color);
       const float s = cos_i * (inv_d * inv_d);
-      const V3 mcol = eval_brdf<NL>(L, fg.normal, ldir, vdir);
+      const V3 mcol = eval_brdf<NL, SIG>(L, fg.normal, ldir, vdir);
       color = color + v3(s * lc.x, s * lc.y, s * lc.z) * mcol;
     }
   }
@@ -428,9 +439,13 @@ __device__ __forceinline__ void store_rgb(const t3_frame& fr, const t3_outputs& 
   }
 }
 
+template <int NL, int MODE, bool TEX, int SIG = 0>
+__device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const PixelGeom& g,
+                                          const t3_outputs& out);
+
 // Shades pixel (x, y) from its packed (depth, id) key and writes every output.
 // MODE is the lighting (T3_LIGHT_LAMPS or T3_LIGHT_IBL_MC).
-template <int NL, int MODE, bool COHERENT_REC = false, bool TEX = true>
+template <int NL, int MODE, bool COHERENT_REC = false, bool TEX = true, int SIG = 0>
 __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
                                                      const float4* __restrict__ rec,
                                                      unsigned long long key, int x, int y,
@@ -452,13 +467,22 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     store_rgb(fr, out, g.i, g.fg.color);
     return;
   }
+  shade_lit<NL, MODE, TEX, SIG>(sc, g, out);
+}
+
+// the lighting of one covered pixel from its geometry (Shader.shade_color)
+template <int NL, int MODE, bool TEX, int SIG>
+__device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const PixelGeom& g,
+                                          const t3_outputs& out) {
+  const t3_frame& fr = sc->frame;
+  const t3_lighting& lt = sc->lighting;
   V3 color;
   if (MODE == T3_LIGHT_LAMPS) {
     LobeState<NL> L;
     V3 amb, emi;
-    eval_material<NL, TEX>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
+    eval_material<NL, TEX, SIG>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
     color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
-    color = color + lamps_term<NL>(lt, L, g.fg, g.vdir);
+    color = color + lamps_term<NL, SIG>(lt, L, g.fg, g.vdir);
   } else {
     // SkyboxLighting.shade_color (lighting.py:20-21): IBL + emission
     IblLobes<NL> L;
@@ -469,8 +493,8 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     if (lt.nlights > 0) {
       LobeState<NL> Ll;
       V3 amb, e2;
-      eval_material<NL, TEX>(g.ob->mat, g.fg, g.vdir, Ll, amb, e2);
-      color = color + lamps_term<NL>(lt, Ll, g.fg, g.vdir);
+      eval_material<NL, TEX, SIG>(g.ob->mat, g.fg, g.vdir, Ll, amb, e2);
+      color = color + lamps_term<NL, SIG>(lt, Ll, g.fg, g.vdir);
     }
   }
   store_rgb(fr, out, g.i, color);
@@ -481,7 +505,7 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
 // compacted into a shared list (warp ballot + one shared atomic per warp) so
 // that full warps run the shading.  s_list holds BLOCK * PPT entries; s_count
 // must be zero on entry and is left non-zero (callers reset it after a barrier).
-template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false, bool TEX = true>
+template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false, bool TEX = true, int SIG = 0>
 __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
                                             const unsigned long long* __restrict__ keys,
                                             const float4* __restrict__ rec, const t3_outputs& out,
@@ -515,7 +539,7 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
     const int64_t i = base + s_list[j];
     const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
     const unsigned long long key = COHERENT ? __ldcg(keys + i) : keys[i];
-    shade_pixel_from_key<NL, MODE, COHERENT, TEX>(sc, rec, key, x, y, out);
+    shade_pixel_from_key<NL, MODE, COHERENT, TEX, SIG>(sc, rec, key, x, y, out);
   }
 }
 
