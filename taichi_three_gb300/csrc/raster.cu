@@ -102,10 +102,15 @@ k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
   const int64_t stride = (int64_t)gridDim.x * BLOCK;
   for (uint32_t e = 0; e < count; e++) {
     const uint32_t n = big.items[e];
-    f3 v[3];
-    face_verts(mesh, face_ref(mesh, n), v);
     Setup s;
-    if (!face_setup(fr, v, s)) continue;
+    if (big.rec) {
+      // the setup record k_raster_direct stored for the face
+      load_record(big.rec, face_base + n, s);
+    } else {
+      f3 v[3];
+      face_verts(mesh, face_ref(mesh, n), v);
+      if (!face_setup(fr, v, s)) continue;
+    }
     const int32_t h = s.topy - s.boty + 1;
     const int64_t area = (int64_t)(s.topx - s.botx + 1) * h;
     const uint32_t id = face_base + n;
@@ -144,7 +149,7 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
     k_raster_direct<BLOCK, true><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
                                                                   (uint32_t)ob.face_base, keys, big,
                                                                   big_threshold);
-    k_raster_big<BLOCK, true><<<2 * 152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
+    k_raster_big<BLOCK, true><<<152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
     return cudaGetLastError();
   }
   k_raster_direct<BLOCK, false><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
@@ -152,7 +157,7 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
                                                                  big_threshold);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_raster_big<BLOCK, false><<<2 * 152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
+  k_raster_big<BLOCK, false><<<152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
   return cudaGetLastError();
 }
 
