@@ -330,7 +330,8 @@ __global__ void k_mlp_pack(const float* __restrict__ params, unsigned char* __re
   for (int l = 0; l < 4; l++) {
     const int n_el = layers[l].K * layers[l].N;
     if (tid >= base && tid < base + n_el) {
-      const int e = tid - base, k = e / layers[l].N, n = e % layers[l].N;  // W[k][n]
+      const int e = tid - base, k0 = e / layers[l].N, n = e % layers[l].N;  // W[k0][n]
+      const int k = l == 0 ? packed_k1(k0) : k0;  // layer 1 in the packed feature order
       const uint32_t off = layers[l].off + tc_chunk_off(n, k & ~7, layers[l].K) + (k & 7) * 2;
       *reinterpret_cast<__nv_bfloat16*>(blob + off) = __float2bfloat16_rn(layers[l].W[e]);
     }
@@ -362,7 +363,7 @@ k_mlp_infer_tc(const unsigned char* __restrict__ blob, const float* __restrict__
       float x[8];
 #pragma unroll
       for (int i = 0; i < 8; i++) x[i] = row < B ? X[row * T3_MLP_IN + k + i] : 0.0f;
-      *reinterpret_cast<uint4*>(sm + kA + tc_chunk_off(threadIdx.x, k, T3_MLP_IN)) = pack8_bf16(x);
+      *reinterpret_cast<uint4*>(sm + kA + tc_chunk_off(threadIdx.x, packed_k1(k), T3_MLP_IN)) = pack8_bf16(x);
     }
     float out[16];
     if (!mlp_tile(t, out)) {

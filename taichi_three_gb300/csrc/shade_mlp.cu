@@ -2,16 +2,17 @@
 // (T3_LIGHT_IBL_MLP): interpolation and material evaluation on the CUDA cores,
 // the network on the tensor cores, fused in one persistent kernel.
 //
-// One CTA of 128 threads per SM (the packed network and the A / H operands
-// take 185 KB of shared memory).  The CTA walks its share of the frame in
-// chunks of 128 pixels: empty pixels get the sky along the view ray at once,
-// covered ones are appended to a shared list.  Whenever 128 covered pixels are
-// pending (or the frame is done), thread t takes list entry t: it interpolates
-// the fragment, evaluates the material into the weights of the network's nine
-// outputs, adds emission and any lamps, and writes its Fourier features as row
-// t of the A operand; one elected thread then issues the four layers'
-// tcgen05.mma (t3_mlp_tc.cuh), and thread t reads row t of the result from
-// tensor memory and composes the pixel:
+// One persistent CTA per SM holds the packed network in shared memory and
+// kMlpGroups independent groups of 128 threads (t3_mlp_group.cuh).  Each
+// group walks its own stream of 128-pixel chunks: empty pixels get the sky
+// along the view ray at once, covered ones are appended to the group's list.
+// Whenever 128 covered pixels are pending (or the stream ends), the group's
+// thread t takes list entry t: it interpolates the fragment, evaluates the
+// material into the weights of the network's nine outputs, adds emission and
+// any lamps, and encodes its Fourier features into row t of the A operand
+// chunk by chunk while the group's elected thread issues the layers'
+// tcgen05.mma; thread t then reads row t of the result from tensor memory and
+// composes the pixel:
 //   rgb = emission + lamps + cd * E_d + c1 * S1 + c2 * S2,
 // with (E_d, S1, S2) = expm1 of the network outputs, cd the summed Lambert lobe
 // weights, c1 / c2 the CookTorrance lobe weight times f0 / (1 - f0) -- the

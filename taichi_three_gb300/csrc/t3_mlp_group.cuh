@@ -3,17 +3,19 @@
 //
 // A CTA holds the packed network once (t3_mlp_tc.cuh layout, 70,464 bytes) and
 // kMlpGroups groups of 128 threads (4 warps each).  Group g owns TMEM columns
-// [128 g, 128 g + 128) of the CTA's 512 (layer outputs alternate between
-// columns +0 and +64) and two 16 KB A-chunk buffers; once the first layer is
-// done, buffer 0 holds the hidden operand H of the later layers.
+// [64 g, 64 g + 64) of the CTA's 512 -- every layer accumulates into the same
+// columns: the epilogue has read a layer's output into registers before the
+// next layer's MMAs are issued -- and two 8 KB A-chunk buffers, which together
+// hold the hidden operand H of the later layers once the first layer is done.
 // The first layer's A operand (128 rows x 400 features) is never materialised
-// whole: the group encodes one input coordinate (64 features) at a time into a
-// chunk buffer and its elected thread issues that chunk's four K = 16 MMAs,
-// accumulating into D1; the other buffer is being encoded meanwhile.  Each
-// buffer has an mbarrier that tcgen05.commit arrives on, so a buffer is
-// rewritten only after the MMAs reading it have completed.  Groups synchronise
-// with named barriers (ids 1..kMlpGroups), so one group's gathers and encoding
-// overlap another group's MMAs and epilogues.
+// whole: the group encodes half an input coordinate (32 features, packed
+// order of t3_mlp_tc.cuh) at a time into a chunk buffer and its elected thread
+// issues that chunk's two K = 16 MMAs; the other buffer is being encoded
+// meanwhile.  Each buffer has an mbarrier that tcgen05.commit arrives on, so a
+// buffer is rewritten only after the MMAs reading it have completed.  Small
+// per-group footprints let six groups share an SM, and groups synchronise with
+// named barriers (ids 1..kMlpGroups), so one group's gathers and encoding
+// overlap the other groups' MMA round trips.
 //
 // Every wait is bounded; a group whose wait runs out reports false (after one
 // more bounded wait for its own MMAs) and stops.
@@ -24,14 +26,15 @@
 namespace t3 {
 
 #ifndef T3_MLP_GROUPS
-#define T3_MLP_GROUPS 4
+#define T3_MLP_GROUPS 6
 #endif
-constexpr int kMlpGroups = T3_MLP_GROUPS;        // 3 or 4 (TMEM: 128 columns each)
+constexpr int kMlpGroups = T3_MLP_GROUPS;        // up to 8 (TMEM: 64 columns each)
 constexpr uint32_t kGroupBase = 71680;           // kBlob rounded up to 1 KB
-constexpr uint32_t kChunkBytes = 128 * 64 * 2;   // 128 rows x 64 BF16
-constexpr uint32_t kGroupBytes = 2 * kChunkBytes;  // A0 (later H), A1
+constexpr uint32_t kChunkBytes = 128 * 32 * 2;   // 128 rows x 32 BF16
+constexpr uint32_t kGroupBytes = 2 * kChunkBytes;  // A0, A1 (together: H, 128 x 64 BF16)
 constexpr uint32_t kMlpGroupSmem = kGroupBase + kMlpGroups * kGroupBytes;
-static_assert(kMlpGroups * 128 <= 512, "TMEM holds 512 columns");
+static_assert(kMlpGroups * 64 <= 512, "TMEM holds 512 columns");
+static_assert(kMlpGroupSmem + kMlpGroups * 1040 + 64 <= 232448, "shared memory per CTA");
 constexpr uint32_t kGroupTmemCols = 512;
 static_assert(kGroupBase >= kBlob, "packed network overlaps the group areas");
 
@@ -108,16 +111,14 @@ __device__ __forceinline__ void group_epilogue(const MlpGroup& G, uint32_t col, 
   }
 }
 
-// Coordinate c (0..5) of the row's inputs as 64 BF16 features in chunk buffer b
-__device__ __forceinline__ void group_encode_coord(const MlpGroup& G, int b, float x) {
-  float s[32], co[32];
-  encode_coord(x, s, co);
+// Half h of the row's coordinate x as 32 BF16 features in chunk buffer b (K = 32 layout)
+__device__ __forceinline__ void group_encode_half(const MlpGroup& G, int b, float x, int h, float st[8]) {
+  float f[32];
+  encode_half(x, h, st, f);
   unsigned char* A = G.sm + G.a[b];
 #pragma unroll
-  for (int q = 0; q < 4; q++) {
-    *reinterpret_cast<uint4*>(A + tc_chunk_off(G.row, 8 * q, 64)) = pack8_bf16(s + 8 * q);
-    *reinterpret_cast<uint4*>(A + tc_chunk_off(G.row, 32 + 8 * q, 64)) = pack8_bf16(co + 8 * q);
-  }
+  for (int q = 0; q < 4; q++)
+    *reinterpret_cast<uint4*>(A + tc_chunk_off(G.row, 8 * q, 32)) = pack8_bf16(f + 8 * q);
 }
 
 // The last 16 inputs (roughness, metallic, zero padding) in chunk buffer b (K = 16 layout)
@@ -136,43 +137,43 @@ __device__ __forceinline__ void group_encode_tail(const MlpGroup& G, int b, floa
 __device__ __forceinline__ bool group_tile(MlpGroup& G, const float in[6], float rough, float metal,
                                            float out[16]) {
   const bool leader = G.row == 0;
-  const uint32_t D1 = 0, D2 = 64;
-  // layer 1: seven K chunks (6 coordinates x 64 features, then 16 tail inputs)
-  for (int c = 0; c < 7; c++) {
-    const int b = c & 1;
-    if (c >= 2 && !group_wait(G, b)) return false;  // chunk c - 2 has left buffer b
-    if (c < 6) group_encode_coord(G, b, in[c]);
+  // layer 1: thirteen K chunks (6 coordinates x 2 halves x 32 features, then
+  // the 16 tail inputs), chunk k in buffer k & 1, all into the group's columns
+  float st[8];
+  for (int k = 0; k < 13; k++) {
+    const int b = k & 1;
+    if (k >= 2 && !group_wait(G, b)) return false;  // chunk k - 2 has left buffer b
+    if (k < 12) group_encode_half(G, b, in[k >> 1], k & 1, st);
     else group_encode_tail(G, b, rough, metal);
     fence_async_smem();
     tc_fence_before();
     group_sync(G.id);
     if (leader) {
       tc_fence_after();
-      if (c < 6) group_issue(G, G.a[b], 1024u, kW1 + (uint32_t)c * 1024u, 6400u, 4, 64, D1, c > 0, b);
-      else group_issue(G, G.a[b], 256u, kW1 + 6144u, 6400u, 1, 64, D1, true, b);
+      if (k < 12) group_issue(G, G.a[b], 512u, kW1 + (uint32_t)k * 512u, 6400u, 2, 64, 0, k > 0, b);
+      else group_issue(G, G.a[b], 256u, kW1 + 6144u, 6400u, 1, 64, 0, true, b);
     }
   }
-  if (!group_wait(G, 1)) return false;  // chunk 5
-  if (!group_wait(G, 0)) return false;  // chunk 6: D1 complete
-  // layers 2-4 alternate between the two column blocks
-  const uint32_t cols[3] = {D2, D1, D2};
+  if (!group_wait(G, 1)) return false;  // chunk 11
+  if (!group_wait(G, 0)) return false;  // chunk 12: layer 1 complete
+  // layers 2-4 read the previous output back (bias + ReLU into H) and overwrite
+  // the same columns: each epilogue's TMEM loads complete (tcgen05.wait::ld)
+  // before the group barrier that precedes the next issue
   const uint32_t w[3] = {kW2, kW3, kW4};
   const uint32_t bias_in[3] = {kB1, kB2, kB3};
-  uint32_t src = D1;
   for (int l = 0; l < 3; l++) {
-    group_epilogue(G, src, bias_in[l]);
+    group_epilogue(G, 0, bias_in[l]);
     fence_async_smem();
     tc_fence_before();
     group_sync(G.id);
     if (leader) {
       tc_fence_after();
-      group_issue(G, G.h, 1024u, w[l], 1024u, 4, l == 2 ? 16 : 64, cols[l], false, 2);
+      group_issue(G, G.h, 1024u, w[l], 1024u, 4, l == 2 ? 16 : 64, 0, false, 2);
     }
     if (!group_wait(G, 2)) return false;
-    src = cols[l];
   }
   const uint32_t lane_base = (uint32_t)((threadIdx.x & 96) << 16);
-  tc_ld16(G.tmem + lane_base + D2, out);
+  tc_ld16(G.tmem + lane_base, out);
   const float* b4 = reinterpret_cast<const float*>(G.sm + kB4);
 #pragma unroll
   for (int i = 0; i < 16; i++) out[i] += b4[i];
@@ -214,7 +215,7 @@ __device__ __forceinline__ MlpGroup group_init(unsigned char* sm, uint64_t (*gba
   MlpGroup G;
   const int g = threadIdx.x >> 7;
   G.sm = sm;
-  G.tmem = tmem_base + (uint32_t)g * 128u;
+  G.tmem = tmem_base + (uint32_t)g * 64u;
   for (int k = 0; k < 3; k++) {
     G.bar[k] = smem_addr(&gbar[g][k]);
     G.ph[k] = 0;
@@ -224,7 +225,7 @@ __device__ __forceinline__ MlpGroup group_init(unsigned char* sm, uint64_t (*gba
   const uint32_t base = kGroupBase + (uint32_t)g * kGroupBytes;
   G.a[0] = base;
   G.a[1] = base + kChunkBytes;
-  G.h = base;  // chunk buffer 0 is free once the first layer has completed
+  G.h = base;  // both chunk buffers are free once the first layer has completed
   return G;
 }
 

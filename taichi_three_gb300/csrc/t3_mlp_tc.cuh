@@ -69,27 +69,41 @@ __device__ __forceinline__ void mirror_inputs(const float nv[6], float in[6]) {
   in[5] = 2.0f * d * nv[2] - nv[5];
 }
 
-// Row `row` of the A operand (K = 400, BF16, core-matrix layout) from the six
-// direction coordinates (n, v), roughness and metallic.
-__device__ __forceinline__ void encode_row_bf16(const float nv[6], float rough, float metal,
-                                                unsigned char* A, int row) {
-  float in[6];
-  mirror_inputs(nv, in);
-#pragma unroll 1
-  for (int c = 0; c < 6; c++) {
-    float s[32], co[32];
-    encode_coord(in[c], s, co);
+// Packed K order of the first layer.  Features are produced per input
+// coordinate in two halves: half h holds the sines, then the cosines, of
+// octaves 4h..4h+3 (16 + 16 features), so a 32-feature K chunk is one half of
+// one coordinate.  packed_k1 maps a feature's index in the encoder's order
+// (coordinate c: 32 sines, then 32 cosines, f = 4 o + j) to its K position in
+// the packed W1 and in the A operand; 8-aligned runs stay 8-aligned and
+// contiguous.  The tail (roughness, metallic, padding) keeps its positions.
+__host__ __device__ __forceinline__ int packed_k1(int k) {
+  if (k >= 384) return k;
+  const int c = k >> 6, f = k & 63;
+  const bool cosine = f >= 32;
+  const int fi = f & 31;
+  return c * 64 + (fi >> 4) * 32 + (cosine ? 16 : 0) + (fi & 15);
+}
+
+// Half h of coordinate x's features in packed order: out[0..15] = sin, out[16..31]
+// = cos of octaves 4h..4h+3 (the same values as encode_coord); st carries the
+// (sin, cos) pairs of the four base phases from half 0 to half 1.
+__device__ __forceinline__ void encode_half(float x, int h, float st[8], float out[32]) {
+  const float base[4] = {3.141592653589793f, 3.7360043360892607f, 4.442882938158366f, 5.283508001182123f};
+  if (h == 0) {
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      *reinterpret_cast<uint4*>(A + tc_chunk_off(row, c * 64 + 8 * q, T3_MLP_IN)) = pack8_bf16(s + 8 * q);
-      *reinterpret_cast<uint4*>(A + tc_chunk_off(row, c * 64 + 32 + 8 * q, T3_MLP_IN)) =
-          pack8_bf16(co + 8 * q);
+    for (int j = 0; j < 4; j++) __sincosf(x * base[j], &st[2 * j], &st[2 * j + 1]);
+  }
+#pragma unroll
+  for (int o = 0; o < 4; o++) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float a = st[2 * j], b = st[2 * j + 1];
+      out[o * 4 + j] = a;
+      out[16 + o * 4 + j] = b;
+      st[2 * j] = 2.0f * a * b;
+      st[2 * j + 1] = (b - a) * (b + a);
     }
   }
-  float tail[8] = {rough, metal, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  *reinterpret_cast<uint4*>(A + tc_chunk_off(row, 384, T3_MLP_IN)) = pack8_bf16(tail);
-  tail[0] = tail[1] = 0.0f;
-  *reinterpret_cast<uint4*>(A + tc_chunk_off(row, 392, T3_MLP_IN)) = pack8_bf16(tail);
 }
 
 // one layer: D[128 x N] (TMEM column col) = A[128 x K] * W^T
