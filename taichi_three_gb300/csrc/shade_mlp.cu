@@ -98,14 +98,22 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
   const int64_t nchunks = (npix + 127) / 128;
   const int64_t stride = (int64_t)gridDim.x * kMlpGroups;
   int64_t chunk = (int64_t)blockIdx.x * kMlpGroups + g;
+  // the key of this thread's pixel in the next chunk, loaded one chunk ahead
+  auto key_of = [&](int64_t c) {
+    const int64_t i = c * 128 + G.row;
+    return c < nchunks && i < npix ? keys[i] : T3_EMPTY_KEY;
+  };
+  unsigned long long key = key_of(chunk);
   int pending = 0;
   while (ok) {
     // collect covered pixels until a full tile is pending or the stream ends
     while (pending < 128 && chunk < nchunks) {
       const int64_t i = chunk * 128 + G.row;
+      const unsigned long long k = key;
+      key = key_of(chunk + stride);
       bool covered = false;
       if (i < npix) {
-        if (keys[i] == T3_EMPTY_KEY) write_sky(fr, env, out, i);
+        if (k == T3_EMPTY_KEY) write_sky(fr, env, out, i);
         else covered = true;
       }
       const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
