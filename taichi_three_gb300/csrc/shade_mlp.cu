@@ -30,7 +30,7 @@ struct MlpCoeffs {
 
 // lobe weights of one fragment (materials of Lambert, CookTorrance and
 // Emission leaves with at most one CookTorrance; checked on the host)
-template <int NL>
+template <int NL, bool TEX, int SIG>
 __device__ __forceinline__ void eval_mlp_coeffs(const DevMaterial& mat, const Frag& fg, MlpCoeffs& q) {
   q.cd = q.c1 = q.c2 = q.base = v3(0.f, 0.f, 0.f);
   q.rough = 1.0f;
@@ -42,18 +42,19 @@ __device__ __forceinline__ void eval_mlp_coeffs(const DevMaterial& mat, const Fr
     V3 w = v3(1.f, 1.f, 1.f);
     for (int j = 0; j < lb.nfac; j++) {
       const int fj = lb.fac[j];
-      const V3 f = eval_value(mat, fj & 0xFFFF, fg);
+      const V3 f = eval_value<TEX>(mat, fj & 0xFFFF, fg);
       w = w * ((fj & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
     }
-    if (lb.kind == T3_OP_LAMBERT) {
+    const int kind = SIG ? sig_kind<SIG>(k) : lb.kind;
+    if (kind == T3_OP_LAMBERT) {
       q.cd = q.cd + w;
-    } else if (lb.kind == T3_OP_COOK) {
-      const V3 f0 = eval_value(mat, lb.p1, fg);
-      q.rough = eval_value(mat, lb.p0, fg).x;
+    } else if (kind == T3_OP_COOK) {
+      const V3 f0 = eval_value<TEX>(mat, lb.p1, fg);
+      q.rough = eval_value<TEX>(mat, lb.p0, fg).x;
       q.c1 = q.c1 + w * f0;
       q.c2 = q.c2 + w * one_minus(f0);
       q.metal = fminf(1.0f, fmaxf(0.0f, (f0.x + f0.y + f0.z) * (1.0f / 3.0f)));
-    } else if (lb.kind == T3_OP_EMISSION) {
+    } else if (kind == T3_OP_EMISSION) {
       q.base = q.base + w;
     }
   }
@@ -70,7 +71,7 @@ __device__ __forceinline__ void write_sky(const t3_frame& fr, const Env& env, co
   store_rgb(fr, out, i, env_sample(env, view_ray(fr, xadd((float)x, fr.bias[0]), xadd((float)y, fr.bias[1]))));
 }
 
-template <int NL>
+template <int NL, bool TEX, int SIG>
 __global__ void __launch_bounds__(kMlpGroups * 128, 1)
 k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __restrict__ keys,
             const float4* __restrict__ rec, t3_outputs out, int64_t npix, int32_t* __restrict__ status) {
@@ -147,12 +148,12 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
         store_rgb(fr, out, pix, pg.fg.color);  // a line pixel
       } else if (hit) {
         mine = true;
-        eval_mlp_coeffs<NL>(pg.ob->mat, pg.fg, q);
+        eval_mlp_coeffs<NL, TEX, SIG>(pg.ob->mat, pg.fg, q);
         if (lt.nlights > 0) {
           LobeState<NL> L;
           V3 amb, emi;
-          eval_material<NL>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
-          q.base = q.base + lamps_term<NL>(lt, L, pg.fg, pg.vdir);
+          eval_material<NL, TEX, SIG>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
+          q.base = q.base + lamps_term<NL, SIG>(lt, L, pg.fg, pg.vdir);
         }
         const float nv[6] = {pg.fg.normal.x, pg.fg.normal.y, pg.fg.normal.z, pg.vdir.x, pg.vdir.y, pg.vdir.z};
         mirror_inputs(nv, in);
@@ -187,11 +188,11 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
   group_cta_end(tmem_base);
 }
 
-template <int NL>
+template <int NL, bool TEX, int SIG>
 static cudaError_t launch_shade_mlp_t(const DevScene& sc, const unsigned long long* keys,
                                       const float4* rec, const t3_outputs& out, int64_t npix,
                                       int32_t* status, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_shade_mlp<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_shade_mlp<NL, TEX, SIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kMlpGroupSmem);
   if (e != cudaSuccess) return e;
   int dev = 0, nsm = 0;
@@ -202,15 +203,18 @@ static cudaError_t launch_shade_mlp_t(const DevScene& sc, const unsigned long lo
   const int64_t want = (nchunks + kMlpGroups - 1) / kMlpGroups;
   const int grid = (int)(want < nsm ? want : nsm);
   if (grid <= 0) return cudaSuccess;
-  k_shade_mlp<NL><<<grid, kMlpGroups * 128, kMlpGroupSmem, st>>>(sc, keys, rec, out, npix, status);
+  k_shade_mlp<NL, TEX, SIG><<<grid, kMlpGroups * 128, kMlpGroupSmem, st>>>(sc, keys, rec, out, npix, status);
   return cudaGetLastError();
 }
 
 cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                              const t3_outputs& out, int32_t* status, cudaStream_t st) {
   const int64_t npix = (int64_t)sc.frame.width * sc.frame.height;
-  if (max_lobes(sc) <= 2) return launch_shade_mlp_t<2>(sc, keys, rec, out, npix, status, st);
-  return launch_shade_mlp_t<4>(sc, keys, rec, out, npix, status, st);
+  // untextured PBR scenes take the instance with the lobe kinds as constants
+  if (!has_textures(sc) && lobe_signature(sc) == T3_SIG_PBR)
+    return launch_shade_mlp_t<2, false, T3_SIG_PBR>(sc, keys, rec, out, npix, status, st);
+  if (max_lobes(sc) <= 2) return launch_shade_mlp_t<2, true, 0>(sc, keys, rec, out, npix, status, st);
+  return launch_shade_mlp_t<4, true, 0>(sc, keys, rec, out, npix, status, st);
 }
 
 } // namespace t3
