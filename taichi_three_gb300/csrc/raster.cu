@@ -56,6 +56,7 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
                 unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold) {
   __shared__ __align__(16) float sv[BLOCK * 9];
   __shared__ WarpFaces wfs[BLOCK / 32];
+  __shared__ WarpCols wcs[BLOCK / 32];
   const int64_t f0 = (int64_t)blockIdx.x * BLOCK;
   const bool staged = stage_soup<BLOCK>(mesh, nfaces, f0, sv);
   const int64_t n = f0 + threadIdx.x;
@@ -87,8 +88,8 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
     }
   }
   GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
-  warp_raster(wfs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0, fr.width - 1, 0,
-              fr.height - 1, fr, sink);
+  warp_raster_spans(wfs[threadIdx.x >> 5], wcs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0,
+                    fr.width - 1, 0, fr.height - 1, fr, sink);
 }
 
 // Large faces: every CTA walks a slice of every queued face's bbox.

@@ -125,6 +125,186 @@ __device__ __forceinline__ void warp_raster(WarpFaces& wf, const Setup& s, bool 
   __syncwarp();
 }
 
+// ---- column-span walk ---------------------------------------------------------
+// The bbox walk above tests every pixel centre of a face's bbox; for the small
+// faces of a soup about 30 % of those tests pass.  Here the warp first computes,
+// for each column of each face's bbox, the rows whose centres can pass: each
+// edge function is linear along a column, so "w >= 0" bounds the row from one
+// side, and the bound is widened by a margin far above the rounding error of
+// the exact evaluation (below).  Only those candidates get the exact test, so
+// coverage is unchanged.
+//
+// Margin: the exact test computes w = (px - bx) * bcn.y - (py - by) * bcn.x in
+// FP32 (each operation rounded, |error| <= 3u (|px - bx| |bcn.y| + |py - by|
+// |bcn.x|), u = 2^-24) and the third weight as (1 - w_bc) - w_ca; a pixel passes
+// only if every weight is >= 0 (with positive clip-w reciprocals the division
+// by their sum keeps the signs, and the weights sum to 1, so not all can be
+// negative).  A row bound B = -A / k from the FP32 coefficients is off by at
+// most 4u |B| plus A's own rounding.  With N = 2 (dbx + dcx + hb + hc + |by| +
+// |cy| + 2) (|bcn| + |can|)_1 + 4 bounding every |w| term that enters, the
+// error in rows is below 3u N / |k| + 4u |B|; the margin taken is
+// 2^-18 (N / |k| + |B|) + 2^-20, over 20 times that.  Faces whose clip-w
+// reciprocals are not all positive and finite, or whose edge coefficients are
+// not finite, keep their whole columns.
+constexpr int kMaxWarpCols = 160;  // columns per warp walk (more: the bbox walk)
+
+struct WarpCols {
+  int2 col[kMaxWarpCols];  // non-empty columns: (x | face rank << 16, first row | first position << 15)
+};
+
+// rows [lo, hi] (within [y0, y1]) of column x whose centres can pass t's test
+__device__ __forceinline__ void column_rows(const Setup& t, int x, int y0, int y1, float biasx, float biasy,
+                                            int& lo, int& hi) {
+  lo = y0;
+  hi = y1;
+  const bool ok = t.wsa > 0.0f && t.wsb > 0.0f && t.wsc > 0.0f && t.wsa < INFINITY && t.wsb < INFINITY &&
+                  t.wsc < INFINITY;
+  const float S = fabsf(t.bcnx) + fabsf(t.bcny) + fabsf(t.canx) + fabsf(t.cany);
+  if (!ok || !(S < INFINITY)) return;  // also NaN
+  const float px = xadd((float)x, biasx);
+  const float ya = (float)y0 + biasy, yb = (float)y1 + biasy;
+  const float dbx = fabsf(px - t.bx), dcx = fabsf(px - t.cx);
+  const float hb = fmaxf(fabsf(ya - t.by), fabsf(yb - t.by)), hc = fmaxf(fabsf(ya - t.cy), fabsf(yb - t.cy));
+  const float N = 2.0f * (dbx + dcx + hb + hc + fabsf(t.by) + fabsf(t.cy) + 2.0f) * S + 4.0f;
+  // w(py) = A + k py for the edges bc, ca and ab
+  const float A1 = (px - t.bx) * t.bcny + t.by * t.bcnx, k1 = -t.bcnx;
+  const float A2 = (px - t.cx) * t.cany + t.cy * t.canx, k2 = -t.canx;
+  const float A3 = 1.0f - A1 - A2, k3 = t.bcnx + t.canx;
+  const float As[3] = {A1, A2, A3}, ks[3] = {k1, k2, k3};
+  const float flo = (float)y0 - 1.0f, fhi = (float)y1 + 1.0f;
+#pragma unroll
+  for (int e = 0; e < 3; e++) {
+    const float k = ks[e], ak = fabsf(k);
+    if (!(ak * 1048576.0f > S)) continue;  // nearly constant along the column: no bound
+    const float B = __fdividef(-As[e], k);
+    const float m = 3.814697265625e-06f * (__fdividef(N, ak) + fabsf(B)) + 9.5367431640625e-07f;
+    if (!(fabsf(B) < 1e30f) || !(m < 1e30f)) continue;
+    if (k > 0.0f) {
+      const float b = fminf(fmaxf(B - m - biasy, flo), fhi);
+      const int r = (int)ceilf(b);
+      lo = r > lo ? r : lo;
+    } else {
+      const float b = fminf(fmaxf(B + m - biasy, flo), fhi);
+      const int r = (int)floorf(b);
+      hi = r < hi ? r : hi;
+    }
+  }
+}
+
+// warp_raster over column spans: same interface and result; warps whose faces
+// have more than kMaxWarpCols columns in total take the bbox walk.
+template <class Sink>
+__device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, const Setup& s, bool active,
+                                                  uint32_t id, int cx0, int cx1, int cy0, int cy1,
+                                                  const t3_frame& fr, Sink sink) {
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  const int x0 = max(s.botx, cx0), x1 = min(s.topx, cx1);
+  const int y0 = max(s.boty, cy0), y1 = min(s.topy, cy1);
+  const int ncols = (active && x0 <= x1 && y0 <= y1) ? x1 - x0 + 1 : 0;
+  const unsigned live = __ballot_sync(FULL, ncols > 0);
+  if (!live) return;
+  int incl = ncols;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(FULL, incl, 31);
+  // candidate positions are packed in 17 bits: bboxes of up to 2^17 pixels per warp
+  const unsigned area = ncols > 0 ? min((unsigned)ncols * (unsigned)(y1 - y0 + 1), 1u << 20) : 0u;
+  if (total > kMaxWarpCols || __reduce_add_sync(FULL, area) >= (1u << 17)) {
+    warp_raster(wf, s, active, id, cx0, cx1, cy0, cy1, fr, sink);
+    return;
+  }
+  const int first = incl - ncols;  // this face's first column
+  if (ncols > 0) {
+    const int r = __popc(live & ((1u << lane) - 1u));
+    wf.rec[r][0] = make_float4(s.bx, s.by, s.cx, s.cy);
+    wf.rec[r][1] = make_float4(s.bcnx, s.bcny, s.canx, s.cany);
+    wf.rec[r][2] = make_float4(s.wsa, s.wsb, s.wsc, s.Az);
+    wf.rec[r][3] = make_float4(s.Bz, s.Cz, __int_as_float(x0 | (y0 << 16)), __uint_as_float(id));
+    wf.h[r] = y1 - y0 + 1;
+    wf.start[r] = first;
+  }
+  const unsigned upto = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+  const unsigned below = (1u << lane) - 1u;
+  const float biasx = fr.bias[0], biasy = fr.bias[1];
+  __syncwarp();
+  // 1. the candidate rows of every column; non-empty columns are listed in
+  // order with the position of their first candidate
+  int ncand = 0, npix = 0, before = 0;
+  for (int base = 0; base < total; base += 32) {
+    const unsigned bit = (ncols > 0 && first >= base && first < base + 32) ? 1u << (first - base) : 0u;
+    const unsigned starts = __reduce_or_sync(FULL, bit);
+    const int ci = base + lane;
+    int cnt = 0, rlo = 0, x = 0, j = 0;
+    if (ci < total) {
+      j = before + __popc(starts & upto) - 1;
+      const float4 r0 = wf.rec[j][0], r1 = wf.rec[j][1], r2 = wf.rec[j][2];
+      const int xy = __float_as_int(wf.rec[j][3].z);
+      Setup t;
+      t.bx = r0.x; t.by = r0.y; t.cx = r0.z; t.cy = r0.w;
+      t.bcnx = r1.x; t.bcny = r1.y; t.canx = r1.z; t.cany = r1.w;
+      t.wsa = r2.x; t.wsb = r2.y; t.wsc = r2.z;
+      x = (xy & 0xFFFF) + (ci - wf.start[j]);
+      const int fy0 = xy >> 16;
+      int rhi;
+      column_rows(t, x, fy0, fy0 + wf.h[j] - 1, biasx, biasy, rlo, rhi);
+      cnt = rhi >= rlo ? rhi - rlo + 1 : 0;
+    }
+    const unsigned m = __ballot_sync(FULL, cnt > 0);
+    int pre = cnt;  // positions: inclusive scan of the counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULL, pre, o);
+      if (lane >= o) pre += t;
+    }
+    if (cnt > 0) {
+      const int k = ncand + __popc(m & below);
+      wc.col[k] = make_int2(x | (j << 16), rlo | ((npix + pre - cnt) << 15));
+    }
+    ncand += __popc(m);
+    npix += __shfl_sync(FULL, pre, 31);
+    before += __popc(starts);
+  }
+  __syncwarp();
+  // 2. the candidates, 32 at a time: a candidate's column is the last one
+  // starting at or before it (found as in warp_raster, with the column starts
+  // held in registers, five per lane)
+  int cst[kMaxWarpCols / 32];
+#pragma unroll
+  for (int q = 0; q < kMaxWarpCols / 32; q++) {
+    const int k = lane + 32 * q;
+    cst[q] = k < ncand ? (int)((uint32_t)wc.col[k].y >> 15) : -1;
+  }
+  const float maxd = (float)fr.maxdepth;
+  int cbefore = 0;
+  for (int base = 0; base < npix; base += 32) {
+    unsigned bits = 0u;
+#pragma unroll
+    for (int q = 0; q < kMaxWarpCols / 32; q++)
+      if (cst[q] >= base && cst[q] < base + 32) bits |= 1u << (cst[q] - base);
+    const unsigned starts = __reduce_or_sync(FULL, bits);
+    const int idx = base + lane;
+    if (idx < npix) {
+      const int k = cbefore + __popc(starts & upto) - 1;
+      const int2 cd = wc.col[k];
+      const int j = (cd.x >> 16) & 31;
+      const int y = (cd.y & 0x7FFF) + (idx - (int)((uint32_t)cd.y >> 15));
+      const float4 r0 = wf.rec[j][0], r1 = wf.rec[j][1], r2 = wf.rec[j][2], r3 = wf.rec[j][3];
+      Setup t;
+      t.bx = r0.x; t.by = r0.y; t.cx = r0.z; t.cy = r0.w;
+      t.bcnx = r1.x; t.bcny = r1.y; t.canx = r1.z; t.cany = r1.w;
+      t.wsa = r2.x; t.wsb = r2.y; t.wsc = r2.z; t.Az = r2.w;
+      t.Bz = r3.x; t.Cz = r3.y;
+      test_pixel(t, cd.x & 0xFFFF, y, __float_as_uint(r3.w), biasx, biasy, maxd, fr.maxdepth, sink);
+    }
+    cbefore += __popc(starts);
+  }
+  __syncwarp();
+}
+
 // Loads (and transforms) the corners of face n; soup positions come from the
 // block's shared-memory staging area when `staged`.
 __device__ __forceinline__ void load_face(const t3_mesh& mesh, int64_t n, bool staged,
