@@ -71,6 +71,7 @@ __device__ __forceinline__ int find_scene(const BatchArgs& a, uint32_t g, bool s
 __global__ void __launch_bounds__(kBatchBlock, 4) k_batch_raster(const __grid_constant__ BatchArgs a) {
   __shared__ __align__(16) float sv[kBatchBlock * 9];
   __shared__ WarpFaces wfs[kBatchBlock / 32];
+  __shared__ WarpCols wcs[kBatchBlock / 32];
   __shared__ uint32_t s_item;
   __shared__ uint32_t s_big[kBigSlots];
   __shared__ int s_nbig;
@@ -116,7 +117,8 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_batch_raster(const __grid_co
           // beyond the slots the face stays in the warp walk (correct, slower)
         }
       }
-      warp_raster(wfs[threadIdx.x >> 5], st, vis, gid, 0, fr.width - 1, 0, fr.height - 1, fr, sink);
+      warp_raster_spans(wfs[threadIdx.x >> 5], wcs[threadIdx.x >> 5], st, vis, gid, 0, fr.width - 1, 0,
+                        fr.height - 1, fr, sink);
       __syncthreads();  // sv is restaged by the next pass
     }
     // big faces of this chunk: the whole CTA strides over each bbox

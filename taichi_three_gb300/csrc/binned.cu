@@ -123,6 +123,7 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw);  // TS*TS
   uint32_t* queue = reinterpret_cast<uint32_t*>(smem_raw + TS * TS * 8);        // capacity
   __shared__ WarpFaces wfs[BLOCK / 32];
+  __shared__ WarpCols wcs[BLOCK / 32];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_ok;
   __shared__ int s_list[TS * TS];
@@ -184,7 +185,7 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
         gid = queue[i];
         load_record(bins.rec, gid, s);
       }
-      warp_raster(wf, s, act, gid, x0, x1, y0, y1, fr, sink);
+      warp_raster_spans(wf, wcs[warp], s, act, gid, x0, x1, y0, y1, fr, sink);
     }
     // big faces overlapping the tile
     const uint32_t nbig = min(*bins.big_count, bins.big_capacity);
@@ -198,7 +199,7 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
         load_record(bins.rec, gid, s);
         act = !(s.botx > x1 || s.topx < x0 || s.boty > y1 || s.topy < y0);
       }
-      if (__ballot_sync(FULL, act)) warp_raster(wf, s, act, gid, x0, x1, y0, y1, fr, sink);
+      if (__ballot_sync(FULL, act)) warp_raster_spans(wf, wcs[warp], s, act, gid, x0, x1, y0, y1, fr, sink);
     }
   }
   __syncthreads();
