@@ -51,7 +51,7 @@ struct GlobalKeySink {
 };
 
 template <int BLOCK, bool COUNT>
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(BLOCK, 6)
 k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t face_base,
                 unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold) {
   __shared__ __align__(16) float sv[BLOCK * 9];

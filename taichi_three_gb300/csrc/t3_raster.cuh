@@ -211,9 +211,12 @@ __device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, c
     if (lane >= o) incl += t;
   }
   const int total = __shfl_sync(FULL, incl, 31);
-  // candidate positions are packed in 17 bits: bboxes of up to 2^17 pixels per warp
+  // candidate positions are packed in 17 bits: bboxes of up to 2^17 pixels per
+  // warp; columns averaging under three rows (faces of a pixel or two) gain
+  // nothing from the spans and take the bbox walk too
   const unsigned area = ncols > 0 ? min((unsigned)ncols * (unsigned)(y1 - y0 + 1), 1u << 20) : 0u;
-  if (total > kMaxWarpCols || __reduce_add_sync(FULL, area) >= (1u << 17)) {
+  const unsigned warp_area = __reduce_add_sync(FULL, area);
+  if (total > kMaxWarpCols || warp_area >= (1u << 17) || warp_area < 3u * (unsigned)total) {
     warp_raster(wf, s, active, id, cx0, cx1, cy0, cy1, fr, sink);
     return;
   }
