@@ -191,16 +191,30 @@ __device__ __forceinline__ bool inside_clip(f3 p) {
 }
 
 // The reference walks every pixel of [floor(min), ceil(max)] (triangle.py:108-114),
-// but a pixel whose centre c + 0.5 lies outside [min, max] by more than the
-// rounding error of the weights cannot pass the inside test: that error is a
-// few ulps of the viewport coordinates (|w| error <~ 2^-22 * (1 + |coord|)
-// in pixel units), far below the margin used here, 2^-16 * (2 + |coord| +
-// extent).  So only centres in [min - eps, max + eps] are tested, which halves
-// the pixel tests of small faces without changing which pixels are covered.
-__device__ __forceinline__ void tighten_to_centres(float lo, float hi, int32_t& bot, int32_t& top) {
+// but a pixel whose centre lies well outside [min, max] cannot pass the inside
+// test, so only centres in [min - eps, max + eps] are tested (about half the
+// pixel tests of small faces).  The bound, in terms of the setup's FP32
+// values: with positive clip-w reciprocals a pixel passes only if its three
+// computed weights are >= 0.  Each is the exact barycentric coordinate lambda_i
+// plus evaluation and coefficient rounding of at most 8u (T + 1) + 4u T, where
+// u = 2^-24 and T = (ext_x + ext_y + 4) (|bcn| + |can|)_1 bounds every product
+// in the weights over the walked range; the rounding of the face's doubled
+// area n adds at most 8u T to the third.  A centre with lambda_i >= -E lies
+// within E * extent of the corners' [min, max] (it is their affine
+// combination), so eps = 2^-18 (T + 1) (extent + 1), about three times the
+// bound, plus 2^-16 (2 + |coord| + extent) for the viewport coordinates'
+// own rounding.  T is large exactly where cancellation makes the weights
+// inaccurate: thin wedges with a far corner (a centre 0.4 px outside the
+// corners' range can pass there) keep nearly the reference's whole range.
+// Faces whose clip-w reciprocals are not all positive and finite accept
+// centres outside the corners' range and are not tightened.
+__device__ __forceinline__ void tighten_to_centres(float lo, float hi, float T, int32_t& bot, int32_t& top) {
   const float mag = fmaxf(fabsf(lo), fabsf(hi));
   if (!(mag < 16777216.0f)) return;  // also NaN / inf: keep the reference's range
-  const float eps = (2.0f + mag + (hi - lo)) * 1.52587890625e-05f;  // 2^-16
+  const float ext = hi - lo;
+  const float eps = (2.0f + mag + ext) * 1.52587890625e-05f +        // 2^-16
+                    (T + 1.0f) * (ext + 1.0f) * 3.814697265625e-06f;  // 2^-18
+  if (!(eps < 4.0f)) return;  // no centre of the range is excluded (also inf / NaN)
   const int32_t b = (int32_t)ceilf(lo - 0.5f - eps);
   const int32_t t = (int32_t)floorf(hi - 0.5f + eps);
   bot = b > bot ? b : bot;
@@ -239,8 +253,6 @@ __device__ __forceinline__ bool face_setup_ndc(const t3_frame& fr, float4 A4, fl
   s.boty = loy > 0 ? loy : 0;
   s.topx = hix < fr.width - 1 ? hix : fr.width - 1;
   s.topy = hiy < fr.height - 1 ? hiy : fr.height - 1;
-  tighten_to_centres(fminf(fminf(ax, bx), cx), fmaxf(fmaxf(ax, bx), cx), s.botx, s.topx);
-  tighten_to_centres(fminf(fminf(ay, by), cy), fmaxf(fmaxf(ay, by), cy), s.boty, s.topy);
   const float n = cross2_x(xsub(bx, ax), xsub(by, ay), xsub(cx, ax), xsub(cy, ay));
   s.bcnx = xdiv(xsub(bx, cx), n);
   s.bcny = xdiv(xsub(by, cy), n);
@@ -250,6 +262,15 @@ __device__ __forceinline__ bool face_setup_ndc(const t3_frame& fr, float4 A4, fl
   s.wsa = xrcp(wa);
   s.wsb = xrcp(wb);
   s.wsc = xrcp(wc);
+  if (s.wsa > 0.0f && s.wsb > 0.0f && s.wsc > 0.0f && s.wsa < INFINITY && s.wsb < INFINITY &&
+      s.wsc < INFINITY) {
+    const float lox_f = fminf(fminf(ax, bx), cx), hix_f = fmaxf(fmaxf(ax, bx), cx);
+    const float loy_f = fminf(fminf(ay, by), cy), hiy_f = fmaxf(fmaxf(ay, by), cy);
+    const float S = fabsf(s.bcnx) + fabsf(s.bcny) + fabsf(s.canx) + fabsf(s.cany);
+    const float T = ((hix_f - lox_f) + (hiy_f - loy_f) + 4.0f) * S;  // inf / NaN: no tightening
+    tighten_to_centres(lox_f, hix_f, T, s.botx, s.topx);
+    tighten_to_centres(loy_f, hiy_f, T, s.boty, s.topy);
+  }
   s.Az = Av.z; s.Bz = Bv.z; s.Cz = Cv.z;
   return true;
 }

@@ -1,0 +1,210 @@
+"""Raster edge cases aimed at the column-span walk (rows bounded per column by
+the edge functions, widened by a margin, then the exact test): face id, int32
+and float depth must stay bit-exact with the serial oracle where centres sit
+exactly on edges, edges are nearly parallel to the columns, coordinates are far
+off-screen, faces are slivers or degenerate, and corners lie behind the camera."""
+import numpy as np
+import pytest
+import torch
+
+import taichi_three_gb300 as tina
+
+
+
+def _ndc_scene(verts, res=(96, 64), **opts):
+    """Faces given directly in NDC (identity camera), so viewport coordinates
+    are chosen exactly."""
+    scene = tina.Scene(res[0], res[1], **opts)
+    mesh = tina.SimpleMesh()
+    mesh.set_face_verts(np.asarray(verts, np.float32))
+    scene.add_object(mesh)
+    return scene
+
+
+def _vp_to_ndc(px, py, res):
+    return 2.0 * px / res[0] - 1.0, 2.0 * py / res[1] - 1.0
+
+
+def _check(scene, oracle_mod):
+    scene.render()
+    torch.cuda.synchronize()
+    o = oracle_mod.render(scene)
+    fid = scene.face_id.cpu().numpy()
+    assert np.array_equal(fid, o['face_id']), np.argwhere(fid != o['face_id'])[:5].tolist()
+    assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
+    assert np.array_equal(scene.depth_f.cpu().numpy().view(np.uint32), o['depth_f'].view(np.uint32))
+    return fid
+
+
+@pytest.mark.gpu
+def test_edges_through_pixel_centres(cuda, oracle_mod):
+    # right triangles whose edges run exactly through rows / columns of centres,
+    # and diagonals through centres (weights exactly 0 on the boundary)
+    res = (96, 64)
+    faces = []
+    rng = np.random.default_rng(1)
+    for _ in range(300):
+        x0, y0 = rng.integers(0, 80) + 0.5, rng.integers(0, 50) + 0.5
+        w, h = rng.integers(1, 12), rng.integers(1, 12)
+        corners = [(x0, y0), (x0 + w, y0), (x0, y0 + h)] if rng.random() < 0.5 else \
+                  [(x0, y0), (x0 + w, y0 + w), (x0, y0 + h)]
+        z = rng.uniform(-0.9, 0.9)
+        tri = [[*_vp_to_ndc(px, py, res), z] for px, py in corners]
+        if rng.random() < 0.5:
+            tri = tri[::-1]
+        faces.append(tri)
+    scene = _ndc_scene(faces, res, culling=False)
+    fid = _check(scene, oracle_mod)
+    assert (fid >= 0).sum() > 1000
+
+
+@pytest.mark.gpu
+def test_near_vertical_and_horizontal_edges(cuda, oracle_mod):
+    # edges with slopes of 1e-7 .. 1e-2 against the pixel grid: their row
+    # bounds are ill-conditioned and must widen instead of cutting pixels
+    res = (128, 96)
+    rng = np.random.default_rng(2)
+    faces = []
+    for _ in range(400):
+        x0, y0 = rng.uniform(4, 110), rng.uniform(4, 80)
+        L = rng.uniform(2, 14)
+        eps = 10.0 ** rng.uniform(-7, -2)
+        if rng.random() < 0.5:
+            corners = [(x0, y0), (x0 + eps, y0 + L), (x0 + L, y0 + rng.uniform(-L, L))]
+        else:
+            corners = [(x0, y0), (x0 + L, y0 + eps), (x0 + rng.uniform(-L, L), y0 + L)]
+        z = rng.uniform(-0.9, 0.9, size=3)
+        faces.append([[*_vp_to_ndc(px, py, res), zz] for (px, py), zz in zip(corners, z)])
+    scene = _ndc_scene(faces, res, culling=False)
+    fid = _check(scene, oracle_mod)
+    assert (fid >= 0).sum() > 2000
+
+
+@pytest.mark.gpu
+def test_slivers_far_coordinates_and_degenerate(cuda, oracle_mod):
+    res = (160, 120)
+    rng = np.random.default_rng(3)
+    faces = []
+    for _ in range(200):  # slivers: two corners almost coincide
+        a = rng.uniform(-1, 1, 2)
+        b = a + rng.uniform(-0.3, 0.3, 2)
+        c = b + rng.normal(0, 1e-5, 2)
+        faces.append([[*a, 0.1], [*b, 0.2], [*c, 0.3]])
+    for _ in range(100):  # one corner far off-screen (viewport coordinates ~1e4)
+        a = rng.uniform(-0.9, 0.9, 2)
+        b = a + rng.uniform(-0.1, 0.1, 2)
+        c = rng.uniform(-150, 150, 2)
+        faces.append([[*a, 0.0], [*b, 0.1], [*c, 0.5]])
+    faces.append([[0.1, 0.1, 0.0], [0.1, 0.1, 0.0], [0.1, 0.1, 0.0]])  # a point
+    faces.append([[-0.5, -0.5, 0.0], [0.0, 0.0, 0.0], [0.5, 0.5, 0.0]])  # a segment
+    scene = _ndc_scene(faces, res, culling=False, clipping=False)
+    fid = _check(scene, oracle_mod)
+    assert (fid >= 0).sum() > 500
+
+
+def _one_face_at_a_time(scene, mesh, faces, oracle_mod):
+    """Renders each face alone (so no other face can win its pixels) and
+    returns how many covered at least one pixel."""
+    hits = 0
+    for f in faces:
+        mesh.set_face_verts(np.asarray(f, np.float32)[None])
+        fid = _check(scene, oracle_mod)
+        hits += bool((fid >= 0).any())
+    return hits
+
+
+@pytest.mark.gpu
+def test_wedges_with_a_far_corner_alone(cuda, oracle_mod):
+    # a short edge on screen and a corner 10^3..10^4 px away: the weights lose
+    # about |p - c| |c - a| / |ab| * 2^-23 px to cancellation, so centres up to
+    # ~1 px outside the corners' range can pass
+    rng = np.random.default_rng(5)
+    faces = []
+    for _ in range(60):
+        a = rng.uniform(-0.9, 0.9, 2)
+        faces.append([[*a, 0.1], [*(a + rng.uniform(-0.1, 0.1, 2)), 0.2], [*rng.uniform(-150, 150, 2), 0.3]])
+    scene = _ndc_scene(faces[:1], (160, 120), culling=False, clipping=False)
+    assert _one_face_at_a_time(scene, list(scene.objects)[0], faces, oracle_mod) > 30
+
+
+@pytest.mark.gpu
+def test_corners_behind_the_camera(cuda, oracle_mod):
+    # clip w of mixed sign: the accepted region is not bounded by the corners'
+    # viewport range, so such faces keep the reference's whole range
+    rng = np.random.default_rng(4)
+    v = rng.uniform(-1.5, 1.5, size=(300, 3, 3)).astype(np.float32)
+    v[:, :, 2] *= 2.5  # the camera sits at z = 3: some corners lie behind it
+    scene = tina.Scene(128, 96, culling=False, clipping=False)
+    mesh = tina.SimpleMesh()
+    mesh.set_face_verts(v)
+    scene.add_object(mesh)
+    scene.engine.set_camera(tina.lookat(back=(0, 0, 3)), tina.perspective(60, 128 / 96))
+    fid = _check(scene, oracle_mod)
+    assert (fid >= 0).sum() > 1000
+    # the faces with a corner behind the camera, one at a time
+    behind = [f for f in v if (f[:, 2] > 3.0).any() and (f[:, 2] < 3.0).any()][:60]
+    assert _one_face_at_a_time(scene, mesh, behind, oracle_mod) > 30
+
+
+def _vp32(c, res):
+    f32 = np.float32
+    return f32(f32(f32(f32(c) * f32(0.5)) + f32(0.5)) * f32(res))
+
+
+def _trimmed(lo, hi, T):
+    """The setup's range of tested centres (t3_device.cuh tighten_to_centres),
+    None where it keeps the reference's range."""
+    f32 = np.float32
+    mag = max(abs(lo), abs(hi))
+    ext = f32(hi - lo)
+    if not mag < 16777216:
+        return None
+    eps = f32(f32((2 + mag + ext) * f32(2.0 ** -16)) + f32(f32(T + 1) * f32(ext + 1) * f32(2.0 ** -18)))
+    if not eps < 4:
+        return None
+    return int(np.ceil(f32(f32(lo - f32(0.5)) - eps))), int(np.floor(f32(f32(hi - f32(0.5)) + eps)))
+
+
+@pytest.mark.parametrize('seed', [7, 8])
+def test_trimmed_range_holds_every_covered_centre(oracle_mod, seed):
+    """The bound that narrows the walked range to centres near the corners'
+    [min, max], restated in float32, against the oracle's coverage of single
+    faces: wedges with a far corner, slivers, long thin wedges, random faces
+    (identity camera, so every clip w is 1)."""
+    f32 = np.float32
+    W, H = 160, 120
+    rng = np.random.default_rng(seed)
+    scene = tina.Scene(W, H, culling=False, clipping=False)
+    mesh = tina.SimpleMesh()
+    mesh.set_face_verts(np.zeros((1, 3, 3), np.float32))
+    scene.add_object(mesh)
+    checked = 0
+    for it in range(400):
+        a = rng.uniform(-0.9, 0.9, 2)
+        kind = it % 4
+        if kind == 0:
+            b, c = a + rng.uniform(-0.1, 0.1, 2), rng.uniform(-150, 150, 2)
+        elif kind == 1:
+            b = a + rng.uniform(-1, 1, 2)
+            c = b + rng.normal(0, 10 ** rng.uniform(-7, -3), 2)
+        elif kind == 2:
+            b, c = a + rng.normal(0, 0.01, 2), a + rng.uniform(-8, 8, 2)
+        else:
+            b, c = rng.uniform(-1.2, 1.2, 2), rng.uniform(-1.2, 1.2, 2)
+        v = np.array([[*a, 0.1], [*b, 0.2], [*c, 0.3]], np.float32)
+        mesh.set_face_verts(v[None])
+        pts = np.argwhere(oracle_mod.render(scene)['face_id'] == 0)
+        if not len(pts):
+            continue
+        (ax, bx, cx), (ay, by, cy) = [_vp32(v[k, 0], W) for k in range(3)], [_vp32(v[k, 1], H) for k in range(3)]
+        with np.errstate(all='ignore'):
+            n = f32(f32(f32(bx - ax) * f32(cy - ay)) - f32(f32(by - ay) * f32(cx - ax)))
+            S = f32(abs(f32(f32(bx - cx) / n)) + abs(f32(f32(by - cy) / n)) +
+                    abs(f32(f32(cx - ax) / n)) + abs(f32(f32(cy - ay) / n)))
+            T = f32(f32(f32(max(ax, bx, cx) - min(ax, bx, cx)) + f32(max(ay, by, cy) - min(ay, by, cy)) + 4) * S)
+        for axis, lo, hi in ((0, min(ax, bx, cx), max(ax, bx, cx)), (1, min(ay, by, cy), max(ay, by, cy))):
+            r = _trimmed(lo, hi, T)
+            if r is not None:
+                assert pts[:, axis].min() >= r[0] and pts[:, axis].max() <= r[1], (it, axis, r, v.tolist())
+        checked += 1
+    assert checked > 250
