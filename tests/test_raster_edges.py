@@ -1,17 +1,21 @@
-"""Raster edge cases aimed at the column-span walk (rows bounded per column by
-the edge functions, widened by a margin, then the exact test): face id, int32
-and float depth must stay bit-exact with the serial oracle where centres sit
-exactly on edges, edges are nearly parallel to the columns, coordinates are far
-off-screen, faces are slivers or degenerate, and corners lie behind the camera."""
+"""Raster edge cases: face id, int32 and float depth stay bit-exact with the
+serial oracle where centres sit exactly on edges, edges are nearly parallel to
+the pixel grid, faces are slivers, points or segments, corners lie ~10^4 px
+off-screen or behind the camera.  These aim at what narrows the pixel tests
+below the reference's bbox walk: the column-span walk (rows bounded per column
+by the edge functions plus a margin) and the trimming of the walked range to
+centres near the corners' [min, max].  Each scene runs through the direct and
+binned rasters and the batched multi-view launch; faces whose pixels other
+faces might win are also rendered one at a time."""
 import numpy as np
 import pytest
-import torch
 
 import taichi_three_gb300 as tina
 
+RASTERS = ['direct', 'binned']
 
 
-def _ndc_scene(verts, res=(96, 64), **opts):
+def _ndc_scene(verts, res, **opts):
     """Faces given directly in NDC (identity camera), so viewport coordinates
     are chosen exactly."""
     scene = tina.Scene(res[0], res[1], **opts)
@@ -25,21 +29,9 @@ def _vp_to_ndc(px, py, res):
     return 2.0 * px / res[0] - 1.0, 2.0 * py / res[1] - 1.0
 
 
-def _check(scene, oracle_mod):
-    scene.render()
-    torch.cuda.synchronize()
-    o = oracle_mod.render(scene)
-    fid = scene.face_id.cpu().numpy()
-    assert np.array_equal(fid, o['face_id']), np.argwhere(fid != o['face_id'])[:5].tolist()
-    assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
-    assert np.array_equal(scene.depth_f.cpu().numpy().view(np.uint32), o['depth_f'].view(np.uint32))
-    return fid
-
-
-@pytest.mark.gpu
-def test_edges_through_pixel_centres(cuda, oracle_mod):
-    # right triangles whose edges run exactly through rows / columns of centres,
-    # and diagonals through centres (weights exactly 0 on the boundary)
+def centres_scene(**opts):
+    """Right triangles whose edges run exactly through rows / columns of
+    centres, and diagonals through centres (weights exactly 0 there)."""
     res = (96, 64)
     faces = []
     rng = np.random.default_rng(1)
@@ -53,15 +45,12 @@ def test_edges_through_pixel_centres(cuda, oracle_mod):
         if rng.random() < 0.5:
             tri = tri[::-1]
         faces.append(tri)
-    scene = _ndc_scene(faces, res, culling=False)
-    fid = _check(scene, oracle_mod)
-    assert (fid >= 0).sum() > 1000
+    return _ndc_scene(faces, res, culling=False, **opts), 1000
 
 
-@pytest.mark.gpu
-def test_near_vertical_and_horizontal_edges(cuda, oracle_mod):
-    # edges with slopes of 1e-7 .. 1e-2 against the pixel grid: their row
-    # bounds are ill-conditioned and must widen instead of cutting pixels
+def near_axis_scene(**opts):
+    """Edges with slopes of 1e-7 .. 1e-2 against the pixel grid: their row
+    bounds are ill-conditioned and must widen instead of cutting pixels."""
     res = (128, 96)
     rng = np.random.default_rng(2)
     faces = []
@@ -75,31 +64,79 @@ def test_near_vertical_and_horizontal_edges(cuda, oracle_mod):
             corners = [(x0, y0), (x0 + L, y0 + eps), (x0 + rng.uniform(-L, L), y0 + L)]
         z = rng.uniform(-0.9, 0.9, size=3)
         faces.append([[*_vp_to_ndc(px, py, res), zz] for (px, py), zz in zip(corners, z)])
-    scene = _ndc_scene(faces, res, culling=False)
-    fid = _check(scene, oracle_mod)
-    assert (fid >= 0).sum() > 2000
+    return _ndc_scene(faces, res, culling=False, **opts), 2000
 
 
-@pytest.mark.gpu
-def test_slivers_far_coordinates_and_degenerate(cuda, oracle_mod):
-    res = (160, 120)
+def far_scene(**opts):
+    """Slivers (two corners almost coincide), wedges with one corner ~10^4 px
+    off-screen, a point face and a segment face."""
     rng = np.random.default_rng(3)
     faces = []
-    for _ in range(200):  # slivers: two corners almost coincide
+    for _ in range(200):
         a = rng.uniform(-1, 1, 2)
         b = a + rng.uniform(-0.3, 0.3, 2)
         c = b + rng.normal(0, 1e-5, 2)
         faces.append([[*a, 0.1], [*b, 0.2], [*c, 0.3]])
-    for _ in range(100):  # one corner far off-screen (viewport coordinates ~1e4)
+    for _ in range(100):
         a = rng.uniform(-0.9, 0.9, 2)
         b = a + rng.uniform(-0.1, 0.1, 2)
         c = rng.uniform(-150, 150, 2)
         faces.append([[*a, 0.0], [*b, 0.1], [*c, 0.5]])
-    faces.append([[0.1, 0.1, 0.0], [0.1, 0.1, 0.0], [0.1, 0.1, 0.0]])  # a point
-    faces.append([[-0.5, -0.5, 0.0], [0.0, 0.0, 0.0], [0.5, 0.5, 0.0]])  # a segment
-    scene = _ndc_scene(faces, res, culling=False, clipping=False)
+    faces.append([[0.1, 0.1, 0.0], [0.1, 0.1, 0.0], [0.1, 0.1, 0.0]])
+    faces.append([[-0.5, -0.5, 0.0], [0.0, 0.0, 0.0], [0.5, 0.5, 0.0]])
+    return _ndc_scene(faces, (160, 120), culling=False, clipping=False, **opts), 500
+
+
+def behind_scene(**opts):
+    """Random faces around a perspective camera at z = 3, some with corners
+    behind it (clip w of mixed sign)."""
+    rng = np.random.default_rng(4)
+    v = rng.uniform(-1.5, 1.5, size=(300, 3, 3)).astype(np.float32)
+    v[:, :, 2] *= 2.5
+    scene = tina.Scene(128, 96, culling=False, clipping=False, **opts)
+    mesh = tina.SimpleMesh()
+    mesh.set_face_verts(v)
+    scene.add_object(mesh)
+    scene.engine.set_camera(tina.lookat(back=(0, 0, 3)), tina.perspective(60, 128 / 96))
+    return scene, 1000
+
+
+SCENES = [centres_scene, near_axis_scene, far_scene, behind_scene]
+
+
+def _compare(scene, oracle_mod):
+    import torch
+    torch.cuda.synchronize()
+    o = oracle_mod.render(scene)
+    fid = scene.face_id.cpu().numpy()
+    assert np.array_equal(fid, o['face_id']), np.argwhere(fid != o['face_id'])[:5].tolist()
+    assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
+    assert np.array_equal(scene.depth_f.cpu().numpy().view(np.uint32), o['depth_f'].view(np.uint32))
+    return fid
+
+
+def _check(scene, oracle_mod):
+    scene.render()
+    return _compare(scene, oracle_mod)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('raster', RASTERS)
+@pytest.mark.parametrize('make', SCENES, ids=lambda f: f.__name__)
+def test_edge_scene(cuda, oracle_mod, make, raster):
+    scene, min_cover = make(raster=raster)
     fid = _check(scene, oracle_mod)
-    assert (fid >= 0).sum() > 500
+    assert (fid >= 0).sum() > min_cover
+
+
+@pytest.mark.gpu
+def test_edge_scenes_batched(cuda, oracle_mod):
+    built = [make() for make in SCENES]
+    b = tina.BatchRenderer([s for s, _ in built])
+    b.render()
+    assert b.status() == 0
+    for scene, min_cover in built:
+        assert (_compare(scene, oracle_mod) >= 0).sum() > min_cover
 
 
 def _one_face_at_a_time(scene, mesh, faces, oracle_mod):
@@ -114,7 +151,8 @@ def _one_face_at_a_time(scene, mesh, faces, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_wedges_with_a_far_corner_alone(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', RASTERS)
+def test_wedges_with_a_far_corner_alone(cuda, oracle_mod, raster):
     # a short edge on screen and a corner 10^3..10^4 px away: the weights lose
     # about |p - c| |c - a| / |ab| * 2^-23 px to cancellation, so centres up to
     # ~1 px outside the corners' range can pass
@@ -123,25 +161,18 @@ def test_wedges_with_a_far_corner_alone(cuda, oracle_mod):
     for _ in range(60):
         a = rng.uniform(-0.9, 0.9, 2)
         faces.append([[*a, 0.1], [*(a + rng.uniform(-0.1, 0.1, 2)), 0.2], [*rng.uniform(-150, 150, 2), 0.3]])
-    scene = _ndc_scene(faces[:1], (160, 120), culling=False, clipping=False)
+    scene = _ndc_scene(faces[:1], (160, 120), culling=False, clipping=False, raster=raster)
     assert _one_face_at_a_time(scene, list(scene.objects)[0], faces, oracle_mod) > 30
 
 
 @pytest.mark.gpu
-def test_corners_behind_the_camera(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', RASTERS)
+def test_corners_behind_the_camera_alone(cuda, oracle_mod, raster):
     # clip w of mixed sign: the accepted region is not bounded by the corners'
     # viewport range, so such faces keep the reference's whole range
-    rng = np.random.default_rng(4)
-    v = rng.uniform(-1.5, 1.5, size=(300, 3, 3)).astype(np.float32)
-    v[:, :, 2] *= 2.5  # the camera sits at z = 3: some corners lie behind it
-    scene = tina.Scene(128, 96, culling=False, clipping=False)
-    mesh = tina.SimpleMesh()
-    mesh.set_face_verts(v)
-    scene.add_object(mesh)
-    scene.engine.set_camera(tina.lookat(back=(0, 0, 3)), tina.perspective(60, 128 / 96))
-    fid = _check(scene, oracle_mod)
-    assert (fid >= 0).sum() > 1000
-    # the faces with a corner behind the camera, one at a time
+    scene, _ = behind_scene(raster=raster)
+    mesh = list(scene.objects)[0]
+    v = mesh.verts.cpu().numpy()
     behind = [f for f in v if (f[:, 2] > 3.0).any() and (f[:, 2] < 3.0).any()][:60]
     assert _one_face_at_a_time(scene, mesh, behind, oracle_mod) > 30
 
@@ -208,3 +239,10 @@ def test_trimmed_range_holds_every_covered_centre(oracle_mod, seed):
                 assert pts[:, axis].min() >= r[0] and pts[:, axis].max() <= r[1], (it, axis, r, v.tolist())
         checked += 1
     assert checked > 250
+
+
+def test_edge_scenes_cover_on_the_oracle(oracle_mod):
+    """The GPU cases' coverage floors hold on the oracle (no GPU needed)."""
+    for make in SCENES:
+        scene, min_cover = make()
+        assert (oracle_mod.render(scene)['face_id'] >= 0).sum() > min_cover, make.__name__
