@@ -7,6 +7,8 @@ by the edge functions plus a margin) and the trimming of the walked range to
 centres near the corners' [min, max].  Each scene runs through the direct and
 binned rasters and the batched multi-view launch; faces whose pixels other
 faces might win are also rendered one at a time."""
+import os
+
 import numpy as np
 import pytest
 
@@ -196,12 +198,80 @@ def _trimmed(lo, hi, T):
     return int(np.ceil(f32(f32(lo - f32(0.5)) - eps))), int(np.floor(f32(f32(hi - f32(0.5)) + eps)))
 
 
+def _column_rows(t, x, y0, y1):
+    """Candidate rows [lo, hi] of column x (t3_raster.cuh column_rows) in
+    float32, with exact divisions where the kernel divides approximately (the
+    margin's 2^-18 |B| term covers the difference)."""
+    f32 = np.float32
+    lo, hi = y0, y1
+    S = f32(abs(t['bcnx']) + abs(t['bcny']) + abs(t['canx']) + abs(t['cany']))
+    if not S < np.inf:
+        return lo, hi
+    bias = f32(0.5)
+    px = f32(f32(x) + bias)
+    ya, yb = f32(f32(y0) + bias), f32(f32(y1) + bias)
+    dbx, dcx = abs(f32(px - t['bx'])), abs(f32(px - t['cx']))
+    hb = max(abs(f32(ya - t['by'])), abs(f32(yb - t['by'])))
+    hc = max(abs(f32(ya - t['cy'])), abs(f32(yb - t['cy'])))
+    N = f32(f32(2) * f32(dbx + dcx + hb + hc + abs(t['by']) + abs(t['cy']) + f32(2)) * S + f32(4))
+    A1 = f32(f32(f32(px - t['bx']) * t['bcny']) + f32(t['by'] * t['bcnx']))
+    A2 = f32(f32(f32(px - t['cx']) * t['cany']) + f32(t['cy'] * t['canx']))
+    A3 = f32(f32(f32(1) - A1) - A2)
+    flo, fhi = f32(y0 - 1), f32(y1 + 1)
+    for A, k in ((A1, f32(-t['bcnx'])), (A2, f32(-t['canx'])), (A3, f32(t['bcnx'] + t['canx']))):
+        ak = abs(k)
+        if not f32(ak * f32(1048576)) > S:
+            continue
+        B = f32(-A / k)
+        m = f32(f32(f32(2.0 ** -18) * f32(f32(N / ak) + abs(B))) + f32(2.0 ** -20))
+        if not (abs(B) < 1e30 and m < 1e30):
+            continue
+        if k > 0:
+            lo = max(lo, int(np.ceil(min(max(f32(f32(B - m) - bias), flo), fhi))))
+        else:
+            hi = min(hi, int(np.floor(min(max(f32(f32(B + m) - bias), flo), fhi))))
+    return lo, hi
+
+
+def _adversarial_faces(rng, n, W, H):
+    """Single faces in NDC (z 0.1 / 0.2 / 0.3): wedges with a far corner,
+    slivers, long thin wedges, edges within 1e-8..1e-2 of the pixel axes,
+    right triangles with edges through pixel centres, random faces."""
+    for it in range(n):
+        kind = it % 6
+        a = rng.uniform(-0.9, 0.9, 2)
+        if kind == 0:
+            b, c = a + rng.uniform(-0.1, 0.1, 2), rng.uniform(-150, 150, 2)
+        elif kind == 1:
+            b = a + rng.uniform(-1, 1, 2)
+            c = b + rng.normal(0, 10 ** rng.uniform(-7, -3), 2)
+        elif kind == 2:
+            b, c = a + rng.normal(0, 0.01, 2), a + rng.uniform(-8, 8, 2)
+        elif kind == 3:
+            L, e = rng.uniform(0.02, 0.2), 10 ** rng.uniform(-8, -2)
+            if rng.random() < 0.5:
+                b, c = a + [e, L], a + [L, rng.uniform(-L, L)]
+            else:
+                b, c = a + [L, e], a + [rng.uniform(-L, L), L]
+        elif kind == 4:
+            a = np.array([(rng.integers(0, W - 10) + 0.5) / W * 2 - 1, (rng.integers(0, H - 10) + 0.5) / H * 2 - 1])
+            b, c = a + [rng.integers(1, 12) / W * 2, 0], a + [0, rng.integers(1, 12) / H * 2]
+        else:
+            b, c = rng.uniform(-1.2, 1.2, 2), rng.uniform(-1.2, 1.2, 2)
+        yield np.array([[*a, 0.1], [*b, 0.2], [*c, 0.3]], np.float32)
+
+
+# faces per seed; T3_SWEEP_FACES=20000 runs the large sweep
+SWEEP_FACES = int(os.environ.get('T3_SWEEP_FACES', '600'))
+
+
 @pytest.mark.parametrize('seed', [7, 8])
-def test_trimmed_range_holds_every_covered_centre(oracle_mod, seed):
-    """The bound that narrows the walked range to centres near the corners'
-    [min, max], restated in float32, against the oracle's coverage of single
-    faces: wedges with a far corner, slivers, long thin wedges, random faces
-    (identity camera, so every clip w is 1)."""
+def test_narrowed_walks_hold_every_covered_centre(oracle_mod, seed):
+    """The two bounds that narrow the pixel tests below the reference's bbox
+    walk, restated in float32, against the oracle's coverage of single
+    adversarial faces (identity camera, so every clip w is 1): the trimming of
+    the walked range to centres near the corners' [min, max], and the
+    column-span walk's candidate rows within that range."""
     f32 = np.float32
     W, H = 160, 120
     rng = np.random.default_rng(seed)
@@ -210,35 +280,32 @@ def test_trimmed_range_holds_every_covered_centre(oracle_mod, seed):
     mesh.set_face_verts(np.zeros((1, 3, 3), np.float32))
     scene.add_object(mesh)
     checked = 0
-    for it in range(400):
-        a = rng.uniform(-0.9, 0.9, 2)
-        kind = it % 4
-        if kind == 0:
-            b, c = a + rng.uniform(-0.1, 0.1, 2), rng.uniform(-150, 150, 2)
-        elif kind == 1:
-            b = a + rng.uniform(-1, 1, 2)
-            c = b + rng.normal(0, 10 ** rng.uniform(-7, -3), 2)
-        elif kind == 2:
-            b, c = a + rng.normal(0, 0.01, 2), a + rng.uniform(-8, 8, 2)
-        else:
-            b, c = rng.uniform(-1.2, 1.2, 2), rng.uniform(-1.2, 1.2, 2)
-        v = np.array([[*a, 0.1], [*b, 0.2], [*c, 0.3]], np.float32)
+    for v in _adversarial_faces(rng, SWEEP_FACES, W, H):
         mesh.set_face_verts(v[None])
         pts = np.argwhere(oracle_mod.render(scene)['face_id'] == 0)
         if not len(pts):
             continue
         (ax, bx, cx), (ay, by, cy) = [_vp32(v[k, 0], W) for k in range(3)], [_vp32(v[k, 1], H) for k in range(3)]
+        lx, hx, ly, hy = min(ax, bx, cx), max(ax, bx, cx), min(ay, by, cy), max(ay, by, cy)
         with np.errstate(all='ignore'):
             n = f32(f32(f32(bx - ax) * f32(cy - ay)) - f32(f32(by - ay) * f32(cx - ax)))
-            S = f32(abs(f32(f32(bx - cx) / n)) + abs(f32(f32(by - cy) / n)) +
-                    abs(f32(f32(cx - ax) / n)) + abs(f32(f32(cy - ay) / n)))
-            T = f32(f32(f32(max(ax, bx, cx) - min(ax, bx, cx)) + f32(max(ay, by, cy) - min(ay, by, cy)) + 4) * S)
-        for axis, lo, hi in ((0, min(ax, bx, cx), max(ax, bx, cx)), (1, min(ay, by, cy), max(ay, by, cy))):
-            r = _trimmed(lo, hi, T)
-            if r is not None:
-                assert pts[:, axis].min() >= r[0] and pts[:, axis].max() <= r[1], (it, axis, r, v.tolist())
+            t = dict(bx=bx, by=by, cx=cx, cy=cy, bcnx=f32(f32(bx - cx) / n), bcny=f32(f32(by - cy) / n),
+                     canx=f32(f32(cx - ax) / n), cany=f32(f32(cy - ay) / n))
+            S = f32(abs(t['bcnx']) + abs(t['bcny']) + abs(t['canx']) + abs(t['cany']))
+            T = f32(f32(f32(hx - lx) + f32(hy - ly) + 4) * S)
+            rng_x, rng_y = _trimmed(lx, hx, T), _trimmed(ly, hy, T)
+            for axis, r in ((0, rng_x), (1, rng_y)):
+                if r is not None:
+                    assert pts[:, axis].min() >= r[0] and pts[:, axis].max() <= r[1], (axis, r, v.tolist())
+            y0, y1 = max(int(np.floor(ly)), 0), min(int(np.ceil(hy)), H - 1)
+            if rng_y is not None:
+                y0, y1 = max(y0, rng_y[0]), min(y1, rng_y[1])
+            for x in np.unique(pts[:, 0]):
+                ys = pts[pts[:, 0] == x, 1]
+                lo, hi = _column_rows(t, int(x), y0, y1)
+                assert lo <= ys.min() and ys.max() <= hi, (int(x), lo, hi, ys.min(), ys.max(), v.tolist())
         checked += 1
-    assert checked > 250
+    assert checked > SWEEP_FACES // 2
 
 
 def test_edge_scenes_cover_on_the_oracle(oracle_mod):
