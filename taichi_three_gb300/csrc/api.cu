@@ -283,8 +283,9 @@ static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capaci
   if (mode == T3_RASTER_BINNED) {
     L.bins = after_rec;
     L.end = align256(L.bins + 4 * (size_t)L.tiles_x * L.tiles_y * L.bin_capacity);
-    if (sc.lighting.mode == T3_LIGHT_IBL_MLP) {
-      // the tiles hand their keys to the fused network shading pass
+    if (sc.lighting.mode == T3_LIGHT_IBL_MLP || has_points_or_lines(sc)) {
+      // particle and line fragments seed the tiles' keys; the tiles hand their
+      // keys to the fused network shading pass
       L.keys = L.end;
       L.end = align256(L.keys + 8 * (size_t)sc.frame.width * (size_t)sc.frame.height);
     }
@@ -452,7 +453,6 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess)
       e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st);
   } else {
-    if (has_points_or_lines(*scene)) return T3_EUNSUPPORTED;  // particles and lines: direct path only
     if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
@@ -471,9 +471,22 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     b.light_mode = ds.lighting.mode;
     b.keys = ds.lighting.mode == T3_LIGHT_IBL_MLP ? reinterpret_cast<unsigned long long*>(ws + L.keys)
                                                   : nullptr;
+    b.pre = nullptr;
     if (e == cudaSuccess) e = mark(1);
+    if (has_points_or_lines(*scene)) {
+      // particles and lines take the direct rasterisers into the frame's keys,
+      // which then seed the tiles (every fragment is an order-independent
+      // minimum, so the result equals the direct path's)
+      unsigned long long* gk = reinterpret_cast<unsigned long long*>(ws + L.keys);
+      const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
+      if (e == cudaSuccess) e = launch_clear(gk, npix, st, nullptr, 0, nullptr);
+      for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++)
+        if (is_point_or_line(scene->objects[o].mesh))
+          e = launch_raster_point_or_line(scene->frame, scene->objects[o], gk, nullptr, st);
+      b.pre = gk;
+    }
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++)
-      e = launch_bin(scene->frame, scene->objects[o], b, st);
+      if (!is_point_or_line(scene->objects[o].mesh)) e = launch_bin(scene->frame, scene->objects[o], b, st);
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
     if (e == cudaSuccess && b.keys)

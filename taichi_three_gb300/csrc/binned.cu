@@ -145,7 +145,12 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar_a), "r"(1) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = threadIdx.x; i < TS * TS; i += BLOCK) keys[i] = T3_EMPTY_KEY;
+  for (int i = threadIdx.x; i < TS * TS; i += BLOCK) {
+    unsigned long long k = T3_EMPTY_KEY;
+    const int x = x0 + i / TS, y = y0 + i % TS;
+    if (bins.pre && x <= x1 && y <= y1) k = bins.pre[(int64_t)x * H + y];
+    keys[i] = k;
+  }
   __syncthreads();
   // stage this tile's bin with one bulk copy: 16-byte multiples from the
   // 16-byte aligned start of a capacity-sized bin (capacity % 4 == 0)

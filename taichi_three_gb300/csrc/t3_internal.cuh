@@ -41,6 +41,9 @@ struct BinArgs {
   int32_t max_lobes;     // largest flattened material of the scene
   int32_t light_mode;    // T3_LIGHT_*
   unsigned long long* keys;  // T3_LIGHT_IBL_MLP: the frame's packed keys, written by the tiles
+  // the frame's particle and line fragments (packed keys, rasterised before the
+  // tiles), which seed each tile's keys; nullptr when the scene has none
+  const unsigned long long* pre;
 };
 
 // A material tree flattened into a sum of weighted leaf lobes:

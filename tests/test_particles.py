@@ -44,7 +44,8 @@ def _render_both(scene, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_particles_parity(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_particles_parity(cuda, oracle_mod, raster):
     pos, rad, col = _pars(400, 1)
     pars = tina.SimpleParticles()
     pars.set_particles(pos)
@@ -53,12 +54,14 @@ def test_particles_parity(cuda, oracle_mod):
     scene = tina.Scene(160, 120)
     scene.add_object(pars)  # default material: Diffuse(color=Input('color'))
     scene.engine.set_camera(tina.lookat(back=(0.5, 0.4, 3)), tina.perspective(60, 160 / 120))
+    scene.raster_mode = raster
     fid = _render_both(scene, oracle_mod)
     assert len(np.unique(fid[fid >= 0])) > 100
 
 
 @pytest.mark.gpu
-def test_particles_with_triangles_and_pbr(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_particles_with_triangles_and_pbr(cuda, oracle_mod, raster):
     arrays = tina.workloads.soup_arrays(3000, 4, median_sigma=0.08, log_sd=0.6)
     scene, _ = tina.workloads.soup_scene(ntri=3000, res=(128, 96), seed=4, nlights=3, arrays=arrays)
     pos, rad, col = _pars(200, 2, 0.03, 0.1)
@@ -67,6 +70,7 @@ def test_particles_with_triangles_and_pbr(cuda, oracle_mod):
     pars.set_particle_radii(rad)
     pars.set_particle_colors(col)
     scene.add_object(pars, tina.PBR(basecolor='color', metallic=0.4, roughness=0.3))
+    scene.raster_mode = raster
     fid = _render_both(scene, oracle_mod)
     assert (fid >= 3000).sum() > 300 and ((fid >= 0) & (fid < 3000)).sum() > 300
 

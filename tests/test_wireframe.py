@@ -73,11 +73,13 @@ def _render_both(scene, oracle_mod, mode=0):
 
 
 @pytest.mark.gpu
-def test_wireframe_over_soup(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_wireframe_over_soup(cuda, oracle_mod, raster):
     arrays = tina.workloads.soup_arrays(4000, 5, median_sigma=0.06, log_sd=0.6)
     scene, mesh = tina.workloads.soup_scene(ntri=4000, res=(200, 150), seed=5, nlights=2, arrays=arrays)
     wire = tina.MeshToWire(mesh)
     scene.add_object(wire)
+    scene.raster_mode = raster
     fid = _render_both(scene, oracle_mod)
     assert (fid >= 4000).sum() > 2000 and ((fid >= 0) & (fid < 4000)).sum() > 2000
 
@@ -99,7 +101,8 @@ def test_lines_clipping_and_far_endpoints(cuda, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_wire_of_edited_and_indexed_meshes(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_wire_of_edited_and_indexed_meshes(cuda, oracle_mod, raster):
     # MeshToWire over MeshNoCulling (doubled faces, odd copies reversed), over
     # an indexed mesh, over a grid, and a transform outside a line soup
     verts, _, _ = tina.workloads.soup_arrays(300, 7, median_sigma=0.1)
@@ -122,6 +125,7 @@ def test_wire_of_edited_and_indexed_meshes(cuda, oracle_mod):
     scene.add_object(tina.MeshToWire(lines))
     scene.add_object(grid)
     scene.engine.set_camera(tina.lookat(back=(0.3, 0.4, 2.6)), tina.perspective(60, 160 / 120))
+    scene.raster_mode = raster
     fid = _render_both(scene, oracle_mod)
     sc, _ = scene.describe()
     bases = [sc.objects[o].face_base for o in range(sc.nobjects)] + [2 ** 31]
@@ -130,11 +134,13 @@ def test_wire_of_edited_and_indexed_meshes(cuda, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_wires_under_ibl(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_wires_under_ibl(cuda, oracle_mod, raster):
     # lines under the skybox lighting keep their colour; the sky fills the rest
     scene, mesh = tina.workloads.ibl_soup_scene(ntri=500, res=(96, 72), seed=9, env_res=32, spp=8,
                                                 arrays=tina.workloads.soup_arrays(500, 9, median_sigma=0.1))
     scene.add_object(tina.MeshToWire(mesh))
+    scene.raster_mode = raster
     _render_both(scene, oracle_mod, mode=1)
 
 
@@ -155,10 +161,11 @@ def test_wires_large_property(cuda, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_wires_binned_unsupported(cuda):
+def test_wires_batched_unsupported(cuda):
+    # the batched multi-view launch takes triangle scenes only
     lines = tina.SimpleMesh(npolygon=2)
     lines.set_face_verts(_lines(10, 11))
-    scene = tina.Scene(64, raster='binned')
+    scene = tina.Scene(64)
     scene.add_object(lines)
     with pytest.raises(RuntimeError):
-        scene.render()
+        tina.BatchRenderer([scene]).render()
