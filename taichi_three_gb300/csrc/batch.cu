@@ -16,6 +16,8 @@
 //
 // Faces whose bbox exceeds kBigArea pixels are kept out of the warps' walk and
 // rasterised by the whole CTA after its chunk (a CTA-wide stride over the bbox).
+// Particle and line objects take no raster items: the direct particle and
+// line rasterisers write their fragments into the views' keys after the clear.
 #include "t3_raster.cuh"
 #include "t3_shading.cuh"
 
@@ -261,8 +263,6 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
     r = make_dev_scene(scenes[s], ds);
     if (r) return r;
     if (ds.lighting.mode != T3_LIGHT_LAMPS) return T3_EUNSUPPORTED;
-    for (int o = 0; o < scenes[s].nobjects; o++)
-      if (is_point_or_line(scenes[s].objects[o].mesh)) return T3_EUNSUPPORTED;
     if (!outs[s].rgb) return T3_EINVAL;
     nl = max_lobes(ds) > nl ? max_lobes(ds) : nl;
     textured = textured || has_textures(ds) != 0;
@@ -281,7 +281,10 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
     v.raster_item0 = item;
     for (int o = 0; o < scenes[s].nobjects; o++) {
       a.obj_item0[s][o] = item;
-      item += (uint32_t)((scenes[s].objects[o].nfaces + c.faces_per_item - 1) / c.faces_per_item);
+      // particles and lines take no raster items: their own rasterisers run
+      // after the clear (an object without items is skipped by the item search)
+      if (!is_point_or_line(scenes[s].objects[o].mesh))
+        item += (uint32_t)((scenes[s].objects[o].nfaces + c.faces_per_item - 1) / c.faces_per_item);
     }
     for (int o = scenes[s].nobjects; o <= T3_MAX_OBJECTS; o++) a.obj_item0[s][o] = item;
     v.raster_items = item - v.raster_item0;
@@ -296,6 +299,13 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   }
   a.n_items = a.n_raster + sitem;
   e = launch_clear(reinterpret_cast<unsigned long long*>(ws + L.keys[0]), L.total_pix, st);
+  // particles and lines: the direct rasterisers into their view's keys (every
+  // fragment is an order-independent packed minimum, so it does not matter
+  // that the triangles' persistent launch comes after)
+  for (int s = 0; s < nscenes && e == cudaSuccess; s++)
+    for (int o = 0; o < scenes[s].nobjects && e == cudaSuccess; o++)
+      if (is_point_or_line(scenes[s].objects[o].mesh))
+        e = launch_raster_point_or_line(scenes[s].frame, scenes[s].objects[o], a.v[s].keys, nullptr, st);
   if (e != cudaSuccess) return T3_ECUDA;
   int dev = 0, nsm = 0, occ_r = 0, occ_s = 0;
   e = cudaGetDevice(&dev);

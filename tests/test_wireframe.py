@@ -161,11 +161,37 @@ def test_wires_large_property(cuda, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_wires_batched_unsupported(cuda):
-    # the batched multi-view launch takes triangle scenes only
+def test_wires_and_particles_batched(cuda, oracle_mod):
+    # one batched launch over a soup with its wireframe, a line soup and a
+    # particle scene: each view against the oracle at the parity bar
+    arrays = tina.workloads.soup_arrays(2000, 12, median_sigma=0.08, log_sd=0.6)
+    soup, mesh = tina.workloads.soup_scene(ntri=2000, res=(128, 96), seed=12, nlights=2, arrays=arrays)
+    soup.add_object(tina.MeshToWire(mesh))
     lines = tina.SimpleMesh(npolygon=2)
-    lines.set_face_verts(_lines(10, 11))
-    scene = tina.Scene(64)
-    scene.add_object(lines)
-    with pytest.raises(RuntimeError):
-        tina.BatchRenderer([scene]).render()
+    lines.set_face_verts(_lines(400, 13))
+    wires = tina.Scene(96, 80, linecolor=(0.2, 0.9, 0.4))
+    wires.add_object(lines)
+    wires.engine.set_camera(tina.lookat(back=(0.2, 0.1, 3)), tina.perspective(60, 96 / 80))
+    rng = np.random.default_rng(14)
+    pars = tina.SimpleParticles()
+    pars.set_particles(rng.uniform(-1, 1, (300, 3)).astype(np.float32))
+    pars.set_particle_radii(rng.uniform(0.03, 0.12, 300).astype(np.float32))
+    pars.set_particle_colors(rng.uniform(0.2, 1, (300, 3)).astype(np.float32))
+    balls = tina.Scene(100, 90)
+    balls.add_object(pars)
+    balls.engine.set_camera(tina.lookat(back=(0.3, 0.2, 3)), tina.perspective(60, 100 / 90))
+    views = [soup, wires, balls]
+    b = tina.BatchRenderer(views)
+    b.render()
+    assert b.status() == 0
+    for scene in views:
+        torch.cuda.synchronize()
+        o = oracle_mod.render(scene)
+        fid = scene.face_id.cpu().numpy()
+        assert np.array_equal(fid, o['face_id'])
+        assert np.array_equal(scene.engine.depth.cpu().numpy(), o['depth'])
+        assert np.array_equal(scene.depth_f.cpu().numpy().view(np.uint32), o['depth_f'].view(np.uint32))
+        assert np.abs(scene.img.cpu().numpy() - o['rgb']).max() <= 1e-4
+        assert (fid >= 0).sum() > 1000
+    fid = soup.face_id.cpu().numpy()
+    assert (fid >= 2000).sum() > 500 and ((fid >= 0) & (fid < 2000)).sum() > 500
