@@ -80,9 +80,16 @@ typedef struct t3_frame {
 #define T3_MESH_WIREFRAME 32  /* MeshToWire           tina/mesh/wire.py:5-40:
                                  the object is the polygon edges of the mesh as
                                  lines: line n = corners (n % p, (n+1) % p) of
-                                 face n / p, p = 3 (2 for T3_MESH_LINES), over
-                                 the faces after the other edits (NOCULL doubles
-                                 them); object nfaces = lines; direct raster only */
+                                 face n / p, p = 3 (4 for T3_MESH_QUADS, 2 for
+                                 T3_MESH_LINES), over the faces after the other
+                                 edits (NOCULL doubles them); object nfaces =
+                                 lines */
+#define T3_MESH_QUADS 64      /* MeshGrid(as_quad=True) tina/mesh/grid.py:23-58:
+                                 face f of a T3_MESH_GRID is cell f's quad
+                                 (a, b, c, d) = ((i,j), (i+1,j), (i+1,j+1),
+                                 (i,j+1)); nfaces = (n-1)^2.  Only drawn through
+                                 T3_MESH_WIREFRAME (with T3_MESH_TRANSFORM at
+                                 most): a quad is not a triangle raster's face */
 
 typedef struct t3_mesh {
   int32_t kind;        /* T3_MESH_*                                              */

@@ -838,6 +838,25 @@ template <class R> void wire_endpoints(const t3_mesh& m, int64_t n, v3<R>& A, v3
     B = c[(e + 1) % 2];
     return;
   }
+  if (m.flags & T3_MESH_QUADS) {
+    // MeshGrid(as_quad=True) (grid.py:46-58): _get_face_props returns the
+    // cell's (a, b, c, d) = ((i,j), (i+1,j), (i+1,j+1), (i,j+1))
+    const int64_t f = n / 4, stride = m.grid_nx - 1;
+    const int64_t i = f / stride, j = f % stride;
+    const int64_t ii[4] = {i, i + 1, i + 1, i}, jj[4] = {j, j, j + 1, j + 1};
+    v3<R> c[4];
+    for (int k = 0; k < 4; k++) {
+      c[k] = ld3<R>(m.verts + (ii[k] * m.grid_ny + jj[k]) * 3);
+      if (m.flags & T3_MESH_TRANSFORM) {
+        mat4<R> T;
+        for (int q = 0; q < 16; q++) T.m[q] = (R)m.trans[q];
+        c[k] = mapply_pos(T, c[k]);
+      }
+    }
+    A = c[n % 4];
+    B = c[(n + 1) % 4];
+    return;
+  }
   Mesh<R> mesh(&m);
   v3<R> v[3];
   mesh.verts(n / 3, v);

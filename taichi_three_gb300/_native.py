@@ -36,6 +36,7 @@ T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED, T3_MESH_PARTICLES, T3_MESH_LINES = 
 T3_MESH_TRANSFORM, T3_MESH_NOCULL, T3_MESH_FLIP_ORDER, T3_MESH_FLIP_NORMAL, T3_MESH_FLAT_NORMAL = \
     1, 2, 4, 8, 16
 T3_MESH_WIREFRAME = 32
+T3_MESH_QUADS = 64
 
 T3_OP_CONST, T3_OP_ATTR, T3_OP_INPUT, T3_OP_FRESNEL, T3_OP_TEXTURE, T3_OP_CHECKER = 0, 1, 2, 3, 4, 5
 T3_OP_LAMBERT, T3_OP_PHONG, T3_OP_COOK, T3_OP_EMISSION = 16, 17, 18, 19

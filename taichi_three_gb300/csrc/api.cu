@@ -120,9 +120,15 @@ static int check_mesh(const t3_mesh& m, int flags, int64_t nfaces) {
     if (m.flags & ~(T3_MESH_TRANSFORM | T3_MESH_WIREFRAME)) return T3_EINVAL;
     return nfaces <= m.nfaces * ((m.flags & T3_MESH_WIREFRAME) ? 2 : 1) ? T3_OK : T3_EINVAL;
   }
+  if (m.flags & T3_MESH_QUADS) {
+    // MeshGrid(as_quad=True): drawn only as MeshToWire's lines, under MeshTransform at most
+    if (m.kind != T3_MESH_GRID || !(m.flags & T3_MESH_WIREFRAME)) return T3_EUNSUPPORTED;
+    if (m.flags & ~(T3_MESH_QUADS | T3_MESH_TRANSFORM | T3_MESH_WIREFRAME)) return T3_EUNSUPPORTED;
+  }
   if (m.flags & T3_MESH_WIREFRAME) {
-    // MeshToWire: three lines per face of the (NOCULL-doubled) mesh
-    if (nfaces > m.nfaces * ((m.flags & T3_MESH_NOCULL) ? 2 : 1) * 3) return T3_EINVAL;
+    // MeshToWire: three lines per face of the (NOCULL-doubled) mesh, four per quad
+    const int64_t per = (m.flags & T3_MESH_QUADS) ? 4 : 3;
+    if (nfaces > m.nfaces * ((m.flags & T3_MESH_NOCULL) ? 2 : 1) * per) return T3_EINVAL;
     flags &= ~(T3_SMOOTHING | T3_TEXTURING);  // lines read positions only
   }
   if ((flags & T3_SMOOTHING) && !(m.flags & T3_MESH_FLAT_NORMAL) && !m.norms) return T3_EINVAL;

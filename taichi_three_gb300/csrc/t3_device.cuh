@@ -413,6 +413,23 @@ __device__ __forceinline__ void wire_endpoints(const t3_mesh& d, int64_t n, f3& 
     B = swap ? p0 : p1;
     return;
   }
+  if (d.flags & T3_MESH_QUADS) {
+    // MeshGrid(as_quad=True) (grid.py:46-58): quad f = cell f's corners
+    // a=(i,j) b=(i+1,j) c=(i+1,j+1) d=(i,j+1); line n joins corners n % 4 and (n + 1) % 4
+    const int64_t f = n >> 2;
+    const int e = (int)(n & 3);
+    const int64_t stride = (int64_t)d.grid_nx - 1;
+    const int64_t i = f / stride, j = f - i * stride;
+    auto corner = [&](int c) {
+      const int64_t ii = i + (c == 1 || c == 2 ? 1 : 0), jj = j + (c >= 2 ? 1 : 0);
+      f3 p = ld3(d.verts + (ii * d.grid_ny + jj) * 3);
+      if (d.flags & T3_MESH_TRANSFORM) p = mapply_pos_x(d.trans, p);
+      return p;
+    };
+    A = corner(e);
+    B = corner((e + 1) & 3);
+    return;
+  }
   const int64_t f = n / 3;
   const int e = (int)(n - f * 3);
   f3 v[3];

@@ -195,12 +195,12 @@ class PrimitiveMesh(SimpleMesh):
 
 class MeshGrid(MeshBase):
     """Parametric grid (tina/mesh/grid.py): pos/nrm/tex [n, n, 3|2]; two
-    triangles per quad; `pre_compute` (run by every render) recomputes the
-    smooth normals on the device."""
+    triangles per cell, or with `as_quad=True` one quad per cell (drawn only
+    through MeshToWire: four lines per quad); `pre_compute` (run by every
+    render) recomputes the smooth normals on the device."""
 
     def __init__(self, res, as_quad=False):
-        if as_quad:
-            raise NotImplementedError('quad grids are not rasterised by this build')
+        self.as_quad = bool(as_quad)
         if isinstance(res, int):
             res = res, res
         if res[0] != res[1]:
@@ -220,8 +220,12 @@ class MeshGrid(MeshBase):
         self.nrm = torch.zeros((nx, ny, 3), dtype=torch.float32, device=dev)
         self.auto_normals = True
 
+    def get_npolygon(self):
+        return 4 if self.as_quad else 3
+
     def get_nfaces(self):
-        return (self.res[0] - 1) * (self.res[1] - 1) * 2
+        n = (self.res[0] - 1) * (self.res[1] - 1)
+        return n if self.as_quad else n * 2
 
     def displace_wave(self, t, amp=0.1, fx=8.0, fy=8.0, wx=1.0, wy=1.3):
         """pos.z = amp sin(fx x + wx t) cos(fy y + wy t) on the device (the
@@ -247,6 +251,8 @@ class MeshGrid(MeshBase):
         m.norms = ptr(self.nrm, device, keep)
         m.coors = ptr(self.tex, device, keep)
         m.grid_nx, m.grid_ny = self.res
+        if self.as_quad:
+            m.flags |= N.T3_MESH_QUADS
         self._fill_attr(m, device, keep)
 
 
@@ -373,7 +379,9 @@ class MeshEditBase:
         self.mesh.pre_compute()
 
     def _check_inner(self, m, forbidden):
-        if m.flags & forbidden:
+        # T3_MESH_QUADS describes the base grid, not an edit (the library
+        # checks which edits may wrap it)
+        if m.flags & forbidden & ~N.T3_MESH_QUADS:
             raise NotImplementedError(
                 f'{type(self).__name__} around this mesh-edit chain is not supported; nest edits as '
                 'MeshNoCulling(MeshFlipNormal(MeshFlipCulling(MeshFlatNormal(MeshTransform(mesh)))))')

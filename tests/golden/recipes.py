@@ -71,6 +71,14 @@ def inputs(name):
         x, y = np.meshgrid(u * 2 - 1, u * 2 - 1, indexing='ij')
         pos = np.stack([x, y, 0.2 * np.cos(2 * x) * np.sin(3 * y + 0.3)], -1).astype(np.float32)
         return {'pos': pos}
+    if name == 'wire_quads':
+        u = np.linspace(0, 1, 6)
+        x, y = np.meshgrid(u * 2 - 1, u * 2 - 1, indexing='ij')
+        pos = np.stack([x * 1.1, y * 0.9, 0.25 + 0.15 * np.sin(2 * x + 0.4) * np.cos(3 * y)], -1)
+        u2 = np.linspace(0, 1, 9)
+        x2, y2 = np.meshgrid(u2 * 2 - 1, u2 * 2 - 1, indexing='ij')
+        pos2 = np.stack([x2, y2, 0.1 * np.cos(3 * x2) * np.sin(2 * y2 + 0.2)], -1)
+        return {'pos': pos.astype(np.float32), 'pos2': pos2.astype(np.float32)}
     if name == 'smooth_model':
         return {'v': _bumpy_sphere(41)[0], 'f': _bumpy_sphere(41)[1],
                 'v2': _bumpy_sphere(42, nlat=6, nlon=9)[0], 'f2': _bumpy_sphere(42, nlat=6, nlon=9)[1]}
@@ -108,7 +116,8 @@ def _obj(v, f):
 
 
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
-         'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid', 'smooth_model']
+         'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid', 'smooth_model',
+         'wire_quads']
 
 
 def build(tina, name, arrays, matrix):
@@ -233,6 +242,17 @@ def build(tina, name, arrays, matrix):
         scene.add_object(tina.MeshToWire(grid))
         scene.add_object(grid, tina.PBR(metallic=0.3, roughness=0.4))
         scene.engine.set_camera(matrix.lookat(back=(0.3, -1.2, 2.2)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'wire_quads':
+        # a quad grid's wireframe (four lines per cell) over a triangle grid
+        scene = tina.Scene(48, 36, smoothing=True, linecolor=(0.3, 0.8, 1.0))
+        quads = tina.MeshGrid(6, as_quad=True)
+        _set_grid(quads, arrays['pos'])
+        scene.add_object(tina.MeshToWire(quads))
+        surface = tina.MeshGrid(9)
+        _set_grid(surface, arrays['pos2'])
+        scene.add_object(surface, tina.Classic())
+        scene.engine.set_camera(matrix.lookat(back=(0.2, -1.0, 2.4)), matrix.perspective(60, 48 / 36))
         return scene, False
     if name == 'smooth_model':
         scene = tina.Scene(48, 36, smoothing=True)

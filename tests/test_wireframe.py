@@ -46,6 +46,21 @@ def test_describe_wires():
         tina.MeshNoCulling(tina.MeshToWire(mesh))._t3_fill(N.t3_mesh(), 'cpu', [])
 
 
+
+def test_describe_quad_grid_wires():
+    # MeshGrid(as_quad=True) (grid.py:23-44): one quad per cell, four lines each under MeshToWire
+    quads = tina.MeshGrid(5, as_quad=True)
+    assert quads.get_npolygon() == 4 and quads.get_nfaces() == 16
+    assert tina.MeshGrid(5).get_nfaces() == 32
+    wire = tina.MeshToWire(tina.MeshTransform(quads, tina.translate([0, 0, 0.2])))
+    assert wire.get_npolygon() == 2 and wire.get_nfaces() == 64
+    scene = tina.Scene(32)
+    scene.add_object(wire)
+    sc, _ = scene.describe('cpu')
+    m = sc.objects[0].mesh
+    assert m.kind == N.T3_MESH_GRID and sc.objects[0].nfaces == 64 and m.nfaces == 16
+    assert m.flags == N.T3_MESH_QUADS | N.T3_MESH_TRANSFORM | N.T3_MESH_WIREFRAME
+
 def test_default_wire_options():
     scene = tina.Scene(16)
     lines = tina.SimpleMesh(npolygon=2)
@@ -195,3 +210,27 @@ def test_wires_and_particles_batched(cuda, oracle_mod):
         assert (fid >= 0).sum() > 1000
     fid = soup.face_id.cpu().numpy()
     assert (fid >= 2000).sum() > 500 and ((fid >= 0) & (fid < 2000)).sum() > 500
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_quad_grid_wires(cuda, oracle_mod, raster):
+    grid = tina.MeshGrid(12, as_quad=True)
+    p = grid.pos.cpu().numpy()
+    p[..., 2] = 0.2 * np.sin(3 * p[..., 0] + 0.3) * np.cos(2 * p[..., 1])
+    grid.pos.copy_(torch.from_numpy(p).to(grid.pos.device))
+    surface = tina.MeshGrid(16)
+    scene = tina.Scene(150, 110, smoothing=True)
+    scene.add_object(tina.MeshToWire(tina.MeshTransform(grid, tina.translate([0.1, 0.0, 0.15]))))
+    scene.add_object(surface, tina.Classic())
+    scene.engine.set_camera(tina.lookat(back=(0.3, -1.1, 2.3)), tina.perspective(60, 150 / 110))
+    scene.raster_mode = raster
+    fid = _render_both(scene, oracle_mod)
+    nlines = 11 * 11 * 4
+    wires = fid[(fid >= 0) & (fid < nlines)]
+    assert len(wires) > 1000 and set((wires % 4).tolist()) == {0, 1, 2, 3}
+    # a quad is not a face of the triangle raster
+    bad = tina.Scene(32)
+    bad.add_object(tina.MeshGrid(4, as_quad=True))
+    with pytest.raises(RuntimeError):
+        bad.render()
