@@ -66,10 +66,10 @@ typedef struct t3_frame {
 #define T3_MESH_PARTICLES 3 /* SimpleParticles (tina/pars/simple.py) for ParticleRaster
                                (tina/core/particle.py): nfaces = particles,
                                verts = positions [n,3], coors = radii [n],
-                               norms = colours [n,3] (nullptr: white); direct raster only */
+                               norms = colours [n,3] (nullptr: white)                    */
 #define T3_MESH_LINES 4   /* SimpleMesh(npolygon=2) (tina/mesh/simple.py): verts [n,2,3];
                              drawn by the wireframe rasteriser (tina/core/wireframe.py);
-                             direct raster only, flags: TRANSFORM, WIREFRAME            */
+                             flags: TRANSFORM, WIREFRAME                                */
 
 /* mesh flags (mesh-edit nodes) */
 #define T3_MESH_TRANSFORM 1   /* MeshTransform        tina/mesh/trans.py:23-40 */

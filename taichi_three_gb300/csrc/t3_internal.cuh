@@ -96,7 +96,8 @@ cudaError_t launch_raster_particles(const t3_frame& fr, const t3_object& ob, uns
                                     unsigned long long* fragments, cudaStream_t st);
 cudaError_t launch_raster_wires(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                 unsigned long long* fragments, cudaStream_t st);
-// objects of the particle and wireframe rasterisers (direct path only)
+// objects of the particle and wireframe rasterisers (their own direct kernels
+// write the frame's keys in every raster mode)
 inline bool is_point_or_line(const t3_mesh& m) {
   return m.kind == T3_MESH_PARTICLES || m.kind == T3_MESH_LINES || (m.flags & T3_MESH_WIREFRAME) != 0;
 }
