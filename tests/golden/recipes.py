@@ -79,6 +79,15 @@ def inputs(name):
         x2, y2 = np.meshgrid(u2 * 2 - 1, u2 * 2 - 1, indexing='ij')
         pos2 = np.stack([x2, y2, 0.1 * np.cos(3 * x2) * np.sin(2 * y2 + 0.2)], -1)
         return {'pos': pos.astype(np.float32), 'pos2': pos2.astype(np.float32)}
+    if name == 'textured':
+        verts, norms = _soup(60, 31, sigma=0.35)
+        rng = np.random.Generator(np.random.PCG64(32))
+        coors = rng.uniform(0.03, 0.97, size=(60, 3, 2)).astype(np.float32)
+        image = rng.uniform(0.0, 1.0, size=(8, 6, 3)).astype(np.float32)
+        v2, n2 = _soup(50, 33, sigma=0.35)
+        c2 = rng.uniform(0.03, 0.97, size=(50, 3, 2)).astype(np.float32)
+        return {'verts': verts, 'norms': norms, 'coors': coors, 'image': image,
+                'verts2': v2, 'norms2': n2, 'coors2': c2}
     if name == 'smooth_model':
         return {'v': _bumpy_sphere(41)[0], 'f': _bumpy_sphere(41)[1],
                 'v2': _bumpy_sphere(42, nlat=6, nlon=9)[0], 'f2': _bumpy_sphere(42, nlat=6, nlon=9)[1]}
@@ -117,7 +126,7 @@ def _obj(v, f):
 
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
          'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid', 'smooth_model',
-         'wire_quads']
+         'wire_quads', 'textured']
 
 
 def build(tina, name, arrays, matrix):
@@ -253,6 +262,23 @@ def build(tina, name, arrays, matrix):
         _set_grid(surface, arrays['pos2'])
         scene.add_object(surface, tina.Classic())
         scene.engine.set_camera(matrix.lookat(back=(0.2, -1.0, 2.4)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'textured':
+        # an image texture (bilinear at texcoord * (shape - 1)) and a
+        # chessboard, both read at interpolated texcoords inside (0, 1)
+        scene = tina.Scene(48, 36, smoothing=True, texturing=True)
+        mesh = tina.SimpleMesh()
+        mesh.set_face_verts(arrays['verts'])
+        mesh.set_face_norms(arrays['norms'])
+        mesh.set_face_coors(arrays['coors'])
+        scene.add_object(mesh, tina.Diffuse(color=tina.Texture(arrays['image'])))
+        board = tina.SimpleMesh()
+        board.set_face_verts(arrays['verts2'])
+        board.set_face_norms(arrays['norms2'])
+        board.set_face_coors(arrays['coors2'])
+        checker = tina.ChessboardTexture(size=0.2, color0=0.2, color1=[0.9, 0.5, 0.1])
+        scene.add_object(board, tina.PBR(basecolor=checker, metallic=0.2, roughness=0.45))
+        scene.engine.set_camera(matrix.lookat(back=(0.2, 0.3, 3)), matrix.perspective(60, 48 / 36))
         return scene, False
     if name == 'smooth_model':
         scene = tina.Scene(48, 36, smoothing=True)
