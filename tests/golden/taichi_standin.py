@@ -546,6 +546,11 @@ class _FieldElement(Matrix):
 
 
 class Field:
+    # Taichi leaves a read outside a field undefined; with clamp_reads set, an
+    # out-of-range index reads the nearest element (the convention the build
+    # under test documents for its post-processing passes)
+    clamp_reads = False
+
     def __init__(self, shape, dtype, elem=None):
         if isinstance(shape, int):
             shape = (shape,)
@@ -575,6 +580,8 @@ class Field:
 
     def __getitem__(self, key):
         k = self._key(key)
+        if Field.clamp_reads and len(k) == len(self.shape):
+            k = tuple(min(max(i, 0), n - 1) for i, n in zip(k, self.shape))
         if self.elem is None:
             v = self.data[k]
             return np.float32(v) if self.data.dtype == np.float32 else int(v)
