@@ -59,10 +59,10 @@ def load_reference():
 
 
 def main():
-    from recipes import NAMES, build, inputs
+    from recipes import NAMES, ORACLE_NAMES, build, inputs
     tina, matrix = load_reference()
     only = sys.argv[1:]
-    for name in NAMES:
+    for name in NAMES + ORACLE_NAMES:
         if only and name not in only:
             continue
         t0 = time.time()

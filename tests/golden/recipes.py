@@ -88,6 +88,13 @@ def inputs(name):
         c2 = rng.uniform(0.03, 0.97, size=(50, 3, 2)).astype(np.float32)
         return {'verts': verts, 'norms': norms, 'coors': coors, 'image': image,
                 'verts2': v2, 'norms2': n2, 'coors2': c2}
+    if name == 'materials':
+        out = {}
+        for k in range(6):
+            v, n = _soup(40, 71 + k, spread=0.5, sigma=0.3)
+            out[f'verts{k}'] = v + np.float32([(k % 3) * 0.7 - 0.7, (k // 3) * 0.8 - 0.4, 0.0])
+            out[f'norms{k}'] = n
+        return out
     if name == 'smooth_model':
         return {'v': _bumpy_sphere(41)[0], 'f': _bumpy_sphere(41)[1],
                 'v2': _bumpy_sphere(42, nlat=6, nlon=9)[0], 'f2': _bumpy_sphere(42, nlat=6, nlon=9)[1]}
@@ -127,6 +134,11 @@ def _obj(v, f):
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
          'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid', 'smooth_model',
          'wire_quads', 'textured']
+
+
+# golden scenes checked against the oracle only (the CUDA path is held to the
+# oracle on the same materials by tests/test_gpu_parity.py test_material_variants)
+ORACLE_NAMES = ['materials']
 
 
 def build(tina, name, arrays, matrix):
@@ -279,6 +291,24 @@ def build(tina, name, arrays, matrix):
         checker = tina.ChessboardTexture(size=0.2, color0=0.2, color1=[0.9, 0.5, 0.1])
         scene.add_object(board, tina.PBR(basecolor=checker, metallic=0.2, roughness=0.45))
         scene.engine.set_camera(matrix.lookat(back=(0.2, 0.3, 3)), matrix.perspective(60, 48 / 36))
+        return scene, False
+    if name == 'materials':
+        # every material composition: Lambert, Phong, CookTorrance alone, an
+        # AddMaterial with Emission, a Mix by an Input, PBR by an Input
+        scene = tina.Scene(64, 48, smoothing=True)
+        mats = [tina.Lambert(), tina.Phong(shineness=12.5), tina.CookTorrance(roughness=0.3, fresnel=0.5),
+                tina.Lambert() * [0.2, 0.4, 0.6] + tina.Emission() * 0.1,
+                tina.MixMaterial(tina.Lambert(), tina.Phong(shineness=8), tina.Input('normal')),
+                tina.PBR(basecolor=tina.Input('pos'), metallic=0.5, roughness=0.6)]
+        for k, mat in enumerate(mats):
+            mesh = tina.SimpleMesh()
+            mesh.set_face_verts(arrays[f'verts{k}'])
+            mesh.set_face_norms(arrays[f'norms{k}'])
+            scene.add_object(mesh, mat)
+        scene.lighting.set_ambient_light([0.05, 0.1, 0.02])
+        scene.lighting.add_light(dir=[0.2, -1, 0.5], color=[0.5, 0.5, 0.5])
+        scene.lighting.add_light(pos=[0.5, 0.8, 1.5], color=[0.8, 0.7, 0.6])
+        scene.engine.set_camera(matrix.lookat(back=(0.1, 0.2, 3.2)), matrix.perspective(60, 64 / 48))
         return scene, False
     if name == 'smooth_model':
         scene = tina.Scene(48, 36, smoothing=True)

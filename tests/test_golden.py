@@ -42,7 +42,7 @@ def check(name, out, gold, scene, single):
     return err
 
 
-@pytest.mark.parametrize('name', recipes.NAMES)
+@pytest.mark.parametrize('name', recipes.NAMES + recipes.ORACLE_NAMES)
 def test_oracle_matches_reference_golden(oracle_mod, name):
     arrays, gold = load(name)
     scene, single = recipes.build(tina, name, arrays, tina)
