@@ -95,6 +95,10 @@ def inputs(name):
             out[f'verts{k}'] = v + np.float32([(k % 3) * 0.7 - 0.7, (k // 3) * 0.8 - 0.4, 0.0])
             out[f'norms{k}'] = n
         return out
+    if name == 'mesh_edits':
+        verts, norms = _soup(120, 81, spread=0.7, sigma=0.3)
+        v2, n2 = _soup(80, 82, spread=0.6, sigma=0.3)
+        return {'verts': verts, 'norms': norms, 'verts2': v2, 'norms2': n2}
     if name == 'smooth_model':
         return {'v': _bumpy_sphere(41)[0], 'f': _bumpy_sphere(41)[1],
                 'v2': _bumpy_sphere(42, nlat=6, nlon=9)[0], 'f2': _bumpy_sphere(42, nlat=6, nlon=9)[1]}
@@ -138,7 +142,7 @@ NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transfo
 
 # golden scenes checked against the oracle only (the CUDA path is held to the
 # oracle on the same materials by tests/test_gpu_parity.py test_material_variants)
-ORACLE_NAMES = ['materials']
+ORACLE_NAMES = ['materials', 'mesh_edits']
 
 
 def build(tina, name, arrays, matrix):
@@ -309,6 +313,23 @@ def build(tina, name, arrays, matrix):
         scene.lighting.add_light(dir=[0.2, -1, 0.5], color=[0.5, 0.5, 0.5])
         scene.lighting.add_light(pos=[0.5, 0.8, 1.5], color=[0.8, 0.7, 0.6])
         scene.engine.set_camera(matrix.lookat(back=(0.1, 0.2, 3.2)), matrix.perspective(60, 64 / 48))
+        return scene, False
+    if name == 'mesh_edits':
+        # MeshNoCulling(MeshFlipNormal(MeshFlipCulling(MeshTransform(soup)))) and
+        # MeshFlatNormal(soup) (tina/mesh/cull.py, norm.py, trans.py)
+        scene = tina.Scene(64, 48, smoothing=True)
+        base = tina.SimpleMesh()
+        base.set_face_verts(arrays['verts'])
+        base.set_face_norms(arrays['norms'])
+        moved = tina.MeshTransform(base)
+        moved.set_transform(matrix.translate([0.3, -0.1, 0.2]) @ matrix.scale([0.7, 1.1, 0.9]))
+        scene.add_object(tina.MeshNoCulling(tina.MeshFlipNormal(tina.MeshFlipCulling(moved))),
+                         tina.PBR(basecolor=[0.7, 0.5, 0.3], metallic=0.3, roughness=0.35))
+        other = tina.SimpleMesh()
+        other.set_face_verts(arrays['verts2'])
+        other.set_face_norms(arrays['norms2'])
+        scene.add_object(tina.MeshFlatNormal(other), tina.Classic(color=[0.9, 0.3, 0.2]))
+        scene.engine.set_camera(matrix.lookat(back=(1, 1, 2.5)), matrix.perspective(50, 64 / 48))
         return scene, False
     if name == 'smooth_model':
         scene = tina.Scene(48, 36, smoothing=True)
