@@ -132,64 +132,61 @@ class PrimitiveMesh(SimpleMesh):
         self.set_face_norms(faces[:, :, 1])
         self.set_face_coors(faces[:, :, 2, :2])
 
+    @staticmethod
+    def _ring_faces(corner, rows, cols, keep_first=True, keep_last=True):
+        """Two triangles (a, b, c) and (c, d, a) per cell of a (rows x cols)
+        corner table, a = (i, j), b = (i, j+1), c = (i+1, j+1), d = (i+1, j),
+        cells in row-major order; `keep_first` / `keep_last` drop the first
+        triangle of the first row and the second of the last row (a sphere's
+        poles)."""
+        faces = []
+        for i in range(rows):
+            for j in range(cols):
+                a, b, c, d = corner[i][j], corner[i][j + 1], corner[i + 1][j + 1], corner[i + 1][j]
+                if keep_first or i != 0:
+                    faces.append([a, b, c])
+                if keep_last or i != rows - 1:
+                    faces.append([c, d, a])
+        return faces
+
     @classmethod
     def sphere(cls, lons=32, lats=24, rad=1):
-        """UV sphere (tina/mesh/prim.py:22-48): the pole rows drop one triangle
-        per quad, so lons=64, lats=32 gives 3,968 faces."""
-        def at(lat, lon):
-            lat /= lats
-            lon /= lons
-            coor = lon, lat, 0
-            lat = (lat - 0.5) * np.pi
-            lon = (lon * 2 - 1) * np.pi
-            x = np.cos(lat) * np.cos(lon)
-            y = np.cos(lat) * np.sin(lon)
-            z = np.sin(lat)
-            norm = x, y, z
-            vert = x * rad, y * rad, z * rad
-            return vert, norm, coor
-
-        faces = []
-        for lat in range(lats):
-            for lon in range(lons):
-                v1 = at(lat, lon)
-                v2 = at(lat, lon + 1)
-                v3 = at(lat + 1, lon + 1)
-                v4 = at(lat + 1, lon)
-                if lat != 0:
-                    faces.append([v1, v2, v3])
-                if lat != lats - 1:
-                    faces.append([v3, v4, v1])
-        return cls(faces)
+        """UV sphere with the face order of tina/mesh/prim.py:22-48 (face ids
+        must match): corner (i, j) sits at latitude (i / lats - 0.5) pi and
+        longitude (2 j / lons - 1) pi with texcoord (j / lons, i / lats); the
+        pole rows keep one triangle per cell, so lons=64, lats=32 gives 3,968
+        faces."""
+        corner = []
+        for i in range(lats + 1):
+            row = []
+            for j in range(lons + 1):
+                u, v = j / lons, i / lats
+                th, ph = (v - 0.5) * np.pi, (u * 2 - 1) * np.pi
+                n = (np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), np.sin(th))
+                row.append(((n[0] * rad, n[1] * rad, n[2] * rad), n, (u, v, 0)))
+            corner.append(row)
+        return cls(cls._ring_faces(corner, lats, lons, keep_first=False, keep_last=False))
 
     @classmethod
     def cylinder(cls, lons=32, lats=4, rad=1, hei=2):
-        """(tina/mesh/prim.py:50-88)"""
-        def at(lat, lon, rad=rad):
-            lat /= lats
-            lon /= lons
-            coor = lon, lat, 0
-            lat = lat - 0.5
-            lon = (lon * 2 - 1) * np.pi
-            x = np.cos(lon)
-            y = np.sin(lon)
-            z = lat
-            return (x * rad, y * rad, z * hei), (x, y, 0), coor
-
-        faces = []
-        for lat in range(lats):
-            for lon in range(lons):
-                v1, v2, v3, v4 = at(lat, lon), at(lat, lon + 1), at(lat + 1, lon + 1), at(lat + 1, lon)
-                faces.append([v1, v2, v3])
-                faces.append([v3, v4, v1])
-        for lon in range(lons):
-            norm, coor = (0, 0, -1), (0, 0, -1)
-            faces.append([(at(0, lon + 1)[0], norm, coor), (at(0, lon)[0], norm, coor),
-                          ((0, 0, -hei / 2), norm, coor)])
-        for lon in range(lons):
-            norm, coor = (0, 0, 1), (0, 0, 1)
-            faces.append([((0, 0, hei / 2), norm, coor), (at(lats, lon)[0], norm, coor),
-                          (at(lats, lon + 1)[0], norm, coor)])
+        """Capped cylinder with the face order of tina/mesh/prim.py:50-88: the
+        side cells, then the bottom cap's fan, then the top cap's; corner
+        (i, j) at height (i / lats - 0.5) hei and angle (2 j / lons - 1) pi."""
+        corner = []
+        for i in range(lats + 1):
+            row = []
+            for j in range(lons + 1):
+                u, v = j / lons, i / lats
+                ph = (u * 2 - 1) * np.pi
+                x, y = np.cos(ph), np.sin(ph)
+                row.append(((x * rad, y * rad, (v - 0.5) * hei), (x, y, 0), (u, v, 0)))
+            corner.append(row)
+        faces = cls._ring_faces(corner, lats, lons)
+        down, up = ((0, 0, -1), (0, 0, -1)), ((0, 0, 1), (0, 0, 1))  # (normal, texcoord) of the caps
+        for j in range(lons):
+            faces.append([(corner[0][j + 1][0],) + down, (corner[0][j][0],) + down, ((0, 0, -hei / 2),) + down])
+        for j in range(lons):
+            faces.append([((0, 0, hei / 2),) + up, (corner[lats][j][0],) + up, (corner[lats][j + 1][0],) + up])
         return cls(faces)
 
 
