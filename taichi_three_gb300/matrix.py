@@ -1,7 +1,13 @@
-"""Camera and model matrices (numpy float64), Tina's tina/util/matrix.py.
+"""Camera and model matrices (numpy float64) with the names and conventions of
+Tina's tina/util/matrix.py: column vectors, right-handed view space looking
+down -z, OpenGL clip space.
 
-Restated without the `transformations` package (that module imports it at
-load time, tina/util/matrix.py:2, but the functions below do not use it).
+The projections are the OpenGL ones (glOrtho, glFrustum, gluPerspective) and
+the view matrix is gluLookAt's.  Every entry is computed with the operations,
+grouped the same way, that give Tina's float64 values bit for bit: the engine
+rounds proj @ view to float32, and depth buffers are compared bit for bit.
+The `transformations` package that Tina's module imports at load time is not
+needed (none of these functions uses it).
 """
 import numpy as np
 
@@ -11,93 +17,99 @@ def identity():
 
 
 def affine(lin, pos):
-    """[lin | pos; 0 0 0 1]  (tina/util/matrix.py:8-12)"""
-    lin = np.concatenate([lin, np.zeros((1, 3))], axis=0)
-    pos = np.concatenate([pos, np.ones(1)])
-    return np.concatenate([lin, pos[:, None]], axis=1)
+    """The 4x4 matrix [lin | pos; 0 0 0 1] (tina/util/matrix.py:8-12)."""
+    out = np.zeros((4, 4))
+    out[:3, :3] = lin
+    out[:3, 3] = pos
+    out[3, 3] = 1.0
+    return out
 
 
 def lookat(pos=(0, 0, 0), back=(0, 0, 3), up=(0, 1, 1e-12)):
-    """View matrix of a camera at pos + back looking at pos (tina/util/matrix.py:22-34)."""
-    pos = np.array(pos, dtype=float)
-    back = np.array(back, dtype=float)
-    up = np.array(up, dtype=float)
-    fwd = -back
-    fwd /= np.linalg.norm(fwd)
-    right = np.cross(fwd, up)
-    right /= np.linalg.norm(right)
-    up = np.cross(right, fwd)
-    lin = np.transpose(np.stack([right, up, -fwd]))
-    return np.linalg.inv(affine(lin, (pos + back)))
+    """World-to-view matrix of a camera at `pos + back` looking at `pos`
+    (tina/util/matrix.py:22-34): the inverse of the camera frame whose
+    columns are right, up and -forward, forward = -back / |back|."""
+    target = np.array(pos, dtype=float)
+    offset = np.array(back, dtype=float)
+    forward = -offset
+    forward /= np.linalg.norm(forward)
+    side = np.cross(forward, np.array(up, dtype=float))
+    side /= np.linalg.norm(side)
+    frame = np.eye(4)
+    frame[:3, 0] = side
+    frame[:3, 1] = np.cross(side, forward)
+    frame[:3, 2] = -forward
+    frame[:3, 3] = target + offset
+    return np.linalg.inv(frame)
 
 
 def ortho(left=-1, right=1, bottom=-1, top=1, near=-100, far=100):
-    """(tina/util/matrix.py:37-45)"""
-    lin = np.eye(4)
-    lin[0, 0] = 2 / (right - left)
-    lin[1, 1] = 2 / (top - bottom)
-    lin[2, 2] = -2 / (far - near)
-    lin[0, 3] = -(right + left) / (right - left)
-    lin[1, 3] = -(top + bottom) / (top - bottom)
-    lin[2, 3] = -(far + near) / (far - near)
-    return lin
+    """glOrtho: the box [left, right] x [bottom, top] x [-near, -far] onto
+    the clip cube (tina/util/matrix.py:37-45)."""
+    w, h, d = right - left, top - bottom, far - near
+    return np.array([[2 / w, 0.0, 0.0, -(right + left) / w],
+                     [0.0, 2 / h, 0.0, -(top + bottom) / h],
+                     [0.0, 0.0, -2 / d, -(far + near) / d],
+                     [0.0, 0.0, 0.0, 1.0]])
 
 
 def frustum(left=-1, right=1, bottom=-1, top=1, near=1, far=100):
-    """(tina/util/matrix.py:48-58)"""
-    lin = np.eye(4)
-    lin[0, 0] = 2 * near / (right - left)
-    lin[1, 1] = 2 * near / (top - bottom)
-    lin[0, 2] = (right + left) / (right - left)
-    lin[1, 2] = (top + bottom) / (top - bottom)
-    lin[2, 2] = -(far + near) / (far - near)
-    lin[2, 3] = -2 * far * near / (far - near)
-    lin[3, 2] = -1
-    lin[3, 3] = 0
-    return lin
+    """glFrustum: the view pyramid through [left, right] x [bottom, top] at
+    distance `near`, cut at `far` (tina/util/matrix.py:48-58)."""
+    w, h, d = right - left, top - bottom, far - near
+    return np.array([[2 * near / w, 0.0, (right + left) / w, 0.0],
+                     [0.0, 2 * near / h, (top + bottom) / h, 0.0],
+                     [0.0, 0.0, -(far + near) / d, -2 * far * near / d],
+                     [0.0, 0.0, -1.0, 0.0]])
 
 
 def orthogonal(size=1, aspect=1, near=-100, far=100):
-    ax, ay = size * aspect, size
-    return ortho(-ax, ax, -ay, ay, near, far)
+    """ortho of half-height `size` and half-width `size * aspect`."""
+    return ortho(-(size * aspect), size * aspect, -size, size, near, far)
 
 
 def perspective(fov=60, aspect=1, near=0.05, far=500):
-    """(tina/util/matrix.py:66-69)"""
-    fov = np.tan(np.radians(fov) / 2)
-    ax, ay = fov * aspect, fov
-    return frustum(-near * ax, near * ax, -near * ay, near * ay, near, far)
+    """gluPerspective: vertical field of view `fov` degrees
+    (tina/util/matrix.py:66-69)."""
+    half = np.tan(np.radians(fov) / 2)
+    x, y = near * (half * aspect), near * half
+    return frustum(-x, x, -y, y, near, far)
 
 
 def scale(factor):
+    """Scaling by `factor` (a number or three)."""
     return affine(np.eye(3) * np.array(factor), np.zeros(3))
 
 
 def translate(offset):
+    """Translation by `offset` (a number or three)."""
     return affine(np.eye(3), np.array(offset) * np.ones(3))
 
 
 def quaternion(q):
-    """Rotation from quaternion (x, y, z, w) (tina/util/matrix.py:81-92)."""
-    R = np.array([
-        [1.0 - 2 * (q[1] * q[1] + q[2] * q[2]), 2 * (q[0] * q[1] - q[3] * q[2]),
-         2 * (q[3] * q[1] + q[0] * q[2])],
-        [2 * (q[0] * q[1] + q[3] * q[2]), 1.0 - 2 * (q[0] * q[0] + q[2] * q[2]),
-         2 * (q[1] * q[2] - q[3] * q[0])],
-        [2 * (q[0] * q[2] - q[3] * q[1]), 2 * (q[1] * q[2] + q[3] * q[0]),
-         1.0 - 2 * (q[0] * q[0] + q[1] * q[1])]])
-    return affine(R, np.zeros(3))
+    """Rotation of the unit quaternion (x, y, z, w) (tina/util/matrix.py:81-92)."""
+    x, y, z, w = q[0], q[1], q[2], q[3]
+    return affine(np.array([
+        [1.0 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (w * y + x * z)],
+        [2 * (x * y + w * z), 1.0 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+        [2 * (x * z - w * y), 2 * (y * z + w * x), 1.0 - 2 * (x * x + y * y)]]), np.zeros(3))
+
+
+def _axis_rotation(axis, angle):
+    c, s = np.cos(angle), np.sin(angle)
+    i, j = [(1, 2), (0, 2), (0, 1)][axis]
+    r = np.eye(3)
+    r[i, i], r[j, j] = c, c
+    # the y rotation turns z into x: its sine terms swap signs
+    r[i, j], r[j, i] = (s, -s) if axis == 1 else (-s, s)
+    return r
 
 
 def eularXYZ(theta):
-    """R_z @ R_y @ R_x (tina/util/matrix.py:96-104)."""
-    R_x = np.array([[1, 0, 0], [0, np.cos(theta[0]), -np.sin(theta[0])],
-                    [0, np.sin(theta[0]), np.cos(theta[0])]])
-    R_y = np.array([[np.cos(theta[1]), 0, np.sin(theta[1])], [0, 1, 0],
-                    [-np.sin(theta[1]), 0, np.cos(theta[1])]])
-    R_z = np.array([[np.cos(theta[2]), -np.sin(theta[2]), 0],
-                    [np.sin(theta[2]), np.cos(theta[2]), 0], [0, 0, 1]])
-    return affine(R_z @ R_y @ R_x, np.zeros(3))
+    """Rotation about x by theta[0], then y by theta[1], then z by theta[2]:
+    R_z @ R_y @ R_x (tina/util/matrix.py:96-104)."""
+    return affine(_axis_rotation(2, theta[2]) @ _axis_rotation(1, theta[1]) @ _axis_rotation(0, theta[0]),
+                  np.zeros(3))
 
 
 def orbit_camera(theta=0.0, phi=0.0, radius=3.0, center=(0, 0, 0)):
