@@ -2,29 +2,28 @@
 takes ({'v', 'vt', 'vn', 'f'} numpy arrays, 'f' [n, 3, 3] 0-based v/vt/vn
 indices per corner).
 
-Behaviour kept from the reference so that face ids match: vertices, texture
-and normal lines are read first, then faces; polygons are split into
-triangles as (0,1,2),(2,3,0) for quads and a fan (0,n,n+1) beyond; a missing
-index field is 0; empty arrays become one zero row; orient permutes and
-negates axes (a leading '-' reverses each face's corner order); scale='auto'
-centres and normalises.
+Behaviour kept from the reference so that face ids match: faces in file
+order, polygons split into triangles as (0,1,2),(2,3,0) for quads and the fan
+(0,k,k+1) otherwise; attribute rows whose fields are not all numbers are
+skipped; a missing index field is 0; empty arrays become one zero row; orient
+permutes and negates axes (a leading '-' reverses each face's corner order);
+scale='auto' centres and normalises.
 """
 import io
 
 import numpy as np
 
 
-def _triangulate(faces, idx):
-    if len(idx) == 3:
-        faces.append(idx)
-    elif len(idx) == 4:
-        faces.append([idx[0], idx[1], idx[2]])
-        faces.append([idx[2], idx[3], idx[0]])
-    elif len(idx) > 4:
-        for k in range(1, len(idx) - 1):
-            faces.append([idx[0], idx[k], idx[k + 1]])
-    else:
-        raise ValueError(f'a face needs at least 3 corners, got {len(idx)}')
+def _split_polygon(corners):
+    """The triangles of one face in the reference's order (face ids follow
+    it): a quad as (0, 1, 2), (2, 3, 0), any other polygon as the fan
+    (0, k, k + 1)."""
+    n = len(corners)
+    if n < 3:
+        raise ValueError(f'a face needs at least 3 corners, got {n}')
+    if n == 4:
+        return [[corners[0], corners[1], corners[2]], [corners[2], corners[3], corners[0]]]
+    return [[corners[0], corners[k], corners[k + 1]] for k in range(1, n - 1)]
 
 
 def _lines(path):
@@ -38,41 +37,45 @@ def _lines(path):
     return [l if isinstance(l, bytes) else l.encode() for l in lines]
 
 
+def _floats(words):
+    try:
+        return [float(w) for w in words]
+    except ValueError:
+        return None
+
+
 def readobj(path, orient='xyz', scale=None, simple=False, usemtl=True, quadok=False):
-    """OBJ file (path, bytes or a file object) -> dict (tina/assimp/obj.py:17-94)."""
-    lines = _lines(path)
-    v, vt, vn, faces, mtls = [], [], [], [], []
-    mtllib = None
-    for line in lines:
-        parts = line.strip().split(maxsplit=1)
-        if len(parts) != 2:
+    """OBJ file (path, bytes or a file object) -> dict (tina/assimp/obj.py:17-94).
+
+    One pass over the lines: `v` / `vt` / `vn` rows whose fields all parse as
+    numbers, `f` corners as 0-based v/vt/vn triples (a missing field is 0),
+    `usemtl` as [first face, name], the last `mtllib`; lines of one word are
+    skipped."""
+    attrs = {b'v': [], b'vt': [], b'vn': []}
+    faces, mtls, mtllib = [], [], None
+    for line in _lines(path):
+        words = line.split()
+        if len(words) < 2:
             continue
-        try:
-            nums = [float(x) for x in parts[1].split()]
-        except ValueError:
-            continue
-        {b'v': v, b'vt': vt, b'vn': vn}.get(parts[0], []).append(nums)
-    for line in lines:
-        parts = line.strip().split(maxsplit=1)
-        if len(parts) != 2:
-            continue
-        kind, rest = parts[0], parts[1].split()
-        if kind == b'mtllib':
-            mtllib = rest[0]
+        kind, rest = words[0], words[1:]
+        if kind in attrs:
+            nums = _floats(rest)
+            if nums is not None:
+                attrs[kind].append(nums)
+        elif kind == b'f':
+            corners = [[int(x) - 1 if x else 0 for x in w.split(b'/')] for w in rest]
+            faces.extend([corners] if quadok else _split_polygon(corners))
         elif kind == b'usemtl':
             mtls.append([len(faces), rest[0]])
-        elif kind == b'f':
-            idx = [[int(x) - 1 if x else 0 for x in corner.split(b'/')] for corner in rest]
-            if quadok:
-                faces.append(idx)
-            else:
-                _triangulate(faces, idx)
-    out = {
-        'v': np.array(v, np.float32) if v else np.zeros((1, 3), np.float32),
-        'vt': np.array(vt, np.float32) if vt else np.zeros((1, 2), np.float32),
-        'vn': np.array(vn, np.float32) if vn else np.zeros((1, 3), np.float32),
-        'f': np.array(faces, np.int32) if faces else np.zeros((1, 3, 3), np.int32),
-    }
+        elif kind == b'mtllib':
+            mtllib = rest[0]
+
+    def table(rows, width, dtype):
+        return np.array(rows, dtype) if rows else np.zeros((1, width), dtype)
+
+    out = {'v': table(attrs[b'v'], 3, np.float32), 'vt': table(attrs[b'vt'], 2, np.float32),
+           'vn': table(attrs[b'vn'], 3, np.float32),
+           'f': np.array(faces, np.int32) if faces else np.zeros((1, 3, 3), np.int32)}
     if usemtl:
         out['usemtl'] = mtls
         out['mtllib'] = mtllib
