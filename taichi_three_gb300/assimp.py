@@ -92,26 +92,26 @@ def readobj(path, orient='xyz', scale=None, simple=False, usemtl=True, quadok=Fa
 
 
 def objorient(obj, orient):
-    """Axis permutation / negation, e.g. 'xZy' (tina/assimp/obj.py:187-205)."""
-    flip = orient.startswith('-')
-    if flip:
-        orient = orient[1:]
-    axes = ['xyz'.index(c.lower()) for c in orient]
-    neg = [c.isupper() for c in orient]
-    if axes != [0, 1, 2]:
-        obj['v'][:, (0, 1, 2)] = obj['v'][:, tuple(axes)]
-        obj['vn'][:, (0, 1, 2)] = obj['vn'][:, tuple(axes)]
-    for i, n in enumerate(neg):
-        if n:
-            obj['v'][:, i] = -obj['v'][:, i]
-            obj['vn'][:, i] = -obj['vn'][:, i]
-    if flip:
+    """Reorients positions and normals in place, e.g. 'xZy': output axis i
+    takes input axis orient[i], negated where the letter is upper case; a
+    leading '-' also reverses every face's corner order
+    (tina/assimp/obj.py:187-205)."""
+    reverse = orient.startswith('-')
+    spec = orient[1:] if reverse else orient
+    src = ['xyz'.index(c.lower()) for c in spec]
+    sign = np.array([-1.0 if c.isupper() else 1.0 for c in spec], np.float32)  # exact in float32
+    for key in ('v', 'vn'):
+        obj[key][:] = obj[key][:, src] * sign
+    if reverse:
         obj['f'] = np.ascontiguousarray(obj['f'][:, ::-1])
 
 
 def objautoscale(obj):
-    obj['v'] -= np.average(obj['v'], axis=0)
-    obj['v'] /= np.max(np.abs(obj['v']))
+    """Centres the positions on their mean and scales the largest coordinate
+    magnitude to 1."""
+    v = obj['v']
+    v -= v.mean(axis=0)
+    v /= np.abs(v).max()
 
 
 def objverts(obj):
