@@ -38,15 +38,16 @@ class Lighting:
         return i
 
     def set_light(self, i, dir=(0, 0, 1), pos=None, color=(1, 1, 1)):
-        if pos is not None:
-            d = np.array(pos, dtype=np.float64)
-            dirw = 1
+        """Lamp i: a point lamp at `pos` (w = 1), or without `pos` a
+        directional lamp along `dir`, normalised in float64 (w = 0); stored
+        rounded to float32 like Taichi's field assignment."""
+        if pos is None:
+            v = np.asarray(dir, dtype=np.float64)
+            xyzw = np.append(v / np.linalg.norm(v), 0.0)
         else:
-            d = np.array(dir, dtype=np.float64)
-            d = d / np.linalg.norm(d)
-            dirw = 0
-        self.light_dirs[i] = np.array(d.tolist() + [dirw], dtype=np.float32)
-        self.light_colors[i] = np.array(np.array(color).tolist(), dtype=np.float32)
+            xyzw = np.append(np.asarray(pos, dtype=np.float64), 1.0)
+        self.light_dirs[i] = xyzw.astype(np.float32)
+        self.light_colors[i] = np.asarray(color, dtype=np.float64).astype(np.float32)
 
     def set_ambient_light(self, color):
         self.ambient_color = np.array(np.array(color, dtype=np.float64).tolist(),
