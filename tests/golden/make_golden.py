@@ -26,7 +26,7 @@ sys.path.insert(0, HERE)
 MODULES = ['tina.common', 'tina.advans', 'tina.matr.nodes', 'tina.matr.material', 'tina.core.engine',
            'tina.core.shader', 'tina.core.lighting', 'tina.core.triangle', 'tina.mesh.base',
            'tina.mesh.simple', 'tina.mesh.prim', 'tina.mesh.trans', 'tina.mesh.cull', 'tina.mesh.grid',
-           'tina.mesh.norm', 'tina.mesh.model', 'tina.mesh.wire', 'tina.core.particle', 'tina.core.wireframe', 'tina.pars.simple', 'tina.postp.tonemap', 'tina.util.matrix', 'tina.scene.raster']
+           'tina.mesh.norm', 'tina.mesh.conn', 'tina.mesh.model', 'tina.mesh.wire', 'tina.core.particle', 'tina.core.wireframe', 'tina.pars.simple', 'tina.postp.tonemap', 'tina.util.matrix', 'tina.scene.raster']
 
 
 def load_reference():

@@ -99,6 +99,10 @@ def inputs(name):
         verts, norms = _soup(120, 81, spread=0.7, sigma=0.3)
         v2, n2 = _soup(80, 82, spread=0.6, sigma=0.3)
         return {'verts': verts, 'norms': norms, 'verts2': v2, 'norms2': n2}
+    if name == 'indexed_ortho':
+        v, f = _bumpy_sphere(43, nlat=8, nlon=12)
+        n = v / np.linalg.norm(v, axis=1, keepdims=True)
+        return {'v': v, 'n': n.astype(np.float32), 'f': f}
     if name == 'smooth_model':
         return {'v': _bumpy_sphere(41)[0], 'f': _bumpy_sphere(41)[1],
                 'v2': _bumpy_sphere(42, nlat=6, nlon=9)[0], 'f2': _bumpy_sphere(42, nlat=6, nlon=9)[1]}
@@ -142,7 +146,7 @@ NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transfo
 
 # golden scenes checked against the oracle only (the CUDA path is held to the
 # oracle on the same materials by tests/test_gpu_parity.py test_material_variants)
-ORACLE_NAMES = ['materials', 'mesh_edits']
+ORACLE_NAMES = ['materials', 'mesh_edits', 'indexed_ortho']
 
 
 def build(tina, name, arrays, matrix):
@@ -331,6 +335,17 @@ def build(tina, name, arrays, matrix):
         scene.add_object(tina.MeshFlatNormal(other), tina.Classic(color=[0.9, 0.3, 0.2]))
         scene.engine.set_camera(matrix.lookat(back=(1, 1, 2.5)), matrix.perspective(50, 64 / 48))
         return scene, False
+    if name == 'indexed_ortho':
+        # an indexed mesh (tina/mesh/conn.py: shared vertices and normals, int
+        # face indices) seen through an orthographic projection
+        scene = tina.Scene(48, 36, smoothing=True)
+        conn = tina.ConnectiveMesh()
+        conn.set_vertices(arrays['v'])
+        conn.set_vert_norms(arrays['n'])
+        conn.set_faces(arrays['f'])
+        scene.add_object(conn, tina.PBR(basecolor=[0.5, 0.7, 0.4], metallic=0.1, roughness=0.5))
+        scene.engine.set_camera(matrix.lookat(back=(0.5, 0.4, 3)), matrix.orthogonal(1.4, 48 / 36))
+        return scene, True
     if name == 'smooth_model':
         scene = tina.Scene(48, 36, smoothing=True)
         model = tina.MeshSmoothNormal(tina.MeshModel(_obj(arrays['v'], arrays['f'])))
