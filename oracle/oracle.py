@@ -5,7 +5,6 @@ restatement in oracle/tina_oracle.cpp, from the same t3_scene descriptor the
 CUDA library receives (its pointers placed on the host).
 """
 import ctypes as C
-import os
 
 import numpy as np
 

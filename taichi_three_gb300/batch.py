@@ -15,7 +15,7 @@ import torch
 
 from . import _native as N
 from ._device import default_device, require_cuda
-from .autotune import Autotuner, default_tuner
+from .autotune import default_tuner
 
 
 def _stream():

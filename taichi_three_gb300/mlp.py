@@ -10,10 +10,8 @@ forward / backward / adam) on targets integrated by Monte Carlo from the
 environment map, and runs at render time on the tensor cores (BF16 operands,
 FP32 accumulation) fused into the shading kernel.
 """
-import ctypes as C
 import math
 
-import numpy as np
 import torch
 
 from . import _native as N

@@ -4,7 +4,6 @@ import os
 import socket
 
 import pytest
-import torch
 import torch.multiprocessing as mp
 
 from taichi_three_gb300 import replicas

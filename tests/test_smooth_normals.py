@@ -2,7 +2,6 @@
 meshes.  The oracle's serial loop against a numpy restatement, the CUDA
 sort-and-sum (t3_smooth_normals) against the oracle bit for bit, and renders
 through the normals against the oracle."""
-import ctypes as C
 import os
 import sys
 
