@@ -46,6 +46,20 @@ extern "C" {
 #define T3_TEXTURING 8  /* interpolate texcoords          triangle.py:44-46 */
 #define T3_TONEMAP 16   /* ACES after shading             scene/raster.py:202-203 */
 #define T3_WIRE_CLIPPING 32 /* WireframeRaster(clipping=True) wireframe.py:78-81 */
+/* t3_shade pixel selection (the three-method raster protocol).  With neither
+ * flag every pixel is written.  With one or both, only the selected pixels
+ * are written and every other pixel's outputs are left as they are: */
+#define T3_SHADE_OWNED 128  /* pixels whose winning face belongs to an object of
+                               the scene: TriangleRaster.render_color skips
+                               occup == -1 (tina/core/triangle.py:134-139)   */
+#define T3_SHADE_EMPTY 256  /* pixels no fragment reached: background colour or
+                               the sky (Engine.render_background,
+                               tina/core/engine.py:42-49)                    */
+/* Test of the timeout path (no reference counterpart): the binned tiles issue
+ * no bin copy and wait, wait_limit polls, on a barrier nothing arrives on;
+ * every tile then gives up, writes background and sets T3_STATUS_TIMEOUT.  No
+ * copy is in flight, so nothing is drained; the next frame is unaffected. */
+#define T3_STARVE_BIN_COPY 512
 
 typedef struct t3_frame {
   int32_t width, height; /* Engine.res                                      */
@@ -56,7 +70,11 @@ typedef struct t3_frame {
   float bias[2];         /* pixel-centre offset, (0.5, 0.5) by default      */
   float bgcolor[3];      /* Scene(bgcolor=...) image.fill value             */
   float linecolor[3];    /* WireframeRaster(linecolor=...), wireframe.py:6-20 */
-  int32_t _pad[2];       /* 184 bytes: keeps t3_scene.lighting.lights 16-byte aligned */
+  int32_t wait_limit;    /* polls of the binned tiles' first bounded wait on
+                            their bin copy (0: the default, 1 << 22); the
+                            second wait, which lets an issued copy land, keeps
+                            the default                                     */
+  int32_t _pad;          /* 184 bytes: keeps t3_scene.lighting.lights 16-byte aligned */
 } t3_frame;
 
 /* ---- meshes (the mesh protocol of the tina.mesh package) ----------------------------- */
@@ -226,7 +244,12 @@ int t3_struct_sizes(int64_t* out, int n);
 /* Workspace bytes needed by t3_render for this scene at raster mode `mode`
  * with tile edge `tile` (8, 16 or 32) and `bin_capacity` entries per frame
  * for the binned mode (0 = automatic).  Replaces the per-raster fields that
- * TriangleRaster.__init__ allocates (tina/core/triangle.py:16-29). */
+ * TriangleRaster.__init__ allocates (tina/core/triangle.py:16-29).
+ * The first 16 bytes of a workspace are state that t3_render keeps between
+ * frames (whether the direct frame's depth keys were left empty by the last
+ * frame's shading, so that the next frame can skip clearing them): zero them
+ * once when the workspace is allocated, and again after using the memory for
+ * anything else. */
 int t3_workspace_size(const t3_scene* scene, int mode, int tile,
                       int64_t bin_capacity, size_t* bytes);
 
@@ -260,6 +283,8 @@ int t3_raster(const t3_frame* frame, const t3_object* object,
  * (tina/core/triangle.py:134-153, shader.py:119-131, lighting.py:84-98,
  * postp/tonemap.py:10-12) for all objects of the scene.  The workspace (at
  * least t3_workspace_size bytes) receives the device copy of the scene.
+ * frame.flags T3_SHADE_OWNED / T3_SHADE_EMPTY restrict the pixels written
+ * (one object of a multi-object frame, then the background).
  * Lighting T3_LIGHT_LAMPS and T3_LIGHT_IBL_MC; T3_LIGHT_IBL_MLP returns
  * T3_EUNSUPPORTED here (t3_render runs it and reports its device status). */
 int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
@@ -339,9 +364,12 @@ int t3_event_elapsed_ms(void* start, void* end, float* ms); /* waits for `end` *
  * width * height <= T3_NOALLOC_MAX_PIXELS (else T3_ETOOBIG); at most
  * T3_NOALLOC_MAX_BIG_FACES faces with a bbox above 4096 px per frame (more set
  * T3_STATUS_BIG_OVERFLOW in *status and those faces are dropped).  The first
- * call on each device looks the array's address up (make it before any
- * stream capture).  All calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller.  Calls no cudaMalloc/cudaFree. */
+ * call in each CUDA context looks the array's address up and caches it under
+ * the context's id (make that call before any stream capture; a new context,
+ * or the one made after a device reset, gets its own lookup).  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the
+ * caller, and so must replays of a CUDA graph that captured this call (the
+ * graph holds the same array's address).  Calls no cudaMalloc/cudaFree. */
 int t3_render_noalloc(const t3_scene* scene, int32_t* status, const t3_outputs* out, void* stream);
 
 /* ---- post-processing of scene.img (images [W, H, 3] float32, pixel x*H + y) ----

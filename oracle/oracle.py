@@ -34,6 +34,9 @@ def load():
         lib.oracle_pixels_f64.restype = C.c_int
         lib.oracle_pixels_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_uint32,
                                           C.c_int, C.c_void_p, C.c_void_p]
+        lib.oracle_pixels_f32.restype = C.c_int
+        lib.oracle_pixels_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p,
+                                          C.c_void_p]
         _lib = lib
     return _lib
 
@@ -94,6 +97,24 @@ def pixels_f64(scene, pixels, spp=0, seed=0, nthreads=0):
         raise RuntimeError(f'oracle_pixels_f64 failed ({rc})')
     del keep
     return pre, post
+
+
+def pixels_f32(scene, pixels, nthreads=0):
+    """FP32 colours (after the tonemap when the scene has it) and winning face
+    ids of the given pixel indices x*H + y, with the scene's own IBL sample
+    stream: the oracle for sampled pixels of frames too large to shade whole."""
+    lib = load()
+    for obj in scene.objects:
+        pre_compute_host(obj)
+    sc, keep = scene.describe('cpu')
+    px = np.ascontiguousarray(pixels, dtype=np.int64)
+    rgb = np.empty((len(px), 3), np.float32)
+    fid = np.empty(len(px), np.int32)
+    rc = lib.oracle_pixels_f32(C.addressof(sc), _p(px), len(px), int(nthreads), _p(rgb), _p(fid))
+    if rc != 0:
+        raise RuntimeError(f'oracle_pixels_f32 failed ({rc})')
+    del keep
+    return rgb, fid
 
 
 def grid_normals(pos):

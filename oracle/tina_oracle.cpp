@@ -160,8 +160,10 @@ template <class R> struct Mesh {
     if (d->kind == T3_MESH_SOUP) {
       return arr + (f * 3 + k) * width;
     } else if (d->kind == T3_MESH_GRID) {
-      // MeshGrid._get_face_props (tina/mesh/grid.py:46-58)
-      int64_t stride = d->grid_nx - 1;
+      // MeshGrid._get_face_props (tina/mesh/grid.py:46-58); cell stride =
+      // the second axis's cell count (res.x - 1 there: equal on square grids,
+      // out of bounds on rectangular ones)
+      int64_t stride = d->grid_ny - 1;
       int64_t m = f / 2;
       int64_t i = m / stride, j = m % stride;
       int64_t ii[4] = {i, i + 1, i + 1, i};
@@ -841,7 +843,7 @@ template <class R> void wire_endpoints(const t3_mesh& m, int64_t n, v3<R>& A, v3
   if (m.flags & T3_MESH_QUADS) {
     // MeshGrid(as_quad=True) (grid.py:46-58): _get_face_props returns the
     // cell's (a, b, c, d) = ((i,j), (i+1,j), (i+1,j+1), (i,j+1))
-    const int64_t f = n / 4, stride = m.grid_nx - 1;
+    const int64_t f = n / 4, stride = m.grid_ny - 1;
     const int64_t i = f / stride, j = f % stride;
     const int64_t ii[4] = {i, i + 1, i + 1, i}, jj[4] = {j, j, j + 1, j + 1};
     v3<R> c[4];
@@ -1262,20 +1264,24 @@ inline std::vector<int64_t> raster_gids_f32(const t3_scene* sc) {
 
 } // namespace
 
-extern "C" {
-
-// FP64 shading of selected pixels over the FP32 raster's winners, with the IBL
-// sample count / seed overridden (spp > 0): the converged reference image for
-// error statements.  rgb_pre / rgb_post: [n, 3] before / after ACES.
-int oracle_pixels_f64(const t3_scene* sc, const int64_t* pixels, int64_t n, int spp, uint32_t seed,
-                      int nthreads, double* rgb_pre, double* rgb_post) {
+// Shading of selected pixels (indices x*H + y) over the FP32 raster's
+// winners, in precision R: rgb_pre / rgb_post [n, 3] before / after ACES,
+// face_id [n] (nullable) the winning global face id (-1 empty).  spp > 0
+// overrides the IBL sample count and seed (ground-truth runs); spp = 0 keeps
+// the scene's own, the stream the CUDA path draws.
+template <class R>
+int shade_pixels(const t3_scene* sc, const int64_t* pixels, int64_t n, int spp, uint32_t seed,
+                        int nthreads, R* rgb_pre, R* rgb_post, int32_t* face_id) {
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
   const t3_frame& fr = sc->frame;
   const int H = fr.height;
+  const int64_t P = (int64_t)fr.width * fr.height;
+  for (int64_t q = 0; q < n; q++)
+    if (pixels[q] < 0 || pixels[q] >= P) return -1;
   std::vector<int64_t> gid = raster_gids_f32(sc);
-  Ctx<double> cx;
+  Ctx<R> cx;
   cx.sc = sc;
   cx.spp = spp;
   cx.seed = seed;
@@ -1285,13 +1291,13 @@ int oracle_pixels_f64(const t3_scene* sc, const int64_t* pixels, int64_t n, int 
   for (int64_t q = 0; q < n; q++) {
     const int64_t i = pixels[q];
     const int32_t x = (int32_t)(i / H), y = (int32_t)(i % H);
-    v3<double> c = {fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]};
+    v3<R> c = {(R)fr.bgcolor[0], (R)fr.bgcolor[1], (R)fr.bgcolor[2]};
     if (gid[i] >= 0) {
       for (int o = 0; o < sc->nobjects; o++) {
         const t3_object& ob = sc->objects[o];
         if (gid[i] >= ob.face_base && gid[i] < ob.face_base + ob.nfaces) {
-          Mesh<double> mesh(&ob.mesh);
-          c = shade_pixel(cx, ob, mesh, gid[i] - ob.face_base, x, y, (double*)nullptr);
+          Mesh<R> mesh(&ob.mesh);
+          c = shade_pixel(cx, ob, mesh, gid[i] - ob.face_base, x, y, (R*)nullptr);
         }
       }
     } else if (ibl) {
@@ -1300,8 +1306,25 @@ int oracle_pixels_f64(const t3_scene* sc, const int64_t* pixels, int64_t n, int 
     if (rgb_pre) { rgb_pre[3 * q] = c.x; rgb_pre[3 * q + 1] = c.y; rgb_pre[3 * q + 2] = c.z; }
     if (fr.flags & T3_TONEMAP) c = {aces1(c.x), aces1(c.y), aces1(c.z)};
     if (rgb_post) { rgb_post[3 * q] = c.x; rgb_post[3 * q + 1] = c.y; rgb_post[3 * q + 2] = c.z; }
+    if (face_id) face_id[q] = (int32_t)gid[i];
   }
   return 0;
+}
+
+extern "C" {
+
+// FP64 shading of selected pixels with the IBL sample count / seed overridden
+// (spp > 0): the converged reference image for error statements.
+int oracle_pixels_f64(const t3_scene* sc, const int64_t* pixels, int64_t n, int spp, uint32_t seed,
+                      int nthreads, double* rgb_pre, double* rgb_post) {
+  return shade_pixels<double>(sc, pixels, n, spp, seed, nthreads, rgb_pre, rgb_post, nullptr);
+}
+
+// FP32 shading of selected pixels with the scene's own IBL stream: the parity
+// oracle for frames too large to shade whole on the CPU.
+int oracle_pixels_f32(const t3_scene* sc, const int64_t* pixels, int64_t n, int nthreads, float* rgb_post,
+                      int32_t* face_id) {
+  return shade_pixels<float>(sc, pixels, n, 0, 0, nthreads, (float*)nullptr, rgb_post, face_id);
 }
 
 

@@ -19,7 +19,7 @@ from .mesh import (MAX, ConnectiveMesh, MeshFlatNormal, MeshFlipCulling, MeshFli
                    MeshModel, MeshNoCulling, MeshSmoothNormal, MeshToWire, MeshTransform, PrimitiveMesh, SimpleMesh,
                    SimpleParticles)
 from .engine import Engine
-from .scene import ParticleRaster, Scene, Shader, TriangleRaster, WireframeRaster
+from .scene import BackgroundShader, ParticleRaster, Scene, Shader, TriangleRaster, WireframeRaster
 from .postp import Accumator, Blooming, FXAA, ToneMapping, aces_tonemap
 from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from .pipeline import FramePipeline

@@ -32,6 +32,8 @@ T3_NOALLOC_MAX_BIG_FACES = 1 << 16
 
 T3_CULLING, T3_CLIPPING, T3_SMOOTHING, T3_TEXTURING, T3_TONEMAP = 1, 2, 4, 8, 16
 T3_WIRE_CLIPPING = 32
+T3_SHADE_OWNED, T3_SHADE_EMPTY = 128, 256
+T3_STARVE_BIN_COPY = 512
 T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED, T3_MESH_PARTICLES, T3_MESH_LINES = 0, 1, 2, 3, 4
 T3_MESH_TRANSFORM, T3_MESH_NOCULL, T3_MESH_FLIP_ORDER, T3_MESH_FLIP_NORMAL, T3_MESH_FLAT_NORMAL = \
     1, 2, 4, 8, 16
@@ -52,7 +54,7 @@ class t3_frame(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("flags", C.c_int32),
                 ("maxdepth", C.c_int32), ("W2V", C.c_float * 16), ("V2W", C.c_float * 16),
                 ("bias", C.c_float * 2), ("bgcolor", C.c_float * 3), ("linecolor", C.c_float * 3),
-                ("_pad", C.c_int32 * 2)]
+                ("wait_limit", C.c_int32), ("_pad", C.c_int32)]
 
 
 class t3_mesh(C.Structure):
@@ -209,3 +211,12 @@ def check_layout(lib):
 def check(rc, what):
     if rc != T3_OK:
         raise RuntimeError(f"{what} failed: {ERRORS.get(rc, rc)} ({rc})")
+
+
+def new_workspace(nbytes, device):
+    """A t3_render workspace: uninitialised except its first 16 bytes, the
+    frame state t3_render keeps between frames, which start at zero."""
+    import torch
+    ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    ws[:16].zero_()
+    return ws

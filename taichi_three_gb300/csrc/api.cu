@@ -134,7 +134,7 @@ static int check_mesh(const t3_mesh& m, int flags, int64_t nfaces) {
   if ((flags & T3_SMOOTHING) && !(m.flags & T3_MESH_FLAT_NORMAL) && !m.norms) return T3_EINVAL;
   if ((flags & T3_TEXTURING) && !m.coors) return T3_EINVAL;
   if (m.kind == T3_MESH_GRID) {
-    if (m.grid_nx < 2 || m.grid_nx != m.grid_ny) return T3_EINVAL;
+    if (m.grid_nx < 2 || m.grid_ny < 2) return T3_EINVAL;
   } else if (m.kind == T3_MESH_INDEXED) {
     if (!m.faces || m.face_stride <= 0 || m.corner_stride <= 0) return T3_EINVAL;
   } else if (m.kind != T3_MESH_SOUP) {
@@ -149,7 +149,7 @@ static int check_frame(const t3_frame& fr) {
   return T3_OK;
 }
 
-int make_dev_scene(const t3_scene& sc, DevScene& out) {
+int make_dev_scene(const t3_scene& sc, DevScene& out, bool first_ids_free) {
   std::memset(&out, 0, sizeof(out));
   int r = check_frame(sc.frame);
   if (r) return r;
@@ -173,8 +173,8 @@ int make_dev_scene(const t3_scene& sc, DevScene& out) {
     const t3_object& ob = sc.objects[o];
     r = check_mesh(ob.mesh, sc.frame.flags, ob.nfaces);
     if (r) return r;
-    if (ob.face_base != total) return T3_EINVAL;  // objects are numbered consecutively
-    total += ob.nfaces;
+    if (first_ids_free ? ob.face_base < total : ob.face_base != total) return T3_EINVAL;
+    total = ob.face_base + ob.nfaces;
     if (total >= (int64_t)0xFFFFFFFFll) return T3_ETOOBIG;  // ids are uint32 in the key
     out.obj[o].mesh = ob.mesh;
     out.obj[o].face_base = ob.face_base;
@@ -240,6 +240,8 @@ static int64_t total_faces(const t3_scene& sc) {
 }
 
 // Workspace layout of one frame (byte offsets, 256-aligned):
+//   state     16 bytes kept between frames: the key tag and the clear's ticket
+//             (KeyState; zero in a new workspace)
 //   scene     DevScene (device copy of the descriptors)
 //   counters  uint32[64 + ntiles]: per-object big-face counts, big-list count,
 //             tile bin counts -- zeroed by the scene upload every frame
@@ -254,6 +256,33 @@ struct Layout {
   int tile, tiles_x, tiles_y;
 };
 
+constexpr size_t kStateBytes = 256;  // KeyState's tag (8 bytes) and ticket (4), padded
+
+// The tag of a direct frame's key buffer: which workspace, layout and frame
+// size the empty keys belong to (splitmix64 finaliser over the four values).
+static unsigned long long key_tag(const void* ws, size_t keys_at, int64_t npix, size_t end) {
+  unsigned long long h = 0x9E3779B97F4A7C15ull;
+  const unsigned long long v[4] = {(unsigned long long)(uintptr_t)ws, (unsigned long long)keys_at,
+                                   (unsigned long long)npix, (unsigned long long)end};
+  for (unsigned long long x : v) {
+    h ^= x + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h ^= h >> 30;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 27;
+    h *= 0x94D049BB133111EBull;
+    h ^= h >> 31;
+  }
+  return h ? h : 1ull;
+}
+
+static KeyState key_state(void* ws, unsigned long long tag) {
+  KeyState ks;
+  ks.tag_word = reinterpret_cast<unsigned long long*>(ws);
+  ks.ticket = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(ws) + 8);
+  ks.tag = tag;
+  return ks;
+}
+
 static int64_t auto_bin_capacity(const t3_scene& sc, int tile) {
   const int64_t tx = (sc.frame.width + tile - 1) / tile, ty = (sc.frame.height + tile - 1) / tile;
   const int64_t per = 8 * total_faces(sc) / (tx * ty) + 64;
@@ -263,8 +292,8 @@ static int64_t auto_bin_capacity(const t3_scene& sc, int tile) {
 
 static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capacity, Layout& L) {
   std::memset(&L, 0, sizeof(L));
-  L.scene = 0;
-  L.counters = align256(sizeof(DevScene));
+  L.scene = kStateBytes;
+  L.counters = L.scene + align256(sizeof(DevScene));
   L.tile = tile;
   if (mode == T3_RASTER_BINNED) {
     if (tile != 8 && tile != 16 && tile != 32) return T3_EINVAL;
@@ -389,14 +418,14 @@ int t3_raster(const t3_frame* frame, const t3_object* object, uint64_t* depth_id
 int t3_shade(const t3_scene* scene, const uint64_t* depth_id, void* workspace,
              size_t workspace_bytes, const t3_outputs* out, void* stream) {
   if (!scene || !depth_id || !out || !out->rgb || !workspace) return T3_EINVAL;
-  if (workspace_bytes < align256(sizeof(DevScene))) return T3_EINVAL;
+  if (workspace_bytes < kStateBytes + align256(sizeof(DevScene))) return T3_EINVAL;
   // the network pass reports timeouts through a status word: t3_render has one
   if (scene->lighting.mode == T3_LIGHT_IBL_MLP) return T3_EUNSUPPORTED;
   static thread_local DevScene ds;
-  int r = make_dev_scene(*scene, ds);
+  int r = make_dev_scene(*scene, ds, true);
   if (r) return r;
   // the shading kernel takes the scene by value; the workspace is not written
-  return cuda_rc(launch_shade(ds, reinterpret_cast<DevScene*>(workspace),
+  return cuda_rc(launch_shade(ds, reinterpret_cast<DevScene*>(reinterpret_cast<uint8_t*>(workspace) + kStateBytes),
                               reinterpret_cast<const unsigned long long*>(depth_id), nullptr, *out, nullptr,
                               (cudaStream_t)stream));
 }
@@ -432,7 +461,10 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     // and the clear also zeroes the counters and the status
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
     const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
-    if (e == cudaSuccess) e = launch_clear(keys, npix, st, counters, L.ncounters, status);
+    // the keys a previous frame's shading emptied are not cleared again; the
+    // lamp and Monte Carlo shading passes empty them for the next frame
+    const KeyState ks = key_state(ws, key_tag(ws, L.keys, npix, L.end));
+    if (e == cudaSuccess) e = launch_clear(keys, npix, st, counters, L.ncounters, status, ks);
     if (e == cudaSuccess) e = mark(1);
     size_t vtx = L.vtx;
     for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
@@ -457,9 +489,11 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     }
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
-      e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st);
+      e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st, ks);
   } else {
-    if (e == cudaSuccess) e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st);
+    if (e == cudaSuccess)
+      e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st,
+                              reinterpret_cast<unsigned long long*>(ws));
     BinArgs b;
     b.rec = reinterpret_cast<float4*>(ws + L.rec);
     b.bins = reinterpret_cast<uint32_t*>(ws + L.bins);
@@ -518,7 +552,8 @@ int t3_raster_fragments(const t3_scene* scene, void* workspace, size_t workspace
   unsigned long long* count = reinterpret_cast<unsigned long long*>(counters + 62);  // 8-byte aligned
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
   const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
-  cudaError_t e = launch_clear(keys, npix, st, counters, L.ncounters, nullptr);
+  // a full clear (tag 0), which also marks the keys as not known to be empty
+  cudaError_t e = launch_clear(keys, npix, st, counters, L.ncounters, nullptr, key_state(ws, 0ull));
   for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
     BigQueue big;
     big.items = reinterpret_cast<uint32_t*>(ws + L.big);

@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_batch_raster(const __grid_co
 template <int NL, bool TEX, int SIG>
 __global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_constant__ BatchArgs a) {
   __shared__ int s_list[kBatchBlock * kBatchPPT];
+  __shared__ unsigned long long s_key[kBatchBlock * kBatchPPT];
   __shared__ int s_count;
   __shared__ uint32_t s_item;
   for (;;) {
@@ -168,7 +169,8 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_con
     const int64_t base = (int64_t)(gs - v.shade_item0) * a.pixels_per_item;
     for (int64_t p0 = base; p0 < base + a.pixels_per_item && p0 < v.npix; p0 += kBatchBlock * kBatchPPT) {
       shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS, false, TEX, SIG>(v.sc, v.keys, v.rec, v.out,
-                                                                                v.npix, p0, s_list, &s_count);
+                                                                                v.npix, p0, s_list, &s_count,
+                                                                                s_key);
       __syncthreads();
       if (threadIdx.x == 0) s_count = 0;
       __syncthreads();

@@ -155,7 +155,11 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
   // stage this tile's bin with one bulk copy: 16-byte multiples from the
   // 16-byte aligned start of a capacity-sized bin (capacity % 4 == 0)
   const uint32_t bytes = ((n * 4u) + 15u) & ~15u;
-  if (threadIdx.x == 0) {
+  // T3_STARVE_BIN_COPY (tests of the timeout path): nothing is issued and
+  // nothing arrives, so the first wait below runs out
+  const bool starve = (fr.flags & T3_STARVE_BIN_COPY) != 0;
+  const uint32_t first_limit = fr.wait_limit > 0 ? (uint32_t)fr.wait_limit : (1u << 22);
+  if (threadIdx.x == 0 && !starve) {
     if (bytes) {
       const uint32_t* src = bins.bins + (size_t)tile * bins.capacity;
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
@@ -167,9 +171,10 @@ k_tile(const DevScene* __restrict__ sc, BinArgs bins, t3_outputs out) {
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar_a) : "memory");
     }
   }
-  if (!mbar_wait(bar_a, 0, 1u << 22)) {
+  if (!mbar_wait(bar_a, 0, first_limit)) {
     s_ok = 0;
-    mbar_wait(bar_a, 0, 1u << 22);  // let our own copy land before reusing shared memory
+    // let our own copy land before the shared memory is reused (when one was issued)
+    if (!starve) mbar_wait(bar_a, 0, 1u << 22);
   }
   __syncthreads();
   const bool ok = s_ok != 0;

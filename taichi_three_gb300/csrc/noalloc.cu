@@ -12,12 +12,19 @@
 // buffer) lives in `g_noalloc_scratch`, a file-scope __device__ array of
 // T3_NOALLOC_SCRATCH_BYTES (17,056,000 bytes, about 16.3 MiB).  Every GPU that loads the library
 // holds that array until the process exits.  In host code the array's name is
-// only a host-side stand-in, so the first call on each device (with that
-// device current) looks up its device address with cudaGetSymbolAddress and
-// caches it; make that first call before any stream capture.  Each call
-// clears what must start empty (counters, status word, key buffer).  All calls
-// share the one array: calls whose work overlaps on the GPU (other streams,
-// other host threads) race on it and must be serialised by the caller.
+// only a host-side stand-in, so the first call in each CUDA context (with that
+// context current) looks up the array's device address with
+// cudaGetSymbolAddress and caches it under the context's unique id: a device
+// address belongs to the context that loaded the module, so a caller that
+// makes its own contexts, or resets the device (which ends the old context),
+// gets a fresh lookup rather than a stale pointer.  Make the first call in a
+// context before any stream capture.  Each call clears what must start empty
+// (counters, status word, key buffer).  All calls share the one array: calls
+// whose work overlaps on the GPU (other streams, other host threads, replays
+// of a CUDA graph that captured this call) race on it and must be serialised
+// by the caller.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "t3_internal.cuh"
@@ -35,20 +42,66 @@ static_assert(kNoallocBytes == T3_NOALLOC_SCRATCH_BYTES, "scratch size in tina3.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[64];  // per device ordinal
+// device addresses of g_noalloc_scratch, one per CUDA context that has called
+// (keyed by cuCtxGetId, which is unique over the process's lifetime)
+struct NoallocAddr {
+  unsigned long long ctx_id;
+  void* ptr;
+};
+static NoallocAddr g_noalloc_addr[64];
+static int g_noalloc_next;  // slot replaced next once the table is full
 
-// device address of g_noalloc_scratch on the current device (looked up once)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// device address of g_noalloc_scratch in the current context (looked up once per context)
 static int noalloc_scratch(void** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return T3_ECUDA;
-  if (dev < 0 || dev >= 64) return T3_EUNSUPPORTED;
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return T3_ECUDA;
-    g_noalloc_addr[dev] = p;
+  // the two driver calls come through the runtime's entry-point table, so the
+  // library itself does not link against the driver library
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (!get_current &&
+        (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&get_current, 12000, cudaEnableDefault,
+                                          &q1) != cudaSuccess || q1 != cudaDriverEntryPointSuccess))
+      get_current = nullptr;
+    if (!get_id &&
+        (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&get_id, 12000, cudaEnableDefault, &q2) !=
+             cudaSuccess || q2 != cudaDriverEntryPointSuccess))
+      get_id = nullptr;
+    if (!get_current || !get_id) return T3_ECUDA;
   }
-  *out = g_noalloc_addr[dev];
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS) return T3_ECUDA;
+  if (!ctx) {
+    // no context bound to this thread yet: bind the current device's primary
+    // context, as the runtime would on its first call (nothing can be capturing)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return T3_ECUDA;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return T3_ECUDA;
+  }
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return T3_ECUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  for (const NoallocAddr& a : g_noalloc_addr)
+    if (a.ptr && a.ctx_id == id) {
+      *out = a.ptr;
+      return T3_OK;
+    }
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return T3_ECUDA;
+  NoallocAddr* slot = nullptr;
+  for (NoallocAddr& a : g_noalloc_addr)
+    if (!a.ptr) { slot = &a; break; }
+  if (!slot) {
+    slot = &g_noalloc_addr[g_noalloc_next];
+    g_noalloc_next = (g_noalloc_next + 1) % 64;
+  }
+  slot->ctx_id = id;
+  slot->ptr = p;
+  *out = p;
   return T3_OK;
 }
 

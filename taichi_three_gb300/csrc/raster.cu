@@ -20,20 +20,37 @@
 namespace t3 {
 
 // key buffer <- empty; also zeroes `ncounters` frame counters and the status
-// word (one launch where the frame needs no device copy of the scene)
+// word (one launch where the frame needs no device copy of the scene).  With a
+// key state (t3_render's direct frames) the keys are left alone when the tag
+// says the previous frame's shading emptied them; the last block to finish
+// then marks them as not known to be empty.
 __global__ void k_clear(unsigned long long* __restrict__ keys, int64_t n, uint32_t* __restrict__ counters,
-                        int ncounters, int32_t* __restrict__ status) {
+                        int ncounters, int32_t* __restrict__ status, KeyState ks) {
+  __shared__ int s_skip;
+  if (threadIdx.x == 0)
+    s_skip = ks.tag_word && ks.tag != 0ull && *(volatile unsigned long long*)ks.tag_word == ks.tag;
+  __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < ncounters) counters[i] = 0u;
   if (i == 0 && status) *status = 0;
-  if ((reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
-    ulonglong2* k2 = reinterpret_cast<ulonglong2*>(keys);
-    const int64_t n2 = n >> 1;
-    for (int64_t j = i; j < n2; j += stride) k2[j] = make_ulonglong2(T3_EMPTY_KEY, T3_EMPTY_KEY);
-    if (i == 0 && (n & 1)) keys[n - 1] = T3_EMPTY_KEY;
-  } else {
-    for (int64_t j = i; j < n; j += stride) keys[j] = T3_EMPTY_KEY;
+  if (!s_skip) {
+    if ((reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
+      ulonglong2* k2 = reinterpret_cast<ulonglong2*>(keys);
+      const int64_t n2 = n >> 1;
+      for (int64_t j = i; j < n2; j += stride) k2[j] = make_ulonglong2(T3_EMPTY_KEY, T3_EMPTY_KEY);
+      if (i == 0 && (n & 1)) keys[n - 1] = T3_EMPTY_KEY;
+    } else {
+      for (int64_t j = i; j < n; j += stride) keys[j] = T3_EMPTY_KEY;
+    }
+  }
+  if (ks.tag_word && threadIdx.x == 0) {
+    // this block has read the tag: order that read before the ticket
+    __threadfence();
+    if (atomicAdd(ks.ticket, 1u) == gridDim.x - 1) {
+      *ks.tag_word = 0ull;
+      *ks.ticket = 0u;
+    }
   }
 }
 
@@ -132,11 +149,16 @@ k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
 }
 
 cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, uint32_t* counters,
-                         int ncounters, int32_t* status) {
+                         int ncounters, int32_t* status, KeyState ks) {
   const int block = 256;
   int64_t want = ((n >> 1) + block - 1) / block;
-  const int grid = (int)(want < 4 * 152 * 8 ? (want > 0 ? want : 1) : 4 * 152 * 8);
-  k_clear<<<grid, block, 0, st>>>(keys, n, counters, ncounters, status);
+  // with a key state, a grid that exits quickly when the keys are already
+  // empty (four CTAs per SM stride over the buffer when they are not)
+  const int64_t cap = ks.tag_word ? 4 * 152 : 4 * 152 * 8;
+  int64_t grid = want < cap ? want : cap;
+  if (grid * block < ncounters) grid = (ncounters + block - 1) / block;
+  if (grid < 1) grid = 1;
+  k_clear<<<(unsigned)grid, block, 0, st>>>(keys, n, counters, ncounters, status, ks);
   return cudaGetLastError();
 }
 

@@ -15,7 +15,9 @@ namespace t3 {
 // kernel of the frame, including inside a captured CUDA graph.
 __global__ void k_upload_scene(const DevScene sc, DevScene* __restrict__ dst,
                                uint32_t* __restrict__ counters, int ncounters,
-                               int32_t* __restrict__ status) {
+                               int32_t* __restrict__ status, unsigned long long* __restrict__ key_tag) {
+  // a frame of another layout: the direct frame's keys are no longer known empty
+  if (key_tag && blockIdx.x == 0 && threadIdx.x == 0) *key_tag = 0ull;
   // the descriptor is split across blocks: each block copies a 1 KB slice, so
   // the constant-bank reads of the parameter run on many SMs at once
   constexpr int nwords = (int)(sizeof(DevScene) / 4);
@@ -28,11 +30,12 @@ __global__ void k_upload_scene(const DevScene sc, DevScene* __restrict__ dst,
 }
 
 cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
-                                int ncounters, int32_t* status, cudaStream_t st) {
+                                int ncounters, int32_t* status, cudaStream_t st,
+                                unsigned long long* key_tag) {
   constexpr int scene_blocks = (int)((sizeof(DevScene) / 4 + 255) / 256);
   int grid = (ncounters + 255) / 256;
   grid = grid < scene_blocks ? scene_blocks : grid > 64 ? 64 : grid;
-  k_upload_scene<<<grid, 256, 0, st>>>(sc, dst, counters, ncounters, status);
+  k_upload_scene<<<grid, 256, 0, st>>>(sc, dst, counters, ncounters, status, key_tag);
   return cudaGetLastError();
 }
 
@@ -43,13 +46,17 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
 template <int BLOCK, int PPT, int NL, int MODE, bool TEX, int SIG>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_shade(const __grid_constant__ DevScene sc, const unsigned long long* __restrict__ keys,
-        const float4* __restrict__ rec, t3_outputs out, int64_t npix) {
+        const float4* __restrict__ rec, t3_outputs out, int64_t npix, KeyState reset) {
   __shared__ int s_list[BLOCK * PPT];
+  __shared__ unsigned long long s_key[BLOCK * PPT];
   __shared__ int s_count;
   if (threadIdx.x == 0) s_count = 0;
+  // the keys are empty once every block has run: mark them so for the next frame
+  if (reset.tag_word && blockIdx.x == 0 && threadIdx.x == 0) *reset.tag_word = reset.tag;
   __syncthreads();
-  shade_block<BLOCK, PPT, NL, MODE, false, TEX, SIG>(&sc, keys, rec, out, npix,
-                                                     (int64_t)blockIdx.x * BLOCK * PPT, s_list, &s_count);
+  shade_block<BLOCK, PPT, NL, MODE, false, TEX, SIG>(
+      &sc, keys, rec, out, npix, (int64_t)blockIdx.x * BLOCK * PPT, s_list, &s_count, s_key,
+      reset.tag_word ? const_cast<unsigned long long*>(keys) : nullptr);
 }
 
 // the lobe signature shared by every shaded object, when an instance exists
@@ -70,43 +77,45 @@ int lobe_signature(const DevScene& sc) {
 
 template <int NL, int MODE, bool TEX, int SIG = 0>
 static void launch_shade_t(const DevScene& sc, const unsigned long long* keys, const float4* rec,
-                           const t3_outputs& out, int64_t npix, cudaStream_t st) {
+                           const t3_outputs& out, int64_t npix, cudaStream_t st, const KeyState& ks) {
   constexpr int BLOCK = 256, PPT = 4;
   const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
   if constexpr (MODE == T3_LIGHT_LAMPS && !TEX && SIG == 0) {
     // untextured lamp scenes with one common lobe signature
     const int sig = lobe_signature(sc);
-    if (NL == 2 && sig == T3_SIG_PBR) return launch_shade_t<2, MODE, TEX, T3_SIG_PBR>(sc, keys, rec, out, npix, st);
+    if (NL == 2 && sig == T3_SIG_PBR) return launch_shade_t<2, MODE, TEX, T3_SIG_PBR>(sc, keys, rec, out, npix, st, ks);
     if (NL == 2 && sig == T3_SIG_CLASSIC)
-      return launch_shade_t<2, MODE, TEX, T3_SIG_CLASSIC>(sc, keys, rec, out, npix, st);
+      return launch_shade_t<2, MODE, TEX, T3_SIG_CLASSIC>(sc, keys, rec, out, npix, st, ks);
     if (NL == 1 && sig == T3_SIG_DIFFUSE)
-      return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE>(sc, keys, rec, out, npix, st);
+      return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE>(sc, keys, rec, out, npix, st, ks);
   }
-  k_shade<BLOCK, PPT, NL, MODE, TEX, SIG><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix);
+  k_shade<BLOCK, PPT, NL, MODE, TEX, SIG><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix, ks);
 }
 
 template <int MODE, bool TEX>
 static void launch_shade_m(const DevScene& sc, const unsigned long long* keys, const float4* rec,
-                           const t3_outputs& out, int64_t npix, int max_lobes, cudaStream_t st) {
-  if (max_lobes <= 1) launch_shade_t<1, MODE, TEX>(sc, keys, rec, out, npix, st);
-  else if (max_lobes == 2) launch_shade_t<2, MODE, TEX>(sc, keys, rec, out, npix, st);
-  else launch_shade_t<4, MODE, TEX>(sc, keys, rec, out, npix, st);
+                           const t3_outputs& out, int64_t npix, int max_lobes, cudaStream_t st,
+                           const KeyState& ks) {
+  if (max_lobes <= 1) launch_shade_t<1, MODE, TEX>(sc, keys, rec, out, npix, st, ks);
+  else if (max_lobes == 2) launch_shade_t<2, MODE, TEX>(sc, keys, rec, out, npix, st, ks);
+  else launch_shade_t<4, MODE, TEX>(sc, keys, rec, out, npix, st, ks);
 }
 
 cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
-                         const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st) {
+                         const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st,
+                         KeyState reset) {
   const t3_frame& fr = sc_host.frame;
   const int64_t npix = (int64_t)fr.width * fr.height;
   const int max_lobes = t3::max_lobes(sc_host), light_mode = sc_host.lighting.mode;
   const bool textured = has_textures(sc_host) != 0;
   if (light_mode == T3_LIGHT_LAMPS && textured)
-    launch_shade_m<T3_LIGHT_LAMPS, true>(sc_host, keys, rec, out, npix, max_lobes, st);
+    launch_shade_m<T3_LIGHT_LAMPS, true>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_LAMPS)
-    launch_shade_m<T3_LIGHT_LAMPS, false>(sc_host, keys, rec, out, npix, max_lobes, st);
+    launch_shade_m<T3_LIGHT_LAMPS, false>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_IBL_MC && textured)
-    launch_shade_m<T3_LIGHT_IBL_MC, true>(sc_host, keys, rec, out, npix, max_lobes, st);
+    launch_shade_m<T3_LIGHT_IBL_MC, true>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_IBL_MC)
-    launch_shade_m<T3_LIGHT_IBL_MC, false>(sc_host, keys, rec, out, npix, max_lobes, st);
+    launch_shade_m<T3_LIGHT_IBL_MC, false>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_IBL_MLP)
     return launch_shade_mlp(sc_host, keys, rec, out, status, st);
   else

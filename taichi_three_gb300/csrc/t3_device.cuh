@@ -93,8 +93,10 @@ __device__ __forceinline__ const float* base_ptr(const t3_mesh& d, int64_t f, in
   if (d.kind == T3_MESH_SOUP) {
     return arr + (f * 3 + k) * width;
   } else if (d.kind == T3_MESH_GRID) {
-    // MeshGrid._get_face_props (tina/mesh/grid.py:46-58); square grids
-    const uint32_t stride = (uint32_t)d.grid_nx - 1u;
+    // MeshGrid._get_face_props (tina/mesh/grid.py:46-58); the cell stride is
+    // the second axis's cell count (the reference's res.x - 1 equals it on
+    // square grids and reads outside a rectangular one)
+    const uint32_t stride = (uint32_t)d.grid_ny - 1u;
     const uint32_t m = (uint32_t)(f >> 1);
     const uint32_t i = m / stride, j = m - i * stride;
     // corners a=(i,j) b=(i+1,j) c=(i+1,j+1) d=(i,j+1); odd faces take (a, c, d)
@@ -283,7 +285,7 @@ __device__ __forceinline__ bool face_setup(const t3_frame& fr, const f3 v[3], Se
 // vertex row of corner k of base face f (GRID and INDEXED meshes; base_ptr's indexing)
 __device__ __forceinline__ int64_t corner_vertex(const t3_mesh& d, int64_t f, int k) {
   if (d.kind == T3_MESH_GRID) {
-    const uint32_t stride = (uint32_t)d.grid_nx - 1u;
+    const uint32_t stride = (uint32_t)d.grid_ny - 1u;
     const uint32_t m = (uint32_t)(f >> 1);
     const uint32_t i = m / stride, j = m - i * stride;
     int c = k;
@@ -418,7 +420,7 @@ __device__ __forceinline__ void wire_endpoints(const t3_mesh& d, int64_t n, f3& 
     // a=(i,j) b=(i+1,j) c=(i+1,j+1) d=(i,j+1); line n joins corners n % 4 and (n + 1) % 4
     const int64_t f = n >> 2;
     const int e = (int)(n & 3);
-    const int64_t stride = (int64_t)d.grid_nx - 1;
+    const int64_t stride = (int64_t)d.grid_ny - 1;
     const int64_t i = f / stride, j = f - i * stride;
     auto corner = [&](int c) {
       const int64_t ii = i + (c == 1 || c == 2 ? 1 : 0), jj = j + (c >= 2 ? 1 : 0);

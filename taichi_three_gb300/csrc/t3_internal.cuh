@@ -89,8 +89,24 @@ static_assert((offsetof(DevScene, lighting) + offsetof(t3_lighting, lights)) % 1
 static_assert(sizeof(t3_light) % 16 == 0, "t3_light must be a multiple of 16 bytes");
 
 
+// The direct frame's key buffer between frames.  t3_render keeps, at the start
+// of its workspace, a 64-bit tag and a u32 ticket: the shading pass resets
+// every key it reads to empty and then stores the frame's tag, so the next
+// frame with the same tag (same workspace, layout and size) finds its keys
+// already empty and skips the clear; the clear stores 0 (keys not known to be
+// empty) once all of its blocks have read the tag.  Every other use of the
+// workspace leaves 0 there.
+struct KeyState {
+  unsigned long long* tag_word = nullptr;  // nullptr: no state kept (always clear)
+  uint32_t* ticket = nullptr;              // blocks of the clear that have read the tag
+  unsigned long long tag = 0;              // this frame's tag (0: never skip the clear)
+};
+
 int flatten_material(const t3_material& in, DevMaterial& out);
-int make_dev_scene(const t3_scene& sc, DevScene& out);
+// first_ids_free: objects may start at any face id past the previous object's
+// last (t3_shade of one object of a protocol frame); otherwise they are
+// numbered consecutively from 0 (every frame that indexes setup records by id)
+int make_dev_scene(const t3_scene& sc, DevScene& out, bool first_ids_free = false);
 
 cudaError_t launch_raster_particles(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                     unsigned long long* fragments, cudaStream_t st);
@@ -111,15 +127,19 @@ cudaError_t launch_vertex_ndc(const t3_frame& fr, const t3_mesh& mesh, int64_t n
 int64_t mesh_vertex_rows(const t3_mesh& m);  // rows the vertex stage transforms (0: none)
 cudaError_t launch_red_min_rate(unsigned long long* buf, int64_t n, int rounds, cudaStream_t st);
 cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, uint32_t* counters = nullptr,
-                         int ncounters = 0, int32_t* status = nullptr);
+                         int ncounters = 0, int32_t* status = nullptr, KeyState ks = KeyState());
 cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* counters,
-                                int ncounters, int32_t* status, cudaStream_t st);
+                                int ncounters, int32_t* status, cudaStream_t st,
+                                unsigned long long* key_tag = nullptr);
 cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsigned long long* keys,
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 // the shading pass; the scene descriptor is passed to the kernels by value
 // (sc_dev, its uploaded copy, is kept for kernels that read it from memory)
+// reset (lamp and Monte Carlo lighting): the pass returns every key it reads
+// to empty and then stores reset.tag in *reset.tag_word
 cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
-                         const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st);
+                         const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st,
+                         KeyState reset = KeyState());
 cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                              const t3_outputs& out, int32_t* status, cudaStream_t st);
 int max_lobes(const DevScene& sc);

@@ -263,6 +263,19 @@ __device__ __forceinline__ V3 view_ray(const t3_frame& fr, float px, float py) {
   return normalized(ro1 - ro);
 }
 
+// the object owning the key's face id (-1: empty pixel, or an id no object owns)
+__device__ __forceinline__ int key_owner(const DevScene* __restrict__ sc, unsigned long long key) {
+  int o = -1;
+  if (key != T3_EMPTY_KEY) {
+    const int64_t gid = (int64_t)(uint32_t)key;
+    const int nobj = sc->nobjects;
+    for (int j = 0; j < nobj; j++) {
+      if (gid >= sc->obj[j].face_base && gid < sc->obj[j].face_base + sc->obj[j].nfaces) o = j;
+    }
+  }
+  return o;
+}
+
 // Everything shading needs about one covered pixel.
 struct PixelGeom {
   int64_t i;          // pixel index x*H + y
@@ -289,15 +302,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   const int64_t i = (int64_t)x * H + y;
   g.i = i;
   g.flat = false;
-  // the object owning this face id (-1: empty pixel, or an id no object owns)
-  int o = -1;
-  if (key != T3_EMPTY_KEY) {
-    const int64_t gid = (int64_t)(uint32_t)key;
-    const int nobj = sc->nobjects;
-    for (int j = 0; j < nobj; j++) {
-      if (gid >= sc->obj[j].face_base && gid < sc->obj[j].face_base + sc->obj[j].nfaces) o = j;
-    }
-  }
+  const int o = key_owner(sc, key);
   if (o < 0) {
     if (out.face_id) out.face_id[i] = -1;
     if (out.depth) out.depth[i] = fr.maxdepth;
@@ -453,6 +458,11 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
   const t3_frame& fr = sc->frame;
   PixelGeom g;
   const t3_lighting& lt = sc->lighting;
+  if (const int sel = fr.flags & (T3_SHADE_OWNED | T3_SHADE_EMPTY)) {
+    // protocol frames: only the selected pixels are written
+    const bool empty = key == T3_EMPTY_KEY;
+    if (empty ? !(sel & T3_SHADE_EMPTY) : (!(sel & T3_SHADE_OWNED) || key_owner(sc, key) < 0)) return;
+  }
   if (!pixel_geometry<COHERENT_REC>(sc, rec, key, x, y, out, g)) {
     V3 bg = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
     if (MODE != T3_LIGHT_LAMPS) {
@@ -523,14 +533,18 @@ __device__ __forceinline__ void prefetch_face(const DevScene* __restrict__ sc, c
 
 // One block's share of the shading pass: pixels [base, base + BLOCK * PPT) of
 // the frame.  Empty pixels are written as background at once; covered ones are
-// compacted into a shared list (warp ballot + one shared atomic per warp) so
-// that full warps run the shading.  s_list holds BLOCK * PPT entries; s_count
-// must be zero on entry and is left non-zero (callers reset it after a barrier).
+// compacted into a shared list (warp ballot + one shared atomic per warp), with
+// their keys, so that full warps run the shading.  s_list and s_key hold
+// BLOCK * PPT entries; s_count must be zero on entry and is left non-zero
+// (callers reset it after a barrier).  reset_keys (nullable): the frame's key
+// buffer, whose keys this block returns to empty as it reads them.
 template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false, bool TEX = true, int SIG = 0>
 __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
                                             const unsigned long long* __restrict__ keys,
                                             const float4* __restrict__ rec, const t3_outputs& out,
-                                            int64_t npix, int64_t base, int* s_list, int* s_count) {
+                                            int64_t npix, int64_t base, int* s_list, int* s_count,
+                                            unsigned long long* s_key,
+                                            unsigned long long* reset_keys = nullptr) {
   const t3_frame& fr = sc->frame;
   const int H = fr.height;
   const V3 bg = background(fr);
@@ -540,19 +554,31 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
     const int local = k * BLOCK + threadIdx.x;
     const int64_t i = base + local;
     bool covered = false;
+    unsigned long long key = T3_EMPTY_KEY;
     if (i < npix) {
       // with IBL, empty pixels show the sky and go through the shading list too
-      const unsigned long long key = COHERENT ? __ldcg(keys + i) : keys[i];
-      if (MODE == T3_LIGHT_LAMPS && key == T3_EMPTY_KEY) write_empty(fr, out, i, bg);
-      else covered = true;
-      if (key != T3_EMPTY_KEY) prefetch_face(sc, rec, key);
+      key = COHERENT ? __ldcg(keys + i) : keys[i];
+      if (MODE == T3_LIGHT_LAMPS && key == T3_EMPTY_KEY) {
+        // protocol frames that select pixels write empty ones only with T3_SHADE_EMPTY
+        if (!(fr.flags & T3_SHADE_OWNED) || (fr.flags & T3_SHADE_EMPTY)) write_empty(fr, out, i, bg);
+      } else {
+        covered = true;
+      }
+      if (key != T3_EMPTY_KEY) {
+        prefetch_face(sc, rec, key);
+        if (reset_keys) reset_keys[i] = T3_EMPTY_KEY;
+      }
     }
     const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
     if (m) {
       int slot = 0;
       if (lane == 0) slot = atomicAdd(s_count, __popc(m));
       slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-      if (covered) s_list[slot + __popc(m & ((1u << lane) - 1u))] = local;
+      if (covered) {
+        const int at = slot + __popc(m & ((1u << lane) - 1u));
+        s_list[at] = local;
+        s_key[at] = key;
+      }
     }
   }
   __syncthreads();
@@ -560,8 +586,7 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
   for (int j = threadIdx.x; j < n; j += BLOCK) {
     const int64_t i = base + s_list[j];
     const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
-    const unsigned long long key = COHERENT ? __ldcg(keys + i) : keys[i];
-    shade_pixel_from_key<NL, MODE, COHERENT, TEX, SIG>(sc, rec, key, x, y, out);
+    shade_pixel_from_key<NL, MODE, COHERENT, TEX, SIG>(sc, rec, s_key[j], x, y, out);
   }
 }
 

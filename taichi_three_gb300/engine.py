@@ -19,6 +19,10 @@ class Engine:
         self.V2W = np.diag(np.array([1, 1, -1, 1], dtype=np.float32))
         self.bias = np.array([0.5, 0.5], dtype=np.float32)
         self.depth = None  # torch int32 [W, H] after a render
+        # the frame's packed (depth, face id) keys of the three-method raster
+        # protocol (int64 [W, H], -1 = empty) and the next free face id
+        self.keys = None
+        self._face_cursor = 0
 
     def set_camera(self, view, proj):
         """W2V = proj @ view in float64, V2W its inverse, both stored as float32
@@ -35,9 +39,33 @@ class Engine:
             self.bias = np.random.random(2).astype(np.float32)
 
     def clear_depth(self):
-        if self.depth is None:
-            self.depth = torch.empty(self.res, dtype=torch.int32, device=default_device())
+        """Engine.clear_depth (tina/core/engine.py:68-70): depth = maxdepth, and
+        the frame's depth keys emptied; face ids restart at 0."""
+        dev = default_device()
+        if self.depth is None or tuple(self.depth.shape) != self.res:
+            self.depth = torch.empty(self.res, dtype=torch.int32, device=dev)
         self.depth.fill_(self.maxdepth)
+        if self.keys is None or tuple(self.keys.shape) != self.res:
+            self.keys = torch.empty(self.res, dtype=torch.int64, device=dev)
+        lib = N.load()
+        N.check(lib.t3_clear(self.keys.data_ptr(), self.keys.numel(),
+                             torch.cuda.current_stream().cuda_stream), 't3_clear')
+        self._face_cursor = 0
+
+    def _claim_faces(self, n):
+        """First face id of the next object rasterised in this frame."""
+        base = self._face_cursor
+        if base + n >= 0xFFFFFFFF:
+            raise ValueError('more than 2**32 - 1 faces in one frame')
+        self._face_cursor = base + n
+        return base
+
+    def _keys_to_depth(self):
+        """engine.depth from the packed keys: the high word holds the int32
+        depth with its sign bit flipped, i.e. depth + 2**31; empty pixels keep
+        maxdepth."""
+        d = ((self.keys >> 32) & 0xFFFFFFFF) - (1 << 31)
+        self.depth.copy_(torch.where(self.keys == -1, torch.full_like(d, self.maxdepth), d))
 
     def _t3_fill_frame(self, fr, flags, bgcolor):
         fr.width, fr.height = self.res

@@ -191,8 +191,10 @@ class PrimitiveMesh(SimpleMesh):
 
 
 class MeshGrid(MeshBase):
-    """Parametric grid (tina/mesh/grid.py): pos/nrm/tex [n, n, 3|2]; two
-    triangles per cell, or with `as_quad=True` one quad per cell (drawn only
+    """Parametric grid (tina/mesh/grid.py): pos/nrm/tex [nx, ny, 3|2]; two
+    triangles per cell (cell m = (m // (ny - 1), m % (ny - 1)): the reference's
+    order on square grids, where its stride res.x - 1 equals ny - 1; on a
+    rectangular grid that stride would index past the second axis), or with `as_quad=True` one quad per cell (drawn only
     through MeshToWire: four lines per quad); `pre_compute` (run by every
     render) recomputes the smooth normals on the device."""
 
@@ -200,9 +202,9 @@ class MeshGrid(MeshBase):
         self.as_quad = bool(as_quad)
         if isinstance(res, int):
             res = res, res
-        if res[0] != res[1]:
-            raise NotImplementedError("MeshGrid's face indexing (grid.py:46-58) covers square grids only")
         self.res = tuple(int(r) for r in res)
+        if min(self.res) < 2:
+            raise ValueError('MeshGrid needs at least 2 x 2 vertices')
         dev = default_device()
         nx, ny = self.res
         # init_pos (tina/mesh/grid.py:15-20)

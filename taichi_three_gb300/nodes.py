@@ -15,20 +15,21 @@ class Node:
     defaults = []
 
     def __init__(self, **kwargs):
-        self.params = {}
-        for dfl, key in zip(self.defaults, self.arguments):
-            if key not in kwargs:
-                if dfl is None:
-                    raise ValueError(f'`{key}` must specified for `{type(self)}`')
-                value = dfl
-            else:
-                value = kwargs[key]
-                del kwargs[key]
-            self.params[key] = as_node(value)
-        for key in kwargs.keys():
+        # Contract of the reference's keyword binding: every declared argument
+        # takes the caller's value or its default; a None default means the
+        # argument is required (ValueError when absent); any keyword the node
+        # does not declare is a TypeError.  Required arguments are checked
+        # before unknown keywords, as there.
+        table = dict(zip(self.arguments, self.defaults))
+        missing = [k for k, d in table.items() if d is None and k not in kwargs]
+        if missing:
+            raise ValueError(f'`{missing[0]}` must specified for `{type(self)}`')
+        unknown = [k for k in kwargs if k not in table]
+        if unknown:
             raise TypeError(
-                f"{type(self).__name__}() got an unexpected keyword argument '{key}', "
+                f"{type(self).__name__}() got an unexpected keyword argument '{unknown[0]}', "
                 f"supported keywords are: {self.arguments}")
+        self.params = {k: as_node(kwargs.get(k, d)) for k, d in table.items()}
 
     def param(self, key):
         return self.params[key]

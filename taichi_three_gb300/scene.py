@@ -31,10 +31,77 @@ def _stream():
     return torch.cuda.current_stream().cuda_stream
 
 
-class TriangleRaster:
+class _KeyRaster:
     """The rasteriser protocol set_object / render_occup / render_color
-    (tina/core/triangle.py:5-153).  Options: maxfaces, smoothing, texturing,
-    culling (default True), clipping (default True)."""
+    (tina/scene/raster.py:183-187) over the engine's packed depth-key buffer.
+
+    Engine.clear_depth empties the frame's keys once per frame
+    (tina/scene/raster.py:177); each render_occup depth-tests the current
+    object against them without clearing them (tina/core/triangle.py:121-125),
+    its faces numbered after the objects rasterised before it in the frame, so
+    an earlier object keeps a pixel on a depth tie (the strict `>` of
+    triangle.py:123); engine.depth then holds the frame's int32 depths.
+    render_color shades only the pixels this object won (occup != -1,
+    triangle.py:134-139), leaving every other pixel of the image as it is."""
+
+    mesh = None
+    _base = 0
+    _nfaces = 0
+
+    def flags(self, tonemap=False):
+        return N.T3_TONEMAP if tonemap else 0
+
+    def _fill_frame(self, fr):
+        pass
+
+    # -- protocol ---------------------------------------------------------
+    def set_object(self, mesh):
+        mesh.pre_compute()
+        self.check_faces(mesh)
+        self.mesh = mesh
+
+    def render_occup(self):
+        """Rasterises the current object into the engine's depth keys."""
+        require_cuda(type(self).__name__ + '.render_occup')
+        lib = N.load()
+        dev = default_device()
+        eng = self.engine
+        if eng.keys is None or eng.keys.numel() != eng.res[0] * eng.res[1]:
+            eng.clear_depth()
+        keep = []
+        ob = N.t3_object()
+        self.mesh._t3_fill(ob.mesh, dev, keep)
+        self._nfaces = ob.nfaces = self.check_faces(self.mesh)
+        self._base = ob.face_base = eng._claim_faces(ob.nfaces)
+        fr = N.t3_frame()
+        eng._t3_fill_frame(fr, self.flags(), 0.0)
+        self._fill_frame(fr)
+        need = 256 + 4 * max(1, ob.nfaces)
+        ws = getattr(self, '_ws', None)
+        if ws is None or ws.numel() < need:
+            self._ws = ws = torch.empty(need, dtype=torch.uint8, device=dev)
+            self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        N.check(lib.t3_raster(C.byref(fr), C.byref(ob), eng.keys.data_ptr(), ws.data_ptr(), ws.numel(),
+                              self._status.data_ptr(), _stream()), 't3_raster')
+        self._keep = keep
+        eng._keys_to_depth()
+
+    @property
+    def occup(self):
+        """This object's winning face per pixel, -1 elsewhere (TriangleRaster.occup)."""
+        ids = (self.engine.keys & 0xFFFFFFFF) - self._base
+        mine = (self.engine.keys != -1) & (ids >= 0) & (ids < self._nfaces)
+        return torch.where(mine, ids, torch.full_like(ids, -1)).to(torch.int32)
+
+    def render_color(self, shader):
+        """Shades the pixels this object won with `shader` (a Shader of the scene)."""
+        shader.shade_from_keys(self, self.engine.keys)
+
+
+class TriangleRaster(_KeyRaster):
+    """TriangleRaster (tina/core/triangle.py:5-153) with the protocol of
+    _KeyRaster.  Options: maxfaces, smoothing, texturing, culling (default
+    True), clipping (default True)."""
 
     def __init__(self, engine, maxfaces=None, smoothing=False, texturing=False, culling=True,
                  clipping=True, **extra_options):
@@ -45,10 +112,6 @@ class TriangleRaster:
         self.texturing = texturing
         self.culling = culling
         self.clipping = clipping
-        self.mesh = None
-        self.keys = None
-        self._ws = None
-        self._status = None
 
     def flags(self, tonemap=False):
         f = 0
@@ -65,60 +128,21 @@ class TriangleRaster:
             raise ValueError(f'mesh has {n} faces, more than maxfaces={self.maxfaces}')
         return n
 
-    # -- protocol ---------------------------------------------------------
-    def set_object(self, mesh):
-        mesh.pre_compute()
-        self.check_faces(mesh)
-        self.mesh = mesh
 
-    def render_occup(self):
-        """Clears this raster's key buffer and rasterises the current object into it."""
-        require_cuda('TriangleRaster.render_occup')
-        lib = N.load()
-        W, H = self.res
-        dev = default_device()
-        if self.keys is None or self.keys.numel() != W * H:
-            self.keys = torch.empty((W, H), dtype=torch.int64, device=dev)
-            self._status = torch.zeros(1, dtype=torch.int32, device=dev)
-        keep = []
-        ob = N.t3_object()
-        self.mesh._t3_fill(ob.mesh, dev, keep)
-        ob.nfaces = self.mesh.get_nfaces()
-        ob.face_base = 0
-        fr = N.t3_frame()
-        self.engine._t3_fill_frame(fr, self.flags(), 0.0)
-        need = 256 + 4 * max(1, ob.nfaces)
-        if self._ws is None or self._ws.numel() < need:
-            self._ws = torch.empty(need, dtype=torch.uint8, device=dev)
-        st = _stream()
-        N.check(lib.t3_clear(self.keys.data_ptr(), W * H, st), 't3_clear')
-        N.check(lib.t3_raster(C.byref(fr), C.byref(ob), self.keys.data_ptr(), self._ws.data_ptr(),
-                              self._ws.numel(), self._status.data_ptr(), st), 't3_raster')
-        self._keep = keep
-
-    @property
-    def occup(self):
-        """Winning face id per pixel, -1 where empty (TriangleRaster.occup)."""
-        k = self.keys
-        ids = (k & 0xFFFFFFFF).to(torch.int32)
-        return torch.where(k == -1, torch.full_like(ids, -1), ids)
-
-    def render_color(self, shader):
-        """Shades the pixels this raster won with `shader` (a Shader of the scene)."""
-        shader.shade_from_keys(self, self.keys)
-
-
-class ParticleRaster:
+class ParticleRaster(_KeyRaster):
     """ParticleRaster (tina/core/particle.py): particles rasterised as shaded
-    spheres into the same depth buffer as the triangles (the scene's frame is
-    rendered by t3_render; particles take the direct rasteriser).  Options
-    kept: maxpars, coloring, clipping."""
+    spheres into the same depth keys as the triangles.  Options kept: maxpars,
+    coloring, clipping."""
 
     def __init__(self, engine, maxpars=None, coloring=True, clipping=True, **extra_options):
         self.engine = engine
+        self.res = engine.res
         self.maxpars = maxpars
         self.coloring = coloring
         self.clipping = clipping
+
+    def flags(self, tonemap=False):
+        return (N.T3_CLIPPING if self.clipping else 0) | (N.T3_TONEMAP if tonemap else 0)
 
     def check_faces(self, pars):
         n = pars.get_npars()
@@ -127,10 +151,10 @@ class ParticleRaster:
         return n
 
 
-class WireframeRaster:
+class WireframeRaster(_KeyRaster):
     """WireframeRaster (tina/core/wireframe.py): each line is walked one pixel
     per step along its major axis (draw_line), with the depth interpolated
-    perspective-correctly between the endpoints, through the same depth buffer
+    perspective-correctly between the endpoints, through the same depth keys
     as the triangles; a pixel a line wins takes the raster's line colour.
     Options kept: maxwires, linewidth (stored: the reference draws one-pixel
     lines whatever its value), linecolor, clipping (default False: a line is
@@ -139,6 +163,7 @@ class WireframeRaster:
     def __init__(self, engine, maxwires=None, linewidth=1.5, linecolor=(.9, .6, 0), clipping=False,
                  **extra_options):
         self.engine = engine
+        self.res = engine.res
         self.maxwires = maxwires
         self.linewidth = linewidth
         self.linecolor = tuple(float(c) for c in np.broadcast_to(np.asarray(linecolor, np.float32), (3,)))
@@ -156,45 +181,92 @@ class WireframeRaster:
         if self.clipping:
             fr.flags |= N.T3_WIRE_CLIPPING
 
+    _fill_frame = _t3_fill
+
 
 class Shader:
     """Shader(img, lighting, material) (tina/core/shader.py:112-135): shades the
-    winning fragments of one raster into `img`."""
+    winning fragments of one raster into `img`.  `outputs` (optional) names
+    more buffers written at the same pixels: 'face_id' (global face id),
+    'depth_f' (float depth)."""
 
-    def __init__(self, img, lighting, material, scene=None):
+    def __init__(self, img, lighting, material, outputs=None):
         self.img = img
         self.lighting = lighting
         self.material = material
-        self.scene = scene
+        self.outputs = outputs or {}
+        self._ws = None
 
-    def shade_from_keys(self, raster, keys):
-        require_cuda('Shader')
-        lib = N.load()
-        sc = N.t3_scene()
-        keep = []
-        dev = default_device()
-        raster.engine._t3_fill_frame(sc.frame, raster.flags(), 0.0)
-        self.lighting._t3_fill(sc.lighting)
-        sc.nobjects = 1
-        ob = sc.objects[0]
-        raster.mesh._t3_fill(ob.mesh, dev, keep)
-        ob.nfaces = raster.mesh.get_nfaces()
-        ob.face_base = 0
-        mat, _ = compile_material(self.material, raster.mesh.attr_stride(), dev, keep)
-        ob.material = mat
+    def _workspace(self, lib, sc, dev):
         size = C.c_size_t()
         N.check(lib.t3_workspace_size(C.byref(sc), N.T3_RASTER_DIRECT, 16, 0, C.byref(size)),
                 't3_workspace_size')
-        ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
-        # shade into a scratch image, then keep only the pixels this raster won
-        W, H = raster.res
-        tmp = torch.empty((W, H, 3), dtype=torch.float32, device=dev)
+        if self._ws is None or self._ws.numel() < size.value:
+            self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+        return self._ws
+
+    def _describe(self, raster, dev, keep, flags):
+        sc = N.t3_scene()
+        raster.engine._t3_fill_frame(sc.frame, raster.flags() | flags, getattr(raster, 'bgcolor', 0.0))
+        raster._fill_frame(sc.frame)
+        self.lighting._t3_fill(sc.lighting)
+        if hasattr(self.lighting, '_t3_fill_device'):
+            self.lighting._t3_fill_device(sc.lighting, dev, keep)
+        return sc
+
+    def shade_from_keys(self, raster, keys):
+        """TriangleRaster.render_color: the pixels whose key belongs to the
+        raster's current object, shaded in place (nothing else is written)."""
+        require_cuda('Shader')
+        lib = N.load()
+        keep = []
+        dev = default_device()
+        sc = self._describe(raster, dev, keep, N.T3_SHADE_OWNED)
+        sc.nobjects = 1
+        ob = sc.objects[0]
+        raster.mesh._t3_fill(ob.mesh, dev, keep)
+        if isinstance(raster, ParticleRaster) and not raster.coloring:
+            ob.mesh.norms = None
+        ob.nfaces = raster._nfaces
+        ob.face_base = raster._base
+        stride = raster.mesh.attr_stride() if hasattr(raster.mesh, 'attr_stride') else 0
+        mat, _ = compile_material(self.material, stride, dev, keep)
+        ob.material = mat
+        self._shade(lib, sc, keys, dev)
+
+    def _shade(self, lib, sc, keys, dev):
         outs = N.t3_outputs()
-        outs.rgb = tmp.data_ptr()
+        outs.rgb = self.img.data_ptr()
+        if 'face_id' in self.outputs:
+            outs.face_id = self.outputs['face_id'].data_ptr()
+        if 'depth_f' in self.outputs:
+            outs.depth_f = self.outputs['depth_f'].data_ptr()
+        ws = self._workspace(lib, sc, dev)
         N.check(lib.t3_shade(C.byref(sc), keys.data_ptr(), ws.data_ptr(), ws.numel(), C.byref(outs),
                              _stream()), 't3_shade')
-        won = (keys != -1).unsqueeze(-1)
-        self.img.copy_(torch.where(won, tmp, self.img))
+
+
+class BackgroundShader(Shader):
+    """BackgroundShader + Engine.render_background (tina/core/shader.py,
+    tina/core/engine.py:42-49): the pixels no fragment reached take the
+    background colour, or under SkyboxLighting the sky along the view ray."""
+
+    def __init__(self, img, lighting, bgcolor=0.0, outputs=None):
+        super().__init__(img, lighting, None, outputs)
+        self.bgcolor = bgcolor
+
+    def shade_empty(self, engine):
+        require_cuda('BackgroundShader')
+        lib = N.load()
+        keep = []
+        dev = default_device()
+        sc = N.t3_scene()
+        engine._t3_fill_frame(sc.frame, N.T3_SHADE_EMPTY, self.bgcolor)
+        self.lighting._t3_fill(sc.lighting)
+        if hasattr(self.lighting, '_t3_fill_device'):
+            self.lighting._t3_fill_device(sc.lighting, dev, keep)
+        sc.nobjects = 0
+        self._shade(lib, sc, engine.keys, dev)
 
 
 class Scene:
@@ -244,6 +316,7 @@ class Scene:
             self.lighting.set_ambient_light([0.1, 0.1, 0.1])
         self.default_material = Diffuse()
         self.materials = []
+        self.shaders = {}
         self.objects = {}
         self.raster_options = {k: options[k] for k in
                                ('maxfaces', 'smoothing', 'texturing', 'culling', 'clipping')
@@ -318,7 +391,8 @@ class Scene:
             obj._t3_fill(ob.mesh, device, keep)
             if isinstance(info.raster, ParticleRaster) and not info.raster.coloring:
                 ob.mesh.norms = None  # white particles (ParticleRaster(coloring=False))
-            n = info.raster.check_faces(obj)
+            check = getattr(info.raster, 'check_faces', None)
+            n = check(obj) if check else (obj.get_npars() if hasattr(obj, 'get_npars') else obj.get_nfaces())
             ob.nfaces = n
             ob.face_base = base
             base += n
@@ -347,6 +421,10 @@ class Scene:
         dev = default_device()
         if self.taa:
             self.engine.randomize_bias(self.accum.count == 0)  # raster.py:173-174
+        if self._foreign_rasters():
+            self._render_protocol(dev)
+            self._post_process()
+            return
         for obj in self.objects:
             obj.pre_compute()
         sc, keep = self.describe(dev)
@@ -356,7 +434,7 @@ class Scene:
         N.check(lib.t3_workspace_size(C.byref(sc), mode, self.tile, self.bin_capacity, C.byref(size)),
                 't3_workspace_size')
         if self._ws is None or self._ws.numel() < size.value:
-            self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+            self._ws = N.new_workspace(size.value, dev)
         outs = N.t3_outputs()
         outs.rgb = self.image.data_ptr()
         outs.face_id = self.face_id.data_ptr()
@@ -380,17 +458,59 @@ class Scene:
             N.check(lib.t3_workspace_size(C.byref(sc), mode, self.tile, self.bin_capacity,
                                           C.byref(size)), 't3_workspace_size')
             if self._ws.numel() < size.value:
-                self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+                self._ws = N.new_workspace(size.value, dev)
         if self.blooming is not None:
             self.blooming.apply(self.image)
             if self.tonemap:
                 self._tonemap_pass.apply(self.image)
+        self._post_process()
+        self._keep = keep
+        self._last_scene = sc
+
+    def _post_process(self):
         if self.fxaa is not None:
             self.fxaa.apply(self.image)
         if self.taa:
             self.accum.update(self.image)
-        self._keep = keep
-        self._last_scene = sc
+
+    _OWN_RASTERS = (TriangleRaster, ParticleRaster, WireframeRaster)
+
+    def _foreign_rasters(self):
+        """True when an object was added with a rasteriser of the caller's own
+        (add_object(..., raster=...)): the frame then runs the three-method
+        protocol object by object, as the reference's Scene.render does."""
+        return any(type(info.raster) not in self._OWN_RASTERS for info in self.objects.values())
+
+    def shader_of(self, material):
+        """The Shader of `material` (Scene.shaders, tina/scene/raster.py:95-110),
+        writing scene.img and, at the same pixels, the face id and float depth."""
+        sh = self.shaders.get(material)
+        if sh is None or sh.img is not self.image:
+            sh = Shader(self.image, self.lighting, material,
+                        outputs={'face_id': self.face_id, 'depth_f': self.depth_f})
+            self.shaders[material] = sh
+        return sh
+
+    def _render_protocol(self, dev):
+        """Scene.render's object loop (tina/scene/raster.py:176-190): clear the
+        depth, then per object set_object / render_occup / render_color through
+        its rasteriser, then the background of the pixels no object reached.
+        The image stays HDR through the loop; the tonemap runs after it."""
+        self._alloc_outputs(dev)
+        self.engine.clear_depth()
+        for obj, info in self.objects.items():
+            shader = self.shader_of(info.material)
+            info.raster.set_object(obj)
+            info.raster.render_occup()
+            info.raster.render_color(shader)
+        bg = BackgroundShader(self.image, self.lighting, self.bgcolor,
+                              outputs={'face_id': self.face_id, 'depth_f': self.depth_f})
+        bg.shade_empty(self.engine)
+        if self.blooming is not None:
+            self.blooming.apply(self.image)
+        if self.tonemap:
+            self._tonemap_pass.apply(self.image)
+        self._last_scene = None
 
     def status(self):
         """Device status bits of the last render (synchronises)."""

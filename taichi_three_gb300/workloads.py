@@ -128,20 +128,29 @@ def batch_scenes(n=64, seed=0, t_min=1_000, t_max=2_000_000, resolutions=(256, 5
 
 
 def wave_grid_scene(grid_res=2048, res=(3840, 2160), skybox=None, mlp=None, nlights=2, seed=0,
-                    **options):
+                    lamps_only=False, **options):
     """Animated grid: MeshGrid(grid_res) over [-1, 1]^2 (displaced per frame by
     MeshGrid.displace_wave: z = 0.1 sin(8x + t) cos(8y + 1.3t)), smooth normals,
     PBR (albedo (0.75, 0.62, 0.5), metallic 0.3, roughness 0.35), lit by the
     environment -- the learned network when `mlp` is given, else 256-sample
     Monte Carlo -- plus nlights point lamps; camera in front of and above the
-    grid, fov 60."""
+    grid, fov 60.  lamps_only: the same scene lit by its point lamps alone
+    (no environment, no ambient)."""
+    from .lighting import Lighting
     from .mesh import MeshGrid
     from .skybox import Skybox, SkyboxLighting, procedural_sky
-    sky = skybox if skybox is not None else Skybox(procedural_sky(512, seed=seed))
-    light = SkyboxLighting(sky, mode='mlp' if mlp is not None else 'mc', mlp=mlp, spp=256, seed=seed)
-    opts = dict(smoothing=True, ibl=True, lighting=light)
+    if lamps_only:
+        light = Lighting()
+        opts = dict(smoothing=True, lighting=light)
+    else:
+        sky = skybox if skybox is not None else Skybox(procedural_sky(512, seed=seed))
+        light = SkyboxLighting(sky, mode='mlp' if mlp is not None else 'mc', mlp=mlp, spp=256, seed=seed)
+        opts = dict(smoothing=True, ibl=True, lighting=light)
     opts.update(options)
     scene = Scene(res[0], res[1], **opts)
+    if lamps_only:
+        scene.lighting = light
+        light.set_ambient_light([0.0, 0.0, 0.0])
     grid = MeshGrid(grid_res)
     scene.add_object(grid, M.PBR(basecolor=(0.75, 0.62, 0.5), metallic=0.3, roughness=0.35))
     pos, inten = point_lights(nlights, seed)

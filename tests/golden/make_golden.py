@@ -9,7 +9,7 @@ the raster path is imported: its subpackage __init__ files (which pull in the
 path tracer, GUI and asset loaders) are replaced by empty packages, and
 tina/hacker.py -- monkey-patches of Taichi internals -- by an empty module.
 
-Usage (where the reference is mounted):  python tests/golden/make_golden.py [name ...]
+Usage:  TINA_REFERENCE=/path/to/taichi_three python tests/golden/make_golden.py [name ...]
 """
 import importlib
 import os
@@ -20,7 +20,8 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get('TINA_REFERENCE', '/root/reference')
+# the taichi_three checkout to run (required: no default location is assumed)
+REFERENCE = os.environ.get('TINA_REFERENCE')
 sys.path.insert(0, HERE)
 
 MODULES = ['tina.common', 'tina.advans', 'tina.matr.nodes', 'tina.matr.material', 'tina.core.engine',
@@ -30,6 +31,8 @@ MODULES = ['tina.common', 'tina.advans', 'tina.matr.nodes', 'tina.matr.material'
 
 
 def load_reference():
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, 'tina')):
+        raise SystemExit('set TINA_REFERENCE to a taichi_three checkout (the directory holding tina/)')
     import taichi_standin
     sys.modules['taichi'] = taichi_standin
     sys.modules['taichi.lang'] = taichi_standin.lang
@@ -59,10 +62,10 @@ def load_reference():
 
 
 def main():
-    from recipes import NAMES, ORACLE_NAMES, build, inputs
+    from recipes import NAMES, build, inputs
     tina, matrix = load_reference()
     only = sys.argv[1:]
-    for name in NAMES + ORACLE_NAMES:
+    for name in NAMES:
         if only and name not in only:
             continue
         t0 = time.time()

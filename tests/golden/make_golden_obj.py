@@ -32,4 +32,7 @@ def main(ref_root):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TINA_REFERENCE')
+    if not root:
+        raise SystemExit('usage: make_golden_obj.py /path/to/taichi_three (or set TINA_REFERENCE)')
+    main(root)

@@ -7,7 +7,7 @@ bilerp, FXAA's neighbours and bilerp), which Taichi leaves undefined; the
 stand-in's clamp_reads mode makes those reads take the nearest element, the
 convention the CUDA passes and the oracle document.
 
-Usage (where the reference is mounted):  python tests/golden/make_golden_postfx.py
+Usage:  TINA_REFERENCE=/path/to/taichi_three python tests/golden/make_golden_postfx.py
 """
 import importlib
 import os

@@ -6,7 +6,7 @@ equirectangular map), run under the Taichi stand-in like
 make_golden.py.  (The reference's SkyboxLighting would also bake prefiltered
 IBL tables from an image asset; the background needs only the skybox.)
 
-Usage (where the reference is mounted):  python tests/golden/make_golden_sky.py
+Usage:  TINA_REFERENCE=/path/to/taichi_three python tests/golden/make_golden_sky.py
 """
 import os
 import sys

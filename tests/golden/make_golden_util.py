@@ -4,7 +4,7 @@ frustum, orthogonal, perspective, scale, translate, quaternion, eularXYZ,
 evaluated on fixed arguments) and tina/util/accumator.py (Accumator.update,
 the TAA running mean, over three seeded frames under the Taichi stand-in).
 
-Usage (where the reference is mounted):  python tests/golden/make_golden_util.py
+Usage:  TINA_REFERENCE=/path/to/taichi_three python tests/golden/make_golden_util.py
 """
 import importlib
 import os

@@ -141,12 +141,7 @@ def _obj(v, f):
 
 NAMES = ['tri_pair', 'sphere_lambert', 'soup_pbr', 'soup_classic', 'soup_transform', 'grid_pbr',
          'two_objects', 'particles', 'pars_mixed', 'wire_soup', 'lines', 'wire_grid', 'smooth_model',
-         'wire_quads', 'textured']
-
-
-# golden scenes checked against the oracle only (the CUDA path is held to the
-# oracle on the same materials by tests/test_gpu_parity.py test_material_variants)
-ORACLE_NAMES = ['materials', 'mesh_edits', 'indexed_ortho']
+         'wire_quads', 'textured', 'materials', 'mesh_edits', 'indexed_ortho']
 
 
 def build(tina, name, arrays, matrix):

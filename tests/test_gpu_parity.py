@@ -162,8 +162,11 @@ def test_mesh_edits_and_multi_object(cuda, oracle_mod, rast):
     assert_parity(g, o)
 
 
-def test_mesh_grid_with_device_normals(cuda, oracle_mod):
-    grid = tina.MeshGrid(64)
+@pytest.mark.parametrize('res', [64, (80, 41), (33, 70)], ids=['square', 'wide', 'tall'])
+def test_mesh_grid_with_device_normals(cuda, oracle_mod, res):
+    """MeshGrid (square, and rectangular both ways) with its normals from
+    pre_compute on the device."""
+    grid = tina.MeshGrid(res)
     x, y = grid.pos[..., 0], grid.pos[..., 1]
     grid.pos[..., 2] = 0.1 * torch.sin(8 * x + 0.3) * torch.cos(8 * y + 0.39)
     scene = tina.Scene(200, 150, smoothing=True)
@@ -175,6 +178,8 @@ def test_mesh_grid_with_device_normals(cuda, oracle_mod):
     assert np.array_equal(nrm_gpu.view(np.uint32), nrm_cpu.view(np.uint32))
     o = oracle_mod.render(scene)  # the descriptor carries the device-computed normals
     assert_parity(g, o)
+    assert (g['face_id'] >= 0).sum() > 5000
+    assert g["face_id"].max() > 0.8 * grid.get_nfaces()  # the far cells are drawn too
 
 
 def test_indexed_meshes(cuda, oracle_mod):
@@ -196,19 +201,96 @@ def test_indexed_meshes(cuda, oracle_mod):
         assert_parity(gpu_render(scene), oracle_mod.render(scene))
 
 
-def test_raster_protocol_methods(cuda, oracle_mod):
-    scene, mesh = random_soup_scene(11, ntri=2000, res=(100, 100))
+def _two_overlapping_soups(seed=11, res=(120, 90)):
+    """Two PBR / Classic soups over the same region (each covers the other's
+    pixels), the second with a MeshTransform, so the depth test across objects
+    decides most covered pixels."""
+    scene, a = random_soup_scene(seed, ntri=1500, res=res)
+    v, n, at = tina.workloads.soup_arrays(1200, seed + 1, median_sigma=0.08, log_sd=0.6)
+    b = tina.SimpleMesh()
+    b.set_face_verts(v)
+    b.set_face_norms(n)
+    b.set_face_attrs(at)
+    bt = tina.MeshTransform(b)
+    bt.set_transform(tina.translate([0.05, -0.03, 0.1]))
+    scene.add_object(bt, tina.workloads.classic_face_material())
+    return scene, a, bt
+
+
+def test_raster_protocol_two_objects(cuda, oracle_mod):
+    """tina/scene/raster.py:177, :183-187 driven by hand: one depth clear, then
+    set_object / render_occup / render_color per object.  The shared depth keys
+    make the objects occlude each other: the frame's depth and ids equal
+    Scene.render's and the oracle's bit for bit, the image within 1e-4."""
+    scene, a, bt = _two_overlapping_soups()
     o = oracle_mod.render(scene)
-    raster = tina.TriangleRaster(scene.engine, smoothing=True)
-    raster.set_object(mesh)
-    raster.render_occup()
-    assert np.array_equal(raster.occup.cpu().numpy(), o['face_id'])
-    img = torch.zeros((100, 100, 3), device='cuda')
-    shader = tina.Shader(img, scene.lighting, scene.objects[mesh].material)
-    raster.render_color(shader)
+    g = gpu_render(scene)
+    nA = a.get_nfaces()
+    both = (o['face_id'] >= 0)
+    assert (o['face_id'] >= nA).sum() > 500 and (both & (o['face_id'] < nA)).sum() > 500
+    eng = scene.engine
+    W, H = scene.res
+    img = torch.zeros((W, H, 3), device='cuda')
+    eng.clear_depth()
+    for k, (obj, info) in enumerate(scene.objects.items()):
+        raster = tina.TriangleRaster(eng, smoothing=True)
+        shader = tina.Shader(img, scene.lighting, info.material)
+        raster.set_object(obj)
+        raster.render_occup()
+        occ = raster.occup.cpu().numpy()
+        if k == 0:
+            # the first object alone: its winners of an empty frame
+            assert (occ >= 0).sum() > 0
+        else:
+            # the second object wins exactly the pixels the frame gives it
+            assert np.array_equal(occ >= 0, o['face_id'] >= nA)
+            assert np.array_equal(occ[occ >= 0] + nA, o['face_id'][occ >= 0])
+        raster.render_color(shader)
+    torch.cuda.synchronize()
+    keys = eng.keys.cpu().numpy()
+    ids = np.where(keys == -1, -1, keys & 0xFFFFFFFF).astype(np.int32)
+    assert np.array_equal(ids, o['face_id'])
+    assert np.array_equal(ids, g['face_id'])
+    assert np.array_equal(eng.depth.cpu().numpy(), o['depth'])
     tina.ToneMapping(scene.res).apply(img)
     won = o['face_id'] >= 0
     assert np.abs(img.cpu().numpy()[won] - o['rgb'][won]).max() <= RGB_TOL
+    assert np.abs(img.cpu().numpy()[won] - g['rgb'][won]).max() <= RGB_TOL
+
+
+class _CallersRaster:
+    """A rasteriser of the caller's own (add_object(raster=...)): it only
+    forwards the three protocol methods to a TriangleRaster."""
+
+    def __init__(self, engine, **options):
+        self.inner = tina.TriangleRaster(engine, **options)
+
+    def set_object(self, mesh):
+        self.inner.set_object(mesh)
+
+    def render_occup(self):
+        self.inner.render_occup()
+
+    def render_color(self, shader):
+        self.inner.render_color(shader)
+
+
+def test_scene_render_with_callers_raster(cuda, oracle_mod):
+    """A raster passed to add_object makes Scene.render run the object loop of
+    the protocol (clear, occup + color per object, background, tonemap); every
+    output equals the oracle's at the GPU bar, particles included."""
+    scene, a, bt = _two_overlapping_soups(seed=5)
+    scene.objects[bt].raster = _CallersRaster(scene.engine, smoothing=True)
+    rng = np.random.default_rng(3)
+    pars = tina.SimpleParticles()
+    pars.set_particles(rng.uniform(-0.8, 0.8, (60, 3)).astype(np.float32))
+    pars.set_particle_radii(rng.uniform(0.02, 0.08, 60).astype(np.float32))
+    scene.add_object(pars, tina.Diffuse(color=0.6))
+    assert scene._foreign_rasters()
+    o = oracle_mod.render(scene)
+    g = gpu_render(scene)
+    assert (o['face_id'] >= a.get_nfaces() + bt.get_nfaces()).sum() > 50  # particles win pixels
+    assert_parity(g, o)
 
 
 def test_tonemap_kernel(cuda, oracle_mod):

@@ -1,11 +1,11 @@
 """Image-based lighting (SkyboxLighting): the CUDA Monte Carlo estimator
 against the oracle, which draws the identical random stream.
 
-Bar: id / depth bit-exact (the raster is unchanged); RGB agrees with the FP32
-oracle within the stated tolerance -- the sample directions go through
+Bar: id / depth bit-exact (the raster is unchanged); RGB within 1e-4 of the
+FP32 oracle, which draws the same samples (the sample directions go through
 sin / cos / atan2 / sqrt, whose last-bit differences between the device and
-host libraries move an environment lookup by a fraction of a texel; the error
-against the FP64 oracle is printed.  A white furnace (uniform sky, white
+host libraries move an environment lookup by a fraction of a texel: a few
+1e-7 in practice); the error against the FP64 oracle is printed.  A white furnace (uniform sky, white
 Lambert) must return the sky exactly.
 """
 import numpy as np
@@ -54,7 +54,7 @@ def test_mc_parity(cuda, oracle_mod, material, raster):
     o64 = oracle_mod.render(scene, fp64=True)
     print(f'{material}/{raster}: max {d.max():.3g} mean {d.mean():.3g}; '
           f'vs FP64 max {np.abs(g["rgb"] - o64["rgb"]).max():.3g}')
-    assert d.mean() < 1e-4 and np.quantile(d, 0.999) < 2e-3 and d.max() < 5e-2
+    assert d.max() <= 1e-4
 
 
 def test_background_is_environment(cuda, oracle_mod):

@@ -211,3 +211,22 @@ def test_multi_object_winner_and_shading(oracle_mod):
         assert np.array_equal(a[k], b[k]), k
     lamp = a['face_id'] == 1
     np.testing.assert_allclose(a['rgb'][lamp][0], tina.aces_tonemap(np.array([1.0, 0.2, 0.1])), rtol=1e-6)
+
+
+@pytest.mark.parametrize('lighting', ['lamps', 'mc'])
+def test_sampled_pixels_equal_the_whole_frame(oracle_mod, lighting):
+    """oracle.pixels_f32 (the oracle of sampled pixels in frames too large to
+    shade whole) returns the whole-frame render's own values bit for bit,
+    Monte Carlo stream included."""
+    opts = {}
+    if lighting == 'mc':
+        sky = tina.Skybox(tina.procedural_sky(16, seed=2))
+        opts = dict(ibl=True, lighting=tina.SkyboxLighting(sky, spp=8, seed=7), nlights=0)
+    scene, _ = random_soup_scene(9, ntri=500, res=(48, 40), **opts)
+    full = oracle_mod.render(scene)
+    rng = np.random.default_rng(0)
+    px = rng.choice(48 * 40, 400, replace=False)
+    rgb, fid = oracle_mod.pixels_f32(scene, px)
+    assert np.array_equal(fid, full['face_id'].reshape(-1)[px])
+    assert (fid >= 0).sum() > 50
+    assert np.array_equal(rgb.view(np.uint32), full['rgb'].reshape(-1, 3)[px].view(np.uint32))
