@@ -52,8 +52,20 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
-                   help="skip the learned-IBL, multi-view batch and animated-grid sections")
-    return p.parse_args()
+                   help="skip every extra section (same as --extras '')")
+    p.add_argument("--extras", default=",".join(EXTRAS),
+                   help="comma-separated extra sections to run after the headline frame: "
+                        + ", ".join(EXTRAS))
+    a = p.parse_args()
+    a.extras = [] if a.no_extras else [x for x in a.extras.split(",") if x]
+    bad = [x for x in a.extras if x not in EXTRAS]
+    if bad:
+        p.error(f"unknown extra sections {bad}")
+    return a
+
+
+# extra sections of the JSON line, each a workload of its own with its roofline
+EXTRAS = ("sphere512", "binned", "learned_ibl", "batch", "anim_grid")
 
 
 def peaks():
@@ -302,7 +314,63 @@ def bench_learned_ibl(flush, tc_peak):
             "stages_ms": {k: v[3] for k, v in res.items()}}, sky, net
 
 
-def bench_batch(flush):
+def traffic_of(section, kernel):
+    """ncu DRAM bytes (read + write) per launch of `kernel` in `section`, from
+    profiles/traffic.json (null when not captured)."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(section, {}).get(kernel)
+    except Exception:
+        return None
+
+
+def hbm_roofline(alg_bytes, ms, peak, peak_kind, what, traffic=None):
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "alg_bytes": alg_bytes, "of": what, "peak_source": peak_kind}
+
+
+def bench_sphere(flush, peak):
+    """512x512 Lambert UV sphere (3,968 faces): launch-bound, a few microseconds."""
+    import taichi_three_gb300 as tina
+    scene, mesh = tina.workloads.sphere_scene(512)
+    ms = time_graph(graph_of(scene.render), 50, flush)
+    stages = stage_times(scene, 20)
+    T, P = mesh.get_nfaces(), 512 * 512
+    alg = 72 * T + 36 * P
+    return {"workload": "UV sphere 512x512 (64 lon x 32 lat: 3,968 faces), Diffuse(0.8), 1 directional lamp",
+            "faces": T, "ms_per_frame": ms, "fps": 1e3 / ms, "mtri_s": T / ms / 1e3,
+            "mpix_s": P / ms / 1e3, "stage_ms": stages,
+            "roofline": hbm_roofline(alg, ms, peak[0], peak[1], "whole frame: 72 B/face + 36 B/px")}
+
+
+def bench_binned(flush, peak):
+    """The headline soup frame through the binned tile rasteriser (tile 16,
+    automatic bin capacity): upload, bin, tile (raster + shade in shared memory)."""
+    import taichi_three_gb300 as tina
+    scene, mesh = tina.workloads.soup_scene(ntri=1_000_000, res=(1920, 1080), seed=0, raster="binned")
+    scene.render()  # settles the bin capacity (re-renders once if a bin overflowed)
+    scene.check_bins = False
+    ms = time_graph(graph_of(scene.render), 20, flush)
+    stages = stage_times(scene, 10)
+    stages = dict(zip(("upload", "bin", "tile"), (stages["clear"], stages["raster"], stages["shade"])))
+    T, P = 1_000_000, 1920 * 1080
+    fid = scene.face_id
+    visible = int(torch.unique(fid[fid >= 0]).numel())
+    alg_bin, alg_tile = 36 * T, 24 * P + visible * (36 + 36 + 20)
+    frame = 92 * T + 20 * P
+    return {"workload": "triangle soup 1920x1080, 1,000,000 faces, PBR per-face, 8 point lamps; binned, tile 16",
+            "bin_capacity": scene.bin_capacity, "ms_per_frame": ms, "mtri_s": T / ms / 1e3,
+            "stage_ms": stages,
+            "roofline": hbm_roofline(alg_tile, stages["tile"], peak[0], peak[1],
+                                     "k_tile: 24 B/px outputs + 92 B per visible face",
+                                     traffic_of("binned", "tile")),
+            "roofline_bin": hbm_roofline(alg_bin, stages["bin"], peak[0], peak[1], "k_bin: 36 B/face",
+                                         traffic_of("binned", "bin")),
+            "frame_roofline": hbm_roofline(frame, ms, peak[0], peak[1],
+                                           "whole frame: 92 B/face + 20 B/px (keys stay on chip)")}
+
+
+def bench_batch(flush, peak):
     """64 views (1e3..2e6 faces, 256..1024 px square, Classic + 8 lamps) in one
     raster launch + one shading launch, against the same frames rendered one
     scene at a time (both captured as CUDA graphs)."""
@@ -320,26 +388,47 @@ def bench_batch(flush):
     tuner = Autotuner(timer=lambda fn: time_graph(graph_of(fn), 3))
     cfg, _ = b.autotune(tuner=tuner, repeats=1)
     ms = time_graph(graph_of(lambda: b.render(cfg)), 10, flush)
+    # positions + normals read once, the 3 albedo channels Classic reads, 36 B/px
+    alg = (72 + 12) * faces + 36 * pix
     return {"workload": "64 views: soups of round(exp(U[ln 1e3, ln 2e6])) faces, square "
                         "256/512/768/1024 px, cameras on the radius-3 sphere, Classic, 8 lamps",
             "faces": faces, "pixels": pix, "ms_per_batch": ms, "mtri_s": faces / ms / 1e3,
             "mpix_s": pix / ms / 1e3, "views_per_s": 64e3 / ms, "per_scene_graph_ms": ms_seq,
-            "speedup_vs_per_scene": ms_seq / ms, "autotuned": cfg}
+            "speedup_vs_per_scene": ms_seq / ms, "autotuned": cfg,
+            "roofline": hbm_roofline(alg, ms, peak[0], peak[1],
+                                     "whole batch: 84 B/face + 36 B/px summed over the views",
+                                     {k: traffic_of("batch", k) for k in ("raster", "shade")})}
 
 
-def bench_anim_grid(sky, net, flush):
+def bench_anim_grid(sky, net, flush, peak, tcp):
     """3840x2160, MeshGrid(2048) displaced per frame, PBR + learned IBL + 2
-    lamps, 120 frames in one CUDA graph."""
+    lamps, 120 frames in one CUDA graph.  Without a trained network (the
+    section run alone) an untrained one of the same shape stands in: the
+    work per frame is the same."""
     import taichi_three_gb300 as tina
+    if net is None:
+        sky = tina.Skybox(tina.procedural_sky(512, seed=0))
+        net = tina.IBLNet(seed=0)
     scene, grid = tina.workloads.wave_grid_scene(skybox=sky, mlp=net)
     fg = tina.FrameGraph(scene, 120, update=lambda k: grid.displace_wave(k / 30.0)).capture()
     ms = time_graph(fg.graph, 3, flush)
     T = grid.get_nfaces()
+    V, P = grid.res[0] * grid.res[1], scene.res[0] * scene.res[1]
+    cov = float((scene.face_id >= 0).float().mean())
+    frame_ms = ms / 120
+    alg = 48 * V + 36 * P                     # vertex stage out + back in, 36 B/px
+    flop = MLP_FLOP_PER_PIXEL * cov * P       # the network on every covered pixel
+    hbm = hbm_roofline(alg, frame_ms, peak[0], peak[1], "per frame: 48 B/vertex + 36 B/px")
+    tc = {"bound": "tensor", "achieved": flop / (frame_ms / 1e3) / 1e12, "peak": tcp,
+          "unit": "TFLOP/s", "flop": flop}
+    tc["frac"] = tc["achieved"] / tcp
     return {"workload": "3840x2160, MeshGrid(2048) (8,380,418 faces), z = 0.1 sin(8x+t) cos(8y+1.3t) "
                         "per frame, PBR + learned IBL + 2 point lamps, 120 frames in one CUDA graph",
-            "ms_per_120_frames": ms, "ms_per_frame": ms / 120, "fps": 120e3 / ms,
-            "mtri_s": T * 120 / ms / 1e3, "coverage": float((scene.face_id >= 0).float().mean()),
-            "status": scene.status()}
+            "ms_per_120_frames": ms, "ms_per_frame": frame_ms, "fps": 120e3 / ms,
+            "mtri_s": T * 120 / ms / 1e3, "coverage": cov, "status": scene.status(),
+            "roofline": hbm if hbm["frac"] >= tc["frac"] else tc, "roofline_hbm": hbm,
+            "roofline_tensor": tc,
+            "traffic": {k: traffic_of("anim_grid", k) for k in ("grid_wave", "grid_normals", "vertex_ndc")}}
 
 
 def cpu_baseline(scene, faces, seconds, label):
@@ -387,11 +476,12 @@ def run_reference(args):
             break
     t = sum(times) / len(times)
     value = faces / t / 1e6
-    cfg = dict(cfg, parallelism="replicas only (rank 0 runs)", l2="n/a (CPU)")
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "Mtri/s",
             "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": cfg,
+            "setup": {"parallelism": "replicas only (rank 0 runs)", "l2": "n/a (CPU)",
+                      "threads": threads},
             "fps": 1.0 / t,
             "cpu_baseline": {"value": value, "unit": "Mtri/s", "cores": threads, "kind": "port",
                              "sample": f"{len(times)} whole frames; the reference's Taichi CPU "
@@ -621,23 +711,34 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": dict(cfg, raster=args.raster, parallelism=f"replicas x{world}",
-                           l2="flushed between steps (256 MB write outside the per-step events)",
-                           graph="one CUDA graph per frame"),
+            "config": cfg,
+            "setup": {"raster": args.raster, "parallelism": f"replicas x{world}",
+                      "l2": "flushed between steps (256 MB write outside the per-step events)",
+                      "graph": "one CUDA graph per frame"},
             "fps": world * 1e3 / ms_per_step, "mpix_s": world * P / (ms_per_step / 1e3) / 1e6,
             "gpu_launches": kernels_per_frame * args.steps, "e2e": e2e, "roofline": roofline,
             "atomics": atomics,
             "clocks": clocks, "wall_s_timed": wall}
     if rank == 0 and not args.no_cpu_baseline and args.workload != "ibl1080":
         line["cpu_baseline"] = cpu_baseline(scene, faces, args.cpu_seconds, cfg["workload"])
-    if rank == 0 and world == 1 and not args.no_extras:
+    if rank == 0 and world == 1 and args.extras:
         del scene, mesh, ws, status
-        torch.cuda.empty_cache()
-        line["learned_ibl"], sky, net = bench_learned_ibl(flush, tc_peak())
-        torch.cuda.empty_cache()
-        line["batch"] = bench_batch(flush)
-        torch.cuda.empty_cache()
-        line["anim_grid"] = bench_anim_grid(sky, net, flush)
+        pk = peaks()
+        sky = net = None
+        for name in EXTRAS:
+            if name not in args.extras:
+                continue
+            torch.cuda.empty_cache()
+            if name == "sphere512":
+                line["sphere512"] = bench_sphere(flush, pk)
+            elif name == "binned":
+                line["binned"] = bench_binned(flush, pk)
+            elif name == "learned_ibl":
+                line["learned_ibl"], sky, net = bench_learned_ibl(flush, tc_peak())
+            elif name == "batch":
+                line["batch"] = bench_batch(flush, pk)
+            elif name == "anim_grid":
+                line["anim_grid"] = bench_anim_grid(sky, net, flush, pk, tc_peak())
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -188,6 +188,33 @@ typedef struct t3_light {
                               124-138, 365-405, 460-472): emission + mean of
                               weight * env(dir) over `spp` samples (+ lamps if any)  */
 #define T3_LIGHT_IBL_MLP 2 /* SkyboxLighting by the learned IBL network             */
+#define T3_LIGHT_IBL_PREFILTERED 3 /* SkyboxLighting's own lookup of prefiltered maps
+                              (tina/core/lighting.py:20-21): Lambert.sample_ibl reads
+                              the diffuse map at the normal (material.py:441-442);
+                              CookTorrance.sample_ibl (material.py:256-277) reads the
+                              two specular maps around its roughness at the mirror
+                              direction, lerps them, and scales by f0 * A + B from a
+                              bilinear LUT read at (VoH, roughness) in texel units;
+                              Mix / Scale weigh their children (material.py:141-145,
+                              :187-191); Add sums them; Phong has no lookup
+                              (T3_EUNSUPPORTED, as the reference raises)            */
+
+/* Prefiltered IBL tables.  Maps use the environment's equirect layout (texel
+ * (i, j) at (i*h + j)*3, FP16 when `half`); the LUT is float [lut_w, lut_h, 2]
+ * (A, B), read at (VoH, roughness) without scaling, as the reference does. */
+#define T3_IBL_LEVELS 7 /* the environment + the maps of roughness 0.03, 0.08,
+                           0.18, 0.35, 0.65, 1.0 (CookTorrance.rough_levels,
+                           tina/matr/material.py:252-253)                    */
+typedef struct t3_ibl_map {
+  const void* data;
+  int32_t w, h, half, _pad;
+} t3_ibl_map;
+typedef struct t3_ibl_tables {
+  t3_ibl_map spec[T3_IBL_LEVELS]; /* spec[0] is the environment itself          */
+  t3_ibl_map diffuse;             /* Lambert.cook_for_ibl's map                  */
+  const float* lut;
+  int32_t lut_w, lut_h;           /* at least 2 x 3 texels (the region the lookup reads) */
+} t3_ibl_tables;
 
 /* MLP-IBL network (see t3_mlp_*): 400 -> 64 -> 64 -> 64 -> 16 (9 used),
  * ReLU hidden layers, BF16 weights (inference) with FP32 biases. */
@@ -208,6 +235,8 @@ typedef struct t3_lighting {
   uint32_t seed;    /* Monte Carlo stream seed                                 */
   int32_t _pad;
   const void* mlp;  /* T3_LIGHT_IBL_MLP: packed network (t3_mlp_pack)         */
+  const t3_ibl_tables* tables; /* T3_LIGHT_IBL_PREFILTERED (host memory, read at
+                                  the call; the maps it points to are device data) */
 } t3_lighting;
 
 /* ---- whole-frame parameters --------------------------------------------- */
@@ -445,6 +474,16 @@ int t3_mlp_pack(const float* params, void* blob, void* stream);
 int t3_mlp_infer(const void* blob, const float* X, int64_t B, float* Y, int32_t* status, void* stream);
 /* FP32 CUDA-core inference of the same network (reference path) */
 int t3_mlp_infer_f32(const float* params, const float* X, int64_t B, float* Y, void* stream);
+
+/* Skybox bake of SkyboxLighting's tables (tina/matr/material.py:279-316,
+ * :407-438): out [out_w, out_h, 3] float, texel (i, j) = the environment
+ * averaged about the direction of its equirect coordinate (i, j) / (shape - 1)
+ * (Skybox.unmapcoor, tina/skybox.py:131-135) over `nsamples` directions
+ * tangentspace(dir) @ spherical(h, xi) weighted by h, with
+ * h = sqrt((1 - xi) / (1 - xi (1 - roughness^2))) (CookTorrance, roughness >= 0)
+ * or h = xi (Lambert, roughness < 0); xi from the counter-based stream `seed`. */
+int t3_ibl_bake(const void* env, int env_w, int env_h, int env_half, float roughness, int nsamples,
+                uint32_t seed, float* out, int out_w, int out_h, void* stream);
 
 /* Reads back the device status word written by the last t3_raster/t3_render
  * (synchronises `stream`). */

@@ -34,6 +34,14 @@ def load():
         lib.oracle_pixels_f64.restype = C.c_int
         lib.oracle_pixels_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_uint32,
                                           C.c_int, C.c_void_p, C.c_void_p]
+        lib.oracle_sample_ibl_f32.restype = C.c_int
+        lib.oracle_sample_ibl_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                              C.c_void_p]
+        lib.oracle_sample_leaf_f32.restype = C.c_int
+        lib.oracle_sample_leaf_f32.argtypes = [C.c_int] + [C.c_void_p] * 5 + [C.c_int64, C.c_void_p,
+                                                                             C.c_void_p]
+        lib.oracle_mix_choice_f32.restype = C.c_int
+        lib.oracle_mix_choice_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         lib.oracle_pixels_f32.restype = C.c_int
         lib.oracle_pixels_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p,
                                           C.c_void_p]
@@ -115,6 +123,43 @@ def pixels_f32(scene, pixels, nthreads=0):
         raise RuntimeError(f'oracle_pixels_f32 failed ({rc})')
     del keep
     return rgb, fid
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def sample_ibl(material_desc, tables, idir, nrm):
+    """material.sample_ibl(tab, idir, nrm) for n pairs (t3_material with constant
+    parameters, t3_ibl_tables with host pointers) -> [n, 3]."""
+    lib = load()
+    idir, nrm = _f32(idir), _f32(nrm)
+    out = np.empty((len(idir), 3), np.float32)
+    rc = lib.oracle_sample_ibl_f32(C.addressof(material_desc), C.addressof(tables), _p(idir), _p(nrm),
+                                   len(idir), _p(out))
+    if rc != 0:
+        raise RuntimeError(f'oracle_sample_ibl_f32 failed ({rc})')
+    return out
+
+
+def sample_leaf(op, param, f0, idir, nrm, xi):
+    """One draw of a leaf sampler per row -> (direction [n, 3], weight [n, 3])."""
+    lib = load()
+    param, f0, idir, nrm, xi = _f32(param), _f32(f0), _f32(idir), _f32(nrm), _f32(xi)
+    d = np.empty((len(idir), 3), np.float32)
+    w = np.empty((len(idir), 3), np.float32)
+    lib.oracle_sample_leaf_f32(int(op), _p(param), _p(f0), _p(idir), _p(nrm), _p(xi), len(idir), _p(d), _p(w))
+    return d, w
+
+
+def mix_choice(fac, xi):
+    """MixMaterial.sample's branch choice -> (weight factor [n, 3], second child chosen [n])."""
+    lib = load()
+    fac, xi = _f32(fac), _f32(xi)
+    w = np.empty((len(xi), 3), np.float32)
+    pick = np.empty(len(xi), np.int32)
+    lib.oracle_mix_choice_f32(_p(fac), _p(xi), len(xi), _p(w), _p(pick))
+    return w, pick.astype(bool)
 
 
 def grid_normals(pos):

@@ -612,6 +612,54 @@ inline void flatten(const t3_material& m, int node, FlatLobe cur, std::vector<Fl
   }
 }
 
+// One draw of a leaf material's sampler (tina/matr/material.py sample()) from
+// the uniforms (xu, xv): the direction and the weight the estimator applies.
+//   Lambert (:399-405): u = sqrt(xu) about the normal, weight 1.
+//   CookTorrance (:365-384): u = sqrt((1 - xu) / (1 - xu (1 - a2))) about
+//     reflect(-V, n), weight F * G of sub_brdf(n, V, dir); mirrored with F = 0
+//     below the surface.  r2 = roughness**2.
+//   Phong (:459-472): u = xu^(1 / (m + 1)) about reflect(-V, n), weight 1 (0
+//     mirrored below the surface).  r2 = shineness.
+template <class R>
+v3<R> sample_leaf(int op, R r2, v3<R> f0, v3<R> viewdir, v3<R> normal, R xu, R xv, v3<R>& dir) {
+  if (op == T3_OP_LAMBERT) {
+    dir = normalized(tangent_dir(normal, std::sqrt(xu), xv));
+    return {R(1), R(1), R(1)};
+  }
+  if (op == T3_OP_COOK) {
+    const R a2s = std::max(R(0), r2);
+    const R u = std::sqrt((R(1) - xu) / (R(1) - xu * (R(1) - a2s)));
+    const v3<R> rdir = reflect(neg(viewdir), normal);
+    v3<R> o = tangent_dir(rdir, u, xv);
+    const R a2 = std::max(MaterialEval<R>::c_eps6(), r2);
+    const v3<R> half = normalized(add(viewdir, o));
+    const R NoL = std::max(MaterialEval<R>::c_eps(), dot(viewdir, normal));
+    const R NoV = std::max(MaterialEval<R>::c_eps(), dot(o, normal));
+    const R VoH = std::min(MaterialEval<R>::c_eps_big(), std::max(MaterialEval<R>::c_eps(), dot(half, o)));
+    const R kk = a2 / R(2);
+    R vdf = R(1) / ((NoV * kk + R(1)) - kk);
+    vdf = vdf * (R(1) / ((NoL * kk + R(1)) - kk));
+    vdf = vdf / (R(1) * (R(1) - a2) + MaterialEval<R>::c_4pi() * a2);
+    const R p5 = pow5(R(1) - VoH);
+    v3<R> fdf = {f0.x + (R(1) - f0.x) * p5, f0.y + (R(1) - f0.y) * p5, f0.z + (R(1) - f0.z) * p5};
+    if (dot(o, normal) < R(0)) { o = neg(o); fdf = {R(0), R(0), R(0)}; }
+    dir = o;
+    return muls(vdf, fdf);
+  }
+  if (op == T3_OP_PHONG) {
+    const R m = r2;
+    const R u = std::pow(xu, R(1) / (m + R(2) - R(1)));
+    const v3<R> rdir = reflect(neg(viewdir), normal);
+    v3<R> o = tangent_dir(rdir, u, xv);
+    R wt = 1;
+    if (dot(o, normal) < R(0)) { o = neg(o); wt = 0; }
+    dir = o;
+    return {wt, wt, wt};
+  }
+  dir = normal;
+  return {R(0), R(0), R(0)};
+}
+
 template <class R>
 v3<R> shade_ibl_mc(const t3_lighting& L, const MaterialEval<R>& me, v3<R> normal, v3<R> viewdir,
                    uint32_t pixel, int spp, uint32_t seed) {
@@ -661,47 +709,127 @@ v3<R> shade_ibl_mc(const t3_lighting& L, const MaterialEval<R>& me, v3<R> normal
       for (int j = 0; j < nl - 1; j++)
         if (xs >= cdf[j]) k = j + 1;
       const t3_node& leaf = me.m->nodes[lobes[k].leaf];
-      v3<R> dir, w;
-      if (leaf.op == T3_OP_LAMBERT) {
-        dir = normalized(tangent_dir(normal, std::sqrt(xu), xv));
-        w = W[k];
-      } else if (leaf.op == T3_OP_COOK) {
-        const R a2s = std::max(R(0), r2[k]);
-        const R u = std::sqrt((R(1) - xu) / (R(1) - xu * (R(1) - a2s)));
-        const v3<R> rdir = reflect(neg(viewdir), normal);
-        v3<R> o = tangent_dir(rdir, u, xv);
-        const R a2 = std::max(MaterialEval<R>::c_eps6(), r2[k]);
-        const v3<R> half = normalized(add(viewdir, o));
-        const R NoL = std::max(MaterialEval<R>::c_eps(), dot(viewdir, normal));
-        const R NoV = std::max(MaterialEval<R>::c_eps(), dot(o, normal));
-        const R VoH = std::min(MaterialEval<R>::c_eps_big(), std::max(MaterialEval<R>::c_eps(), dot(half, o)));
-        const R kk = a2 / R(2);
-        R vdf = R(1) / ((NoV * kk + R(1)) - kk);
-        vdf = vdf * (R(1) / ((NoL * kk + R(1)) - kk));
-        vdf = vdf / (R(1) * (R(1) - a2) + MaterialEval<R>::c_4pi() * a2);
-        const R p5 = pow5(R(1) - VoH);
-        v3<R> fdf = {f0[k].x + (R(1) - f0[k].x) * p5, f0[k].y + (R(1) - f0[k].y) * p5,
-                     f0[k].z + (R(1) - f0[k].z) * p5};
-        if (dot(o, normal) < R(0)) { o = neg(o); fdf = {R(0), R(0), R(0)}; }
-        dir = o;
-        w = muls(vdf, mul(W[k], fdf));
-      } else if (leaf.op == T3_OP_PHONG) {
-        const R m = r2[k];
-        const R u = std::pow(xu, R(1) / (m + R(2) - R(1)));
-        const v3<R> rdir = reflect(neg(viewdir), normal);
-        v3<R> o = tangent_dir(rdir, u, xv);
-        R wt = 1;
-        if (dot(o, normal) < R(0)) { o = neg(o); wt = 0; }
-        dir = o;
-        w = muls(wt, W[k]);
-      } else {
-        continue;
-      }
+      if (leaf.op != T3_OP_LAMBERT && leaf.op != T3_OP_COOK && leaf.op != T3_OP_PHONG) continue;
+      v3<R> dir;
+      const v3<R> lw = sample_leaf<R>(leaf.op, r2[k], f0[k], viewdir, normal, xu, xv, dir);
+      const v3<R> w = mul(W[k], lw);
       if (w.x != R(0) || w.y != R(0) || w.z != R(0)) acc = add(acc, mul(w, env.sample(dir)));
     }
     acc = muls(R(1) / (R)spp, acc);
   }
   return add(emission, acc);
+}
+
+// ---------------------------------------------------------------------------
+// SkyboxLighting's own lookup of prefiltered maps (tina/core/lighting.py:20-21):
+// material.sample_ibl(tab, viewdir, normal) + material.emission().
+// ---------------------------------------------------------------------------
+
+// An equirect map of the prefiltered tables, sampled like Skybox.sample.
+template <class R> struct MapView {
+  const void* data;
+  int w, h, half;
+  v3<R> texel(int64_t i, int64_t j) const {
+    i = i < 0 ? 0 : i >= w ? w - 1 : i;
+    j = j < 0 ? 0 : j >= h ? h - 1 : j;
+    const int64_t o = (i * h + j) * 3;
+    if (half) {
+      const uint16_t* t = reinterpret_cast<const uint16_t*>(data) + o;
+      return {(R)half_to_float(t[0]), (R)half_to_float(t[1]), (R)half_to_float(t[2])};
+    }
+    const float* t = reinterpret_cast<const float*>(data) + o;
+    return {(R)t[0], (R)t[1], (R)t[2]};
+  }
+  v3<R> sample(v3<R> dir) const {
+    const R u = dir.y;
+    R p = std::atan2(-dir.z, dir.x) / R(2.0 * M_PI);
+    p = p - std::floor(p);
+    const R cx = p * (R)(w - 1), cy = (u * R(0.5) + R(0.5)) * (R)(h - 1);
+    const R fx = std::floor(cx), fy = std::floor(cy);
+    const int64_t ix = (int64_t)fx, iy = (int64_t)fy;
+    const R x1 = cx - fx, y1 = cy - fy, x0 = R(1) - x1, y0 = R(1) - y1;
+    return add(add(muls(x1 * y1, texel(ix + 1, iy + 1)), muls(x1 * y0, texel(ix + 1, iy))),
+               add(muls(x0 * y0, texel(ix, iy)), muls(x0 * y1, texel(ix, iy + 1))));
+  }
+};
+template <class R> inline MapView<R> map_view(const t3_ibl_map& m) { return {m.data, m.w, m.h, m.half}; }
+
+// bilerp(lut, (VoH, roughness)) of tina/common.py:141-150 at the point in
+// texel units (the reference does not scale it to the table); A, B = the
+// table's first two channels, +1 texels clamped to the table
+template <class R> inline void lut_ab(const t3_ibl_tables& T, R px, R py, R& A, R& B) {
+  const R Ix = std::floor(px), Iy = std::floor(py);
+  const R x0 = px - Ix, x1 = py - Iy, y0 = R(1) - x0, y1 = R(1) - x1;
+  auto at = [&](int64_t i, int64_t j, int c) {
+    i = i < 0 ? 0 : i >= T.lut_w ? T.lut_w - 1 : i;
+    j = j < 0 ? 0 : j >= T.lut_h ? T.lut_h - 1 : j;
+    return (R)T.lut[(i * T.lut_h + j) * 2 + c];
+  };
+  const int64_t ix = (int64_t)Ix, iy = (int64_t)Iy;
+  for (int c = 0; c < 2; c++) {
+    R r = (at(ix + 1, iy + 1, c) * x0) * x1;
+    r = r + (at(ix + 1, iy, c) * x0) * y1;
+    r = r + (at(ix, iy, c) * y0) * y1;
+    r = r + (at(ix, iy + 1, c) * y0) * x1;
+    (c ? B : A) = r;
+  }
+}
+
+// CookTorrance.rough_levels (tina/matr/material.py:251-253): pairs (a, a - b)
+// of consecutive levels, evaluated in double (Python) and used as float
+// constants in the kernel
+inline void rough_level(int id, double& rough, double& step) {
+  static const double lv[6] = {0.03, 0.08, 0.18, 0.35, 0.65, 1.0};
+  rough = lv[id];
+  step = lv[id] - (id ? lv[id - 1] : 0.0);
+}
+
+// CookTorrance.sample_ibl (tina/matr/material.py:256-277)
+template <class R>
+v3<R> cook_sample_ibl(const t3_ibl_tables& T, R roughness, v3<R> f0, v3<R> idir, v3<R> nrm) {
+  const v3<R> rdir = reflect(neg(idir), nrm);
+  v3<R> wei = {R(1), R(1), R(1)};
+  for (int id = 0; id < 6; id++) {
+    double rough_d, step_d;
+    rough_level(id, rough_d, step_d);
+    const R lo = cst<R>(rough_d - step_d), rough = cst<R>(rough_d), step = cst<R>(step_d);
+    if (lo <= roughness && roughness <= rough) {
+      const v3<R> w1 = map_view<R>(T.spec[id]).sample(rdir);
+      const v3<R> w2 = map_view<R>(T.spec[id + 1]).sample(rdir);
+      const R fac2 = (rough - roughness) / step;
+      wei = add(muls(R(1) - fac2, w2), muls(fac2, w1));  // lerp(fac2, wei2, wei1)
+    }
+  }
+  const v3<R> half = normalized(add(idir, rdir));
+  const R VoH = fmin_(MaterialEval<R>::c_eps_big(), fmax_(MaterialEval<R>::c_eps(), dot(half, rdir)));
+  R A, B;
+  lut_ab<R>(T, VoH, roughness, A, B);
+  return {wei.x * (f0.x * A + B), wei.y * (f0.y * A + B), wei.z * (f0.z * A + B)};
+}
+
+// material.sample_ibl over the material tree: Lambert (:441-442), CookTorrance,
+// Mix (:141-145), Scale (:187-191); Add sums its children and Emission gives 0
+// (the reference has neither; Phong has no lookup there and is refused)
+template <class R>
+v3<R> sample_ibl(const MaterialEval<R>& me, const t3_ibl_tables& T, int i, v3<R> idir, v3<R> nrm) {
+  const t3_node& n = me.m->nodes[i];
+  switch (n.op) {
+  case T3_OP_LAMBERT:
+    return map_view<R>(T.diffuse).sample(nrm);
+  case T3_OP_COOK:
+    return cook_sample_ibl<R>(T, me.value(n.a).v.x, me.value(n.b).v, idir, nrm);
+  case T3_OP_MIX: {
+    const v3<R> fac = me.value(n.c).v;
+    const v3<R> w1 = sample_ibl(me, T, n.a, idir, nrm), w2 = sample_ibl(me, T, n.b, idir, nrm);
+    return add(mul(v3<R>{R(1) - fac.x, R(1) - fac.y, R(1) - fac.z}, w1), mul(fac, w2));
+  }
+  case T3_OP_SCALE:
+    return mul(me.value(n.b).v, sample_ibl(me, T, n.a, idir, nrm));
+  case T3_OP_ADD:
+    return add(sample_ibl(me, T, n.a, idir, nrm), sample_ibl(me, T, n.b, idir, nrm));
+  default:
+    return {R(0), R(0), R(0)};
+  }
 }
 
 // Lighting.shade_color (tina/core/lighting.py:84-98)
@@ -982,6 +1110,17 @@ v3<R> shade_pixel(const Ctx<R>& cx, const t3_object& ob, const Mesh<R>& mesh, in
     }
     return c;
   }
+  if (L.mode == T3_LIGHT_IBL_PREFILTERED && L.tables) {
+    // SkyboxLighting.shade_color: sample_ibl(tab, viewdir, normal) + emission
+    v3<R> c = add(sample_ibl(me, *L.tables, me.m->root, viewdir, normal), me.emission(me.m->root).v);
+    if (L.nlights > 0) {
+      t3_lighting lamps = L;
+      lamps.ambient[0] = lamps.ambient[1] = lamps.ambient[2] = 0.0f;
+      v3<R> l = shade_lamps(lamps, me, pos, normal, viewdir);
+      c = add(c, sub(l, me.emission(me.m->root).v));
+    }
+    return c;
+  }
   return shade_lamps(L, me, pos, normal, viewdir);
 }
 
@@ -1195,7 +1334,8 @@ int render(const t3_scene* sc, int mode, float* rgb, float* rgb_pre, double* rgb
     }
   }
 
-  if (sc->lighting.mode == T3_LIGHT_IBL_MC || sc->lighting.mode == T3_LIGHT_IBL_MLP) {
+  if (sc->lighting.mode == T3_LIGHT_IBL_MC || sc->lighting.mode == T3_LIGHT_IBL_MLP ||
+      sc->lighting.mode == T3_LIGHT_IBL_PREFILTERED) {
 #pragma omp parallel for schedule(static) if (mode == 1)
     for (int64_t i = 0; i < P; i++)
       if (gid[i] < 0) img[i] = background_pixel(cx, (int32_t)(i / H), (int32_t)(i % H));
@@ -1286,7 +1426,8 @@ int shade_pixels(const t3_scene* sc, const int64_t* pixels, int64_t n, int spp, 
   cx.spp = spp;
   cx.seed = seed;
   for (int i = 0; i < 16; i++) { cx.W2V.m[i] = fr.W2V[i]; cx.V2W.m[i] = fr.V2W[i]; }
-  const bool ibl = sc->lighting.mode == T3_LIGHT_IBL_MC || sc->lighting.mode == T3_LIGHT_IBL_MLP;
+  const bool ibl = sc->lighting.mode == T3_LIGHT_IBL_MC || sc->lighting.mode == T3_LIGHT_IBL_MLP ||
+                   sc->lighting.mode == T3_LIGHT_IBL_PREFILTERED;
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t q = 0; q < n; q++) {
     const int64_t i = pixels[q];
@@ -1312,6 +1453,61 @@ int shade_pixels(const t3_scene* sc, const int64_t* pixels, int64_t n, int spp, 
 }
 
 extern "C" {
+
+// SkyboxLighting's lookup for n (view direction, normal) pairs of a material
+// whose parameters are constants: out[n, 3] = material.sample_ibl(tab, idir,
+// nrm) with the tables T (the pin against the reference's own sample_ibl).
+int oracle_sample_ibl_f32(const t3_material* mat, const t3_ibl_tables* T, const float* idir, const float* nrm,
+                          int64_t n, float* out) {
+  for (int64_t q = 0; q < n; q++) {
+    Frag<float> fr{};
+    fr.normal = {nrm[3 * q], nrm[3 * q + 1], nrm[3 * q + 2]};
+    fr.attr = nullptr;
+    MaterialEval<float> me{mat, &fr};
+    const v3<float> r = sample_ibl(me, *T, mat->root, v3<float>{idir[3 * q], idir[3 * q + 1], idir[3 * q + 2]},
+                                   fr.normal);
+    out[3 * q] = r.x; out[3 * q + 1] = r.y; out[3 * q + 2] = r.z;
+  }
+  return 0;
+}
+
+// One draw of a leaf sampler for n inputs: op (T3_OP_LAMBERT / COOK / PHONG),
+// param = roughness (its square is taken) or shineness, f0 [n, 3], uniforms
+// xi [n, 2]; out_dir / out_w [n, 3].
+int oracle_sample_leaf_f32(int op, const float* param, const float* f0, const float* idir, const float* nrm,
+                           const float* xi, int64_t n, float* out_dir, float* out_w) {
+  for (int64_t q = 0; q < n; q++) {
+    const float r2 = op == T3_OP_COOK ? param[q] * param[q] : param[q];
+    v3<float> dir;
+    const v3<float> w = sample_leaf<float>(op, r2, v3<float>{f0[3 * q], f0[3 * q + 1], f0[3 * q + 2]},
+                                           v3<float>{idir[3 * q], idir[3 * q + 1], idir[3 * q + 2]},
+                                           v3<float>{nrm[3 * q], nrm[3 * q + 1], nrm[3 * q + 2]}, xi[2 * q],
+                                           xi[2 * q + 1], dir);
+    out_dir[3 * q] = dir.x; out_dir[3 * q + 1] = dir.y; out_dir[3 * q + 2] = dir.z;
+    out_w[3 * q] = w.x; out_w[3 * q + 1] = w.y; out_w[3 * q + 2] = w.z;
+  }
+  return 0;
+}
+
+// MixMaterial.sample's choice (tina/matr/material.py:124-138) for n draws:
+// the second child when xi < smoothlerp(avg(fac), .12, .88), with weight
+// fac / p, else the first with (1 - fac) / (1 - p); out_w [n, 3], pick [n].
+int oracle_mix_choice_f32(const float* fac, const float* xi, int64_t n, float* out_w, int32_t* pick) {
+  for (int64_t q = 0; q < n; q++) {
+    const v3<float> f = {fac[3 * q], fac[3 * q + 1], fac[3 * q + 2]};
+    const float p = mix_prob((f.x + f.y + f.z) / 3.0f);
+    if (xi[q] < p) {
+      pick[q] = 1;
+      out_w[3 * q] = f.x / p; out_w[3 * q + 1] = f.y / p; out_w[3 * q + 2] = f.z / p;
+    } else {
+      pick[q] = 0;
+      out_w[3 * q] = (1.0f - f.x) / (1.0f - p);
+      out_w[3 * q + 1] = (1.0f - f.y) / (1.0f - p);
+      out_w[3 * q + 2] = (1.0f - f.z) / (1.0f - p);
+    }
+  }
+  return 0;
+}
 
 // FP64 shading of selected pixels with the IBL sample count / seed overridden
 // (spp > 0): the converged reference image for error statements.

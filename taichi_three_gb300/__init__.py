@@ -21,7 +21,7 @@ from .mesh import (MAX, ConnectiveMesh, MeshFlatNormal, MeshFlipCulling, MeshFli
 from .engine import Engine
 from .scene import BackgroundShader, ParticleRaster, Scene, Shader, TriangleRaster, WireframeRaster
 from .postp import Accumator, Blooming, FXAA, ToneMapping, aces_tonemap
-from .skybox import PlainSkybox, Skybox, SkyboxLighting, procedural_sky
+from .skybox import IBLTables, PlainSkybox, Skybox, SkyboxLighting, procedural_sky
 from .pipeline import FramePipeline
 from . import workloads
 from .assimp import readobj

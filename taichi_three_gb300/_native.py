@@ -44,7 +44,7 @@ T3_OP_CONST, T3_OP_ATTR, T3_OP_INPUT, T3_OP_FRESNEL, T3_OP_TEXTURE, T3_OP_CHECKE
 T3_OP_LAMBERT, T3_OP_PHONG, T3_OP_COOK, T3_OP_EMISSION = 16, 17, 18, 19
 T3_OP_MIX, T3_OP_SCALE, T3_OP_ADD = 32, 33, 34
 
-T3_LIGHT_LAMPS, T3_LIGHT_IBL_MC, T3_LIGHT_IBL_MLP = 0, 1, 2
+T3_LIGHT_LAMPS, T3_LIGHT_IBL_MC, T3_LIGHT_IBL_MLP, T3_LIGHT_IBL_PREFILTERED = 0, 1, 2, 3
 T3_MLP_IN, T3_MLP_HID, T3_MLP_OUT = 400, 64, 16
 T3_STATUS_BIG_OVERFLOW, T3_STATUS_BIN_OVERFLOW, T3_STATUS_TIMEOUT = 1, 2, 4
 T3_RASTER_DIRECT, T3_RASTER_BINNED = 0, 1
@@ -94,11 +94,25 @@ class t3_light(C.Structure):
     _fields_ = [("dir", C.c_float * 4), ("color", C.c_float * 4)]
 
 
+T3_IBL_LEVELS = 7
+
+
+class t3_ibl_map(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("w", C.c_int32), ("h", C.c_int32), ("half", C.c_int32),
+                ("_pad", C.c_int32)]
+
+
+class t3_ibl_tables(C.Structure):
+    _fields_ = [("spec", t3_ibl_map * T3_IBL_LEVELS), ("diffuse", t3_ibl_map), ("lut", C.c_void_p),
+                ("lut_w", C.c_int32), ("lut_h", C.c_int32)]
+
+
 class t3_lighting(C.Structure):
     _fields_ = [("mode", C.c_int32), ("nlights", C.c_int32), ("ambient", C.c_float * 4),
                 ("lights", t3_light * T3_MAX_LIGHTS), ("env", C.c_void_p), ("env_w", C.c_int32),
                 ("env_h", C.c_int32), ("env_half", C.c_int32), ("spp", C.c_int32),
-                ("seed", C.c_uint32), ("_pad", C.c_int32), ("mlp", C.c_void_p)]
+                ("seed", C.c_uint32), ("_pad", C.c_int32), ("mlp", C.c_void_p),
+                ("tables", C.POINTER(t3_ibl_tables))]
 
 
 class t3_scene(C.Structure):
@@ -170,6 +184,8 @@ SIGNATURES = {
     "t3_mlp_pack": (C.c_int, [_VP, _VP, _VP]),
     "t3_mlp_infer": (C.c_int, [_VP, _VP, _I64, _VP, _VP, _VP]),
     "t3_mlp_infer_f32": (C.c_int, [_VP, _VP, _I64, _VP, _VP]),
+    "t3_ibl_bake": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, C.c_uint32, _VP,
+                              C.c_int, C.c_int, _VP]),
     "t3_event_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "t3_event_destroy": (C.c_int, [_VP]),
     "t3_event_elapsed_ms": (C.c_int, [_VP, _VP, C.POINTER(C.c_float)]),

@@ -162,11 +162,22 @@ int make_dev_scene(const t3_scene& sc, DevScene& out, bool first_ids_free) {
     if (sc.lighting.mode == T3_LIGHT_IBL_MLP &&
         (!sc.lighting.mlp || (reinterpret_cast<uintptr_t>(sc.lighting.mlp) & 15) != 0))
       return T3_EINVAL;
+  } else if (sc.lighting.mode == T3_LIGHT_IBL_PREFILTERED) {
+    const t3_ibl_tables* T = sc.lighting.tables;
+    if (!sc.lighting.env || sc.lighting.env_w < 2 || sc.lighting.env_h < 2 || !T) return T3_EINVAL;
+    for (int k = 0; k <= T3_IBL_LEVELS; k++) {
+      const t3_ibl_map& m = k < T3_IBL_LEVELS ? T->spec[k] : T->diffuse;
+      if (!m.data || m.w < 2 || m.h < 2 || (reinterpret_cast<uintptr_t>(m.data) & 3) != 0) return T3_EINVAL;
+    }
+    if (!T->lut || T->lut_w < 2 || T->lut_h < 2 || (reinterpret_cast<uintptr_t>(T->lut) & 7) != 0)
+      return T3_EINVAL;
+    out.tables = *T;
   } else if (sc.lighting.mode != T3_LIGHT_LAMPS) {
     return T3_EINVAL;
   }
   out.frame = sc.frame;
   out.lighting = sc.lighting;
+  out.lighting.tables = nullptr;  // a host pointer: kernels read out.tables
   out.nobjects = sc.nobjects;
   int64_t total = 0;
   for (int o = 0; o < sc.nobjects; o++) {
@@ -181,6 +192,11 @@ int make_dev_scene(const t3_scene& sc, DevScene& out, bool first_ids_free) {
     out.obj[o].nfaces = ob.nfaces;
     r = flatten_material(ob.material, out.obj[o].mat);
     if (r) return r;
+    if (sc.lighting.mode == T3_LIGHT_IBL_PREFILTERED) {
+      // Phong has no prefiltered lookup (IMaterial.sample_ibl raises, material.py:39-40)
+      for (int k = 0; k < out.obj[o].mat.nlobes; k++)
+        if (out.obj[o].mat.lobes[k].kind == T3_OP_PHONG && !is_wire(ob.mesh)) return T3_EUNSUPPORTED;
+    }
     if (sc.lighting.mode == T3_LIGHT_IBL_MLP) {
       // the network covers Lambert and one CookTorrance lobe (plus emission)
       int cook = 0;

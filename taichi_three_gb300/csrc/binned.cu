@@ -280,6 +280,8 @@ static cudaError_t launch_tile_nl(const DevScene* sc, const BinArgs& bins, int n
     return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_LAMPS>(sc, bins, ntiles, out, st);
   if (bins.light_mode == T3_LIGHT_IBL_MC)
     return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_IBL_MC>(sc, bins, ntiles, out, st);
+  if (bins.light_mode == T3_LIGHT_IBL_PREFILTERED)
+    return launch_tile_b<TS, BLOCK, NL, T3_LIGHT_IBL_PREFILTERED>(sc, bins, ntiles, out, st);
   if (bins.light_mode == T3_LIGHT_IBL_MLP)  // visibility only: one instance serves every NL
     return launch_tile_b<TS, BLOCK, 2, T3_LIGHT_IBL_MLP>(sc, bins, ntiles, out, st);
   return cudaErrorInvalidValue;

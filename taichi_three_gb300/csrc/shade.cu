@@ -116,6 +116,10 @@ cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const 
     launch_shade_m<T3_LIGHT_IBL_MC, true>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_IBL_MC)
     launch_shade_m<T3_LIGHT_IBL_MC, false>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
+  else if (light_mode == T3_LIGHT_IBL_PREFILTERED && textured)
+    launch_shade_m<T3_LIGHT_IBL_PREFILTERED, true>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
+  else if (light_mode == T3_LIGHT_IBL_PREFILTERED)
+    launch_shade_m<T3_LIGHT_IBL_PREFILTERED, false>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_IBL_MLP)
     return launch_shade_mlp(sc_host, keys, rec, out, status, st);
   else

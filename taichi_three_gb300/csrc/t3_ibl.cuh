@@ -232,4 +232,80 @@ __device__ __forceinline__ V3 ibl_mc(const IblLobes<NL>& L, V3 n, V3 vdir, const
   return (1.0f / (float)spp) * acc;
 }
 
+// ---- SkyboxLighting's prefiltered lookup (T3_LIGHT_IBL_PREFILTERED) ---------
+__device__ __forceinline__ Env map_env(const t3_ibl_map& m) { return Env{m.data, m.w, m.h, m.half}; }
+
+// bilerp(lut, (VoH, roughness)) (tina/common.py:141-150) at the point in
+// texel units, as CookTorrance.sample_ibl reads it (material.py:275); the +1
+// texels clamped to the table
+__device__ __forceinline__ void lut_ab(const t3_ibl_tables& T, float px, float py, float& A, float& B) {
+  const float Ix = floorf(px), Iy = floorf(py);
+  const float x0 = px - Ix, x1 = py - Iy, y0 = 1.0f - x0, y1 = 1.0f - x1;
+  const int ix = (int)Ix, iy = (int)Iy;
+  auto at = [&](int i, int j) {
+    i = min(max(i, 0), T.lut_w - 1);
+    j = min(max(j, 0), T.lut_h - 1);
+    return __ldg(reinterpret_cast<const float2*>(T.lut) + ((int64_t)i * T.lut_h + j));
+  };
+  const float2 a = at(ix + 1, iy + 1), b = at(ix + 1, iy), c = at(ix, iy), d = at(ix, iy + 1);
+  A = ((a.x * x0) * x1 + (b.x * x0) * y1) + ((c.x * y0) * y1 + (d.x * y0) * x1);
+  B = ((a.y * x0) * x1 + (b.y * x0) * y1) + ((c.y * y0) * y1 + (d.y * y0) * x1);
+}
+
+// CookTorrance.sample_ibl (tina/matr/material.py:256-277): the maps of the two
+// roughness levels around `r` at the mirror direction, lerped, times
+// f0 * A + B.  rough_levels (:251-253) pair each level with its step from the
+// previous one; the ranges are tested in order and the last match wins.
+__device__ __forceinline__ V3 cook_prefiltered(const t3_ibl_tables& T, float r, V3 f0, V3 n, V3 vdir) {
+  constexpr double lv[7] = {0.0, 0.03, 0.08, 0.18, 0.35, 0.65, 1.0};
+  const V3 rdir = reflect3(v3(-vdir.x, -vdir.y, -vdir.z), n);
+  V3 wei = v3(1.f, 1.f, 1.f);
+#pragma unroll
+  for (int id = 0; id < 6; id++) {
+    const float rough = (float)lv[id + 1], step = (float)(lv[id + 1] - lv[id]);
+    const float lo = (float)(lv[id + 1] - (lv[id + 1] - lv[id]));
+    if (lo <= r && r <= rough) {
+      const V3 w1 = env_sample(map_env(T.spec[id]), rdir);
+      const V3 w2 = env_sample(map_env(T.spec[id + 1]), rdir);
+      const float fac2 = (rough - r) / step;
+      wei = (1.0f - fac2) * w2 + fac2 * w1;  // lerp(fac2, wei2, wei1)
+    }
+  }
+  const V3 half = normalized(vdir + rdir);
+  const float VoH = fminf(1.0f, fmaxf(1e-10f, dot(half, rdir)));
+  float A, B;
+  lut_ab(T, VoH, r, A, B);
+  return v3(wei.x * (f0.x * A + B), wei.y * (f0.y * A + B), wei.z * (f0.z * A + B));
+}
+
+// material.sample_ibl summed over the flattened lobes: each lobe's weight is
+// the product of the Mix / Scale factors on its path (Mix: (1 - f) w1 + f w2,
+// material.py:141-145; Scale: f w, :187-191); Lambert reads the diffuse map at
+// the normal (:441-442).  Returns the emission separately.
+template <int NL, bool TEX>
+__device__ __forceinline__ V3 ibl_prefiltered(const DevMaterial& mat, const t3_ibl_tables& T, const Frag& fg,
+                                              V3 vdir, V3& emission) {
+  V3 acc = v3(0.f, 0.f, 0.f);
+  emission = v3(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < NL; k++) {
+    if (k >= mat.nlobes) continue;
+    const DevLobe& lb = mat.lobes[k];
+    V3 w = v3(1.f, 1.f, 1.f);
+    for (int j = 0; j < lb.nfac; j++) {
+      const V3 f = eval_value<TEX>(mat, lb.fac[j] & 0xFFFF, fg);
+      w = w * ((lb.fac[j] & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
+    }
+    if (lb.kind == T3_OP_EMISSION) {
+      emission = emission + w;
+    } else if (lb.kind == T3_OP_LAMBERT) {
+      acc = acc + w * env_sample(map_env(T.diffuse), fg.normal);
+    } else if (lb.kind == T3_OP_COOK) {
+      const float r = eval_value<TEX>(mat, lb.p0, fg).x;
+      acc = acc + w * cook_prefiltered(T, r, eval_value<TEX>(mat, lb.p1, fg), fg.normal, vdir);
+    }
+  }
+  return acc;
+}
+
 } // namespace t3

@@ -78,10 +78,11 @@ struct DevObject {
 
 struct DevScene {
   t3_frame frame;
-  t3_lighting lighting;
+  t3_lighting lighting;  // lighting.tables is cleared: the tables are copied below
   int32_t nobjects;
   int32_t _pad;
   DevObject obj[T3_MAX_OBJECTS];
+  t3_ibl_tables tables;  // T3_LIGHT_IBL_PREFILTERED
 };
 // the shading kernels read each lamp as two float4 loads
 static_assert((offsetof(DevScene, lighting) + offsetof(t3_lighting, lights)) % 16 == 0,

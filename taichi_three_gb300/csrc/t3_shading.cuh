@@ -493,6 +493,17 @@ __device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const
     eval_material<NL, TEX, SIG>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
     color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
     color = color + lamps_term<NL, SIG>(lt, L, g.fg, g.vdir);
+  } else if (MODE == T3_LIGHT_IBL_PREFILTERED) {
+    // SkyboxLighting.shade_color (lighting.py:20-21) with its prefiltered tables
+    V3 emi;
+    color = ibl_prefiltered<NL, TEX>(g.ob->mat, sc->tables, g.fg, g.vdir, emi);
+    color = emi + color;
+    if (lt.nlights > 0) {
+      LobeState<NL> Ll;
+      V3 amb, e2;
+      eval_material<NL, TEX, SIG>(g.ob->mat, g.fg, g.vdir, Ll, amb, e2);
+      color = color + lamps_term<NL, SIG>(lt, Ll, g.fg, g.vdir);
+    }
   } else {
     // SkyboxLighting.shade_color (lighting.py:20-21): IBL + emission
     IblLobes<NL> L;

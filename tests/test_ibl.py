@@ -27,7 +27,7 @@ def _render(scene):
 
 def test_white_furnace(cuda):
     sky = tina.PlainSkybox((1.0, 1.0, 1.0))
-    scene = tina.Scene(96, ibl=True, tonemap=False, lighting=tina.SkyboxLighting(sky, spp=16))
+    scene = tina.Scene(96, ibl=True, tonemap=False, lighting=tina.SkyboxLighting(sky, mode='mc', spp=16))
     scene.add_object(tina.PrimitiveMesh.sphere(), tina.Diffuse(color=1.0))
     g = _render(scene)
     covered = g['face_id'] >= 0
@@ -37,7 +37,7 @@ def test_white_furnace(cuda):
 
 def _ibl_scene(seed, material, raster='direct', spp=4, res=(64, 48)):
     sky = tina.Skybox(tina.procedural_sky(32, seed=seed))
-    light = tina.SkyboxLighting(sky, spp=spp, seed=seed + 100)
+    light = tina.SkyboxLighting(sky, mode='mc', spp=spp, seed=seed + 100)
     return random_soup_scene(seed, ntri=200, res=res, material=material, nlights=0, ibl=True,
                              lighting=light, raster=raster)[0]
 

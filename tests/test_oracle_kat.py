@@ -221,7 +221,7 @@ def test_sampled_pixels_equal_the_whole_frame(oracle_mod, lighting):
     opts = {}
     if lighting == 'mc':
         sky = tina.Skybox(tina.procedural_sky(16, seed=2))
-        opts = dict(ibl=True, lighting=tina.SkyboxLighting(sky, spp=8, seed=7), nlights=0)
+        opts = dict(ibl=True, lighting=tina.SkyboxLighting(sky, mode='mc', spp=8, seed=7), nlights=0)
     scene, _ = random_soup_scene(9, ntri=500, res=(48, 40), **opts)
     full = oracle_mod.render(scene)
     rng = np.random.default_rng(0)
