@@ -192,6 +192,7 @@ int make_dev_scene(const t3_scene& sc, DevScene& out, bool first_ids_free) {
     out.obj[o].nfaces = ob.nfaces;
     r = flatten_material(ob.material, out.obj[o].mat);
     if (r) return r;
+    find_fast_material(out.obj[o].mat, out.obj[o].fast);
     if (sc.lighting.mode == T3_LIGHT_IBL_PREFILTERED) {
       // Phong has no prefiltered lookup (IMaterial.sample_ibl raises, material.py:39-40)
       for (int k = 0; k < out.obj[o].mat.nlobes; k++)
@@ -215,6 +216,43 @@ int make_dev_scene(const t3_scene& sc, DevScene& out, bool first_ids_free) {
     }
   }
   return T3_OK;
+}
+
+static bool plain_value(const DevMaterial& m, int i) {
+  return i >= 0 && i < m.nnodes && is_basic(m.nodes[i].op);
+}
+
+void find_fast_material(const DevMaterial& m, FastMat& f) {
+  std::memset(&f, 0, sizeof(f));
+  const DevLobe& a = m.lobes[0];
+  if (m.nlobes == 1 && a.kind == T3_OP_LAMBERT && a.nfac == 1 && !(a.fac[0] & ~0xFFFF) &&
+      plain_value(m, a.fac[0])) {
+    f.sig = T3_OP_LAMBERT;  // T3_SIG_DIFFUSE
+    f.node[0] = a.fac[0];
+    return;
+  }
+  if (m.nlobes != 2) return;
+  const DevLobe& b = m.lobes[1];
+  if (a.kind != T3_OP_LAMBERT || a.nfac != 2 || b.nfac != 1) return;
+  const int mixf = a.fac[0], col = a.fac[1], mixg = b.fac[0];
+  const int F = mixf & 0xFFFF;
+  if (mixf != (F | T3_FAC_ONE_MINUS | T3_FAC_MIX) || mixg != (F | T3_FAC_MIX)) return;
+  if ((col & ~0xFFFF) || !plain_value(m, col)) return;
+  if (b.kind == T3_OP_COOK && F < m.nnodes && m.nodes[F].op == T3_OP_FRESNEL && b.p1 == F &&
+      plain_value(m, b.p0)) {
+    const t3_node& alb = m.nodes[m.nodes[F].b];
+    if (std::memcmp(&alb, &m.nodes[col], sizeof(t3_node)) != 0) return;  // basecolor twice
+    f.sig = T3_OP_LAMBERT | (T3_OP_COOK << 8);  // T3_SIG_PBR
+    f.node[0] = col;
+    f.node[1] = F;
+    f.node[2] = b.p0;
+  } else if (b.kind == T3_OP_PHONG && plain_value(m, F) && plain_value(m, b.p0)) {
+    f.sig = T3_OP_LAMBERT | (T3_OP_PHONG << 8);  // T3_SIG_CLASSIC
+    f.node[0] = col;
+    f.node[1] = F;
+    f.node[2] = b.p0;
+    f.int_pow = b.int_pow;
+  }
 }
 
 int max_lobes(const DevScene& sc) {

@@ -257,7 +257,7 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   a.faces_per_item = c.faces_per_item;
   a.pixels_per_item = c.pixels_per_item;
   a.queue = reinterpret_cast<uint32_t*>(ws + L.counters);
-  int nl = 1, sig = -1;
+  int nl = 1, sig = -1, fsig = -1;
   bool textured = false;
   uint32_t item = 0;
   cudaError_t e = cudaSuccess;
@@ -270,6 +270,8 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
     textured = textured || has_textures(ds) != 0;
     const int ssig = lobe_signature(ds);
     sig = sig < 0 || sig == ssig ? ssig : 0;
+    const int sfast = fast_signature(ds);
+    fsig = fsig < 0 || fsig == sfast ? sfast : 0;
     DevScene* dst = reinterpret_cast<DevScene*>(ws + L.scenes + align256b(sizeof(DevScene)) * (size_t)s);
     // the first upload also zeroes the queue counters and the status
     e = launch_upload_scene(ds, dst, s == 0 ? a.queue : nullptr, s == 0 ? 2 : 0, s == 0 ? status : nullptr,
@@ -315,7 +317,11 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   // the shading instance: lobe kinds as constants when every view shares an
   // untextured signature, texture nodes compiled in only when a view has one
   const void* shade_fn;
-  if (!textured && sig == T3_SIG_PBR) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_PBR>;
+  constexpr int F = T3_SIG_FAST;
+  if (!textured && fsig == T3_SIG_PBR) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_PBR | F>;
+  else if (!textured && fsig == T3_SIG_CLASSIC) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC | F>;
+  else if (!textured && fsig == T3_SIG_DIFFUSE) shade_fn = (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE | F>;
+  else if (!textured && sig == T3_SIG_PBR) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_PBR>;
   else if (!textured && sig == T3_SIG_CLASSIC) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC>;
   else if (!textured && sig == T3_SIG_DIFFUSE) shade_fn = (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE>;
   else if (nl <= 2) shade_fn = textured ? (const void*)k_batch_shade<2, true, 0> : (const void*)k_batch_shade<2, false, 0>;

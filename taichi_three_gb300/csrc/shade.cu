@@ -75,13 +75,33 @@ int lobe_signature(const DevScene& sc) {
   return sig == T3_SIG_PBR || sig == T3_SIG_CLASSIC || sig == T3_SIG_DIFFUSE ? sig : 0;
 }
 
+int fast_signature(const DevScene& sc) {
+  int sig = -1;
+  for (int o = 0; o < sc.nobjects; o++) {
+    if (is_wire(sc.obj[o].mesh)) continue;
+    const int s = sc.obj[o].fast.sig;
+    if (s == 0 || (sig >= 0 && s != sig)) return 0;
+    sig = s;
+  }
+  return sig > 0 ? sig : 0;
+}
+
 template <int NL, int MODE, bool TEX, int SIG = 0>
 static void launch_shade_t(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                            const t3_outputs& out, int64_t npix, cudaStream_t st, const KeyState& ks) {
   constexpr int BLOCK = 256, PPT = 4;
   const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
   if constexpr (MODE == T3_LIGHT_LAMPS && !TEX && SIG == 0) {
-    // untextured lamp scenes with one common lobe signature
+    // untextured lamp scenes with one common material shape, or else one
+    // common lobe signature
+    const int fsig = fast_signature(sc);
+    constexpr int F = T3_SIG_FAST;
+    if (NL == 2 && fsig == T3_SIG_PBR)
+      return launch_shade_t<2, MODE, TEX, T3_SIG_PBR | F>(sc, keys, rec, out, npix, st, ks);
+    if (NL == 2 && fsig == T3_SIG_CLASSIC)
+      return launch_shade_t<2, MODE, TEX, T3_SIG_CLASSIC | F>(sc, keys, rec, out, npix, st, ks);
+    if (NL == 1 && fsig == T3_SIG_DIFFUSE)
+      return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE | F>(sc, keys, rec, out, npix, st, ks);
     const int sig = lobe_signature(sc);
     if (NL == 2 && sig == T3_SIG_PBR) return launch_shade_t<2, MODE, TEX, T3_SIG_PBR>(sc, keys, rec, out, npix, st, ks);
     if (NL == 2 && sig == T3_SIG_CLASSIC)

@@ -70,10 +70,26 @@ struct DevMaterial {
   t3_texture textures[T3_MAX_TEXTURES];
 };
 
+// A material of a known shape, found by the host in the flattened lobes, with
+// the node indices of its parameters, so that a shading instance for that
+// shape evaluates each parameter once instead of walking the lobes' factors
+// (the values, and so the pixels, are the same):
+//   T3_SIG_PBR      Mix(Lambert * C, CookTorrance(R, F), F), F a FresnelFactor:
+//                   node = {C, F, R}
+//   T3_SIG_CLASSIC  Mix(Lambert * C, Phong(M), S): node = {C, S, M}, int_pow
+//   T3_SIG_DIFFUSE  Lambert * C: node = {C}
+struct FastMat {
+  int32_t sig;  // 0: none
+  int32_t node[3];
+  int32_t int_pow;
+  int32_t _pad[3];
+};
+
 struct DevObject {
   t3_mesh mesh;
   DevMaterial mat;
   int64_t face_base, nfaces;
+  FastMat fast;
 };
 
 struct DevScene {
@@ -144,6 +160,10 @@ cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const 
 cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                              const t3_outputs& out, int32_t* status, cudaStream_t st);
 int max_lobes(const DevScene& sc);
+// the FastMat shape of a flattened material (fast.sig = 0 when none matches)
+void find_fast_material(const DevMaterial& m, FastMat& fast);
+// the shape shared by every shaded object of the scene, or 0
+int fast_signature(const DevScene& sc);
 // the lobe kinds (one byte per slot) shared by every shaded object of the
 // scene when a specialised shading instance exists for them, else 0
 int lobe_signature(const DevScene& sc);

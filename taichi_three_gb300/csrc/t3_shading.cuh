@@ -147,6 +147,8 @@ constexpr int T3_SIG_PBR = T3_OP_LAMBERT | (T3_OP_COOK << 8);      // PBR
 constexpr int T3_SIG_CLASSIC = T3_OP_LAMBERT | (T3_OP_PHONG << 8); // Classic
 template <int SIG>
 __device__ __forceinline__ constexpr int sig_kind(int k) { return (SIG >> (8 * k)) & 0xFF; }
+// instances whose every object has the FastMat shape of its signature
+constexpr int T3_SIG_FAST = 1 << 24;
 
 template <int NL, bool TEX = true, int SIG = 0>
 __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag& fg, V3 viewdir,
@@ -165,7 +167,7 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
       const V3 f = eval_value<TEX>(mat, lb.fac[j] & 0xFFFF, fg);
       w = w * ((lb.fac[j] & T3_FAC_ONE_MINUS) ? one_minus(f) : f);
     }
-    const int kind = SIG ? sig_kind<SIG>(k) : lb.kind;
+    const int kind = SIG ? sig_kind<SIG & ~T3_SIG_FAST>(k) : lb.kind;
     L.kind[k] = kind;
     if (kind == T3_OP_EMISSION) emission = emission + w;
     else ambient = ambient + w;
@@ -187,13 +189,52 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
   }
 }
 
+// eval_material for an object whose material has its signature's FastMat
+// shape: each parameter evaluated once; the same values as eval_material
+template <int NL, int SIG>
+__device__ __forceinline__ void eval_material_fast(const DevObject& ob, const Frag& fg, V3 viewdir,
+                                                   LobeState<NL>& L, V3& ambient, V3& emission) {
+  constexpr int S = SIG & ~T3_SIG_FAST;
+  const DevMaterial& mat = ob.mat;
+  const V3 c = eval_basic(mat.nodes[ob.fast.node[0]], fg);
+  emission = v3(0.f, 0.f, 0.f);
+  L.n = S == T3_SIG_DIFFUSE ? 1 : 2;
+#pragma unroll
+  for (int k = 0; k < NL; k++) L.kind[k] = sig_kind<S>(k);
+  if constexpr (S == T3_SIG_DIFFUSE) {
+    L.w[0] = c;
+    ambient = c;
+  } else {
+    // Mix(Lambert * C, second, F): weights (1 - F) C and F
+    const V3 f = S == T3_SIG_PBR ? eval_value<false>(mat, ob.fast.node[1], fg)
+                                 : eval_basic(mat.nodes[ob.fast.node[1]], fg);
+    L.w[0] = one_minus(f) * c;
+    L.w[1] = f;
+    ambient = L.w[0] + L.w[1];
+    const float p = eval_basic(mat.nodes[ob.fast.node[2]], fg).x;
+    if constexpr (S == T3_SIG_PBR) {
+      const float NoV = fmaxf(1e-10f, dot(viewdir, fg.normal));
+      const float a2 = fmaxf(1e-6f, p * p);
+      const float kk = a2 * 0.5f;
+      L.a2[1] = a2;
+      L.k[1] = kk;
+      L.gnorm[1] = __fdividef(1.0f, ((NoV * kk + 1.0f) - kk) * (1.0f * (1.0f - a2) + 12.566370614359172f * a2));
+      L.oma2[1] = 1.0f - a2;
+      L.f0[1] = f;
+    } else {
+      L.m[1] = p;
+      L.ipow[1] = ob.fast.int_pow;
+    }
+  }
+}
+
 // sum_k W_k * brdf_k(n, L, V)
 template <int NL, int SIG = 0>
 __device__ __forceinline__ V3 eval_brdf(const LobeState<NL>& L, V3 n, V3 ldir, V3 vdir) {
   V3 acc = v3(0.f, 0.f, 0.f);
 #pragma unroll
   for (int k = 0; k < NL; k++) {
-    const int kind = SIG ? sig_kind<SIG>(k) : L.kind[k];
+    const int kind = SIG ? sig_kind<SIG & ~T3_SIG_FAST>(k) : L.kind[k];
     if (kind == T3_OP_LAMBERT) {
       acc = acc + 0.31830988618379067f * L.w[k];
     } else if (kind == T3_OP_COOK) {
@@ -490,7 +531,8 @@ __device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const
   if (MODE == T3_LIGHT_LAMPS) {
     LobeState<NL> L;
     V3 amb, emi;
-    eval_material<NL, TEX, SIG>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
+    if constexpr ((SIG & T3_SIG_FAST) != 0) eval_material_fast<NL, SIG>(*g.ob, g.fg, g.vdir, L, amb, emi);
+    else eval_material<NL, TEX, SIG>(g.ob->mat, g.fg, g.vdir, L, amb, emi);
     color = emi + v3(lt.ambient[0], lt.ambient[1], lt.ambient[2]) * amb;
     color = color + lamps_term<NL, SIG>(lt, L, g.fg, g.vdir);
   } else if (MODE == T3_LIGHT_IBL_PREFILTERED) {
