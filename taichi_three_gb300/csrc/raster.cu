@@ -96,22 +96,6 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
   }
   if (vis) {
     if (big.rec) store_record(big.rec, face_base + (uint32_t)n, s);
-    if (mesh.kind == T3_MESH_SOUP) {
-      // the shading pass gathers this face's normals and material attributes:
-      // start their DRAM reads into L2 now, while this pass is bound by its
-      // arithmetic (first and last byte of each row: the sectors they span)
-      const int64_t f = (mesh.flags & T3_MESH_NOCULL) ? n >> 1 : n;
-      if ((fr.flags & T3_SMOOTHING) && mesh.norms && !(mesh.flags & T3_MESH_FLAT_NORMAL)) {
-        const char* p = reinterpret_cast<const char*>(mesh.norms + f * 9);
-        asm volatile("prefetch.global.L2 [%0];" :: "l"(p));
-        asm volatile("prefetch.global.L2 [%0];" :: "l"(p + 35));
-      }
-      if (mesh.face_attr && mesh.attr_stride > 0) {
-        const char* p = reinterpret_cast<const char*>(mesh.face_attr + f * mesh.attr_stride);
-        asm volatile("prefetch.global.L2 [%0];" :: "l"(p));
-        asm volatile("prefetch.global.L2 [%0];" :: "l"(p + 4 * mesh.attr_stride - 1));
-      }
-    }
     const int64_t area = (int64_t)(s.topx - s.botx + 1) * (int64_t)(s.topy - s.boty + 1);
     if (area > big_threshold) {
       const uint32_t slot = atomicAdd(big.count, 1u);

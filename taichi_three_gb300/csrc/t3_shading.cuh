@@ -563,27 +563,6 @@ __device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const
   store_rgb(fr, out, g.i, color);
 }
 
-// Starts the L2 fills of everything shading a covered pixel reads -- the
-// face's setup record, its first corner's position and normal, its material
-// attributes -- while the block is still compacting its pixel list, so the
-// dependent loads of the shading loop find them in L2 rather than in DRAM.
-__device__ __forceinline__ void prefetch_face(const DevScene* __restrict__ sc, const float4* __restrict__ rec,
-                                              unsigned long long key) {
-  const int64_t gid = (int64_t)(uint32_t)key;
-  int o = 0;
-  for (int j = 1; j < sc->nobjects; j++)
-    if (gid >= sc->obj[j].face_base) o = j;
-  const t3_mesh& mesh = sc->obj[o].mesh;
-  const int64_t n = gid - sc->obj[o].face_base;
-  if (mesh.kind == T3_MESH_SOUP) {
-    const int64_t f = (mesh.flags & T3_MESH_NOCULL) ? n >> 1 : n;
-    asm volatile("prefetch.global.L2 [%0];" :: "l"(mesh.verts + f * 9));
-    if (mesh.norms) asm volatile("prefetch.global.L2 [%0];" :: "l"(mesh.norms + f * 9));
-    if (mesh.face_attr) asm volatile("prefetch.global.L2 [%0];" :: "l"(mesh.face_attr + f * mesh.attr_stride));
-  }
-  if (rec) asm volatile("prefetch.global.L2 [%0];" :: "l"(rec + gid * 4));
-}
-
 // One block's share of the shading pass: pixels [base, base + BLOCK * PPT) of
 // the frame.  Empty pixels are written as background at once; covered ones are
 // compacted into a shared list (warp ballot + one shared atomic per warp), with
@@ -617,10 +596,7 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
       } else {
         covered = true;
       }
-      if (key != T3_EMPTY_KEY) {
-        prefetch_face(sc, rec, key);
-        if (reset_keys) reset_keys[i] = T3_EMPTY_KEY;
-      }
+      if (key != T3_EMPTY_KEY && reset_keys) reset_keys[i] = T3_EMPTY_KEY;
     }
     const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
     if (m) {
