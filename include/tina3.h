@@ -419,21 +419,35 @@ int t3_accumulate(float* acc, const float* src, int64_t n, int count, void* stre
  * No reference counterpart: the reference renders one Scene per call
  * (tina/scene/raster.py:168-207).  Up to T3_BATCH_MAX_SCENES independent
  * frames (each its own t3_scene: resolution <= 4096 x 4096, camera, objects,
- * lamps; lighting T3_LIGHT_LAMPS) are rasterised by one persistent launch whose
- * CTAs take (scene, object, face chunk) items from a global work queue, then
- * shaded by a second persistent launch over (scene, pixel chunk) items. */
+ * lamps; lighting T3_LIGHT_LAMPS) are rendered by two launches over all of
+ * them.  Direct: a persistent launch whose CTAs take (scene, object, face
+ * chunk) raster items from a global work queue, then a persistent shading
+ * launch over (scene, pixel chunk) items.  Binned: one launch bins every
+ * scene's faces into its screen tiles, then a persistent launch takes
+ * (scene, tile) items from a global queue and rasterises and shades each
+ * tile in shared memory. */
 #define T3_BATCH_MAX_SCENES 64
 
 typedef struct t3_batch_config {
-  int32_t faces_per_item;   /* faces per raster item, multiple of 256 (0: 1024)       */
-  int32_t pixels_per_item;  /* pixels per shading item, multiple of 1024 (0: 4096)    */
-  int32_t ctas_per_sm;      /* cap on resident CTAs per SM, 1..8 (0: as many as fit)  */
-  int32_t _pad;
+  int32_t faces_per_item;   /* direct: faces per raster item, multiple of 256 (0: 1024)    */
+  int32_t pixels_per_item;  /* direct: pixels per shading item, multiple of 1024 (0: 4096) */
+  int32_t ctas_per_sm;      /* cap on resident CTAs per SM, 1..8 (0: as many as fit)       */
+  int32_t raster;           /* T3_RASTER_DIRECT (0) or T3_RASTER_BINNED                    */
+  int32_t tile;             /* binned: tile edge 8, 16 or 32 (0: 16)                       */
+  int32_t tile_threads;     /* binned: threads per tile CTA, 64 (tile 8 only), 128 or 256
+                               (0: 64 for tile 8, else 256)                                */
+  int64_t bin_capacity;     /* binned: entries per tile bin in every scene; 0: each scene's
+                               automatic size (8 x faces / tiles + 64); -k: k times it    */
 } t3_batch_config;
 
-int t3_batch_workspace_size(const t3_scene* scenes, int nscenes, size_t* bytes);
+/* Workspace bytes of t3_render_batch for these scenes and this configuration
+ * (NULL: the direct defaults). */
+int t3_batch_workspace_size(const t3_scene* scenes, int nscenes, const t3_batch_config* config,
+                            size_t* bytes);
 
-/* Renders scenes[i] into outs[i] for i < nscenes (every output as t3_render). */
+/* Renders scenes[i] into outs[i] for i < nscenes (every output as t3_render).
+ * A binned bin that overflows sets T3_STATUS_BIN_OVERFLOW in *status (its
+ * faces are dropped): render again with a larger bin_capacity. */
 int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
                     const t3_batch_config* config, void* workspace, size_t workspace_bytes,
                     int32_t* status, void* stream);

@@ -126,8 +126,9 @@ class t3_outputs(C.Structure):
 
 
 class t3_batch_config(C.Structure):
-    _fields_ = [("faces_per_item", C.c_int32), ("pixels_per_item", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("_pad", C.c_int32)]
+    _fields_ = [("faces_per_item", C.c_int32), ("pixels_per_item", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("raster", C.c_int32), ("tile", C.c_int32), ("tile_threads", C.c_int32),
+                ("bin_capacity", C.c_int64)]
 
 
 T3_BATCH_MAX_SCENES = 64
@@ -167,7 +168,8 @@ SIGNATURES = {
     "t3_render_noalloc": (C.c_int, [C.POINTER(t3_scene), _VP, C.POINTER(t3_outputs), _VP]),
     "t3_raster_fragments": (C.c_int, [C.POINTER(t3_scene), _VP, _SZ, C.POINTER(C.c_int64), _VP]),
     "t3_red_min_rate": (C.c_int, [_VP, _I64, C.c_int, _VP]),
-    "t3_batch_workspace_size": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.POINTER(C.c_size_t)]),
+    "t3_batch_workspace_size": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.POINTER(t3_batch_config),
+                                          C.POINTER(C.c_size_t)]),
     "t3_render_batch": (C.c_int, [C.POINTER(t3_scene), C.POINTER(t3_outputs), C.c_int,
                                   C.POINTER(t3_batch_config), _VP, _SZ, _VP, _VP]),
     "t3_mlp_param_count": (C.c_int64, []),

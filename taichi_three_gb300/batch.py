@@ -3,11 +3,14 @@
 No reference counterpart (Tina renders one Scene per Scene.render call,
 tina/scene/raster.py:168-207).  A BatchRenderer holds up to 64 Scenes (each
 with its own resolution, camera, objects and lamps) and renders all of them
-with two persistent CUDA launches -- every scene's rasterisation in one, every
-scene's shading in the next -- whose CTAs take work items from global queues;
+with two CUDA launches over all of them: direct, a persistent rasterisation
+launch and a persistent shading launch whose CTAs take work items from global
+queues; binned, one launch binning every scene's faces into its tiles and a
+persistent launch rasterising and shading (scene, tile) items;
 each Scene's img / face_id / depth / depth_f are written
 exactly as Scene.render would write them.  BatchRenderer.autotune times the
-work-item sizes and residency on the actual batch and keeps the fastest.
+direct work-item sizes and the binned tile size, threads per tile and bin
+capacity on the actual batch and keeps the fastest.
 """
 import ctypes as C
 
@@ -23,15 +26,30 @@ def _stream():
 
 
 class BatchRenderer:
-    def __init__(self, scenes, faces_per_item=1024, pixels_per_item=4096, ctas_per_sm=0):
+    """raster 'direct' (work items of faces_per_item faces and pixels_per_item
+    pixels) or 'binned' (tiles of `tile` pixels, `tile_threads` threads per
+    tile CTA, bin_capacity entries per tile bin: 0 for each scene's automatic
+    size, -k for k times it); ctas_per_sm caps the resident CTAs of either."""
+
+    def __init__(self, scenes, faces_per_item=1024, pixels_per_item=4096, ctas_per_sm=0, raster='direct',
+                 tile=16, tile_threads=0, bin_capacity=0):
         self.scenes = list(scenes)
         if not 1 <= len(self.scenes) <= N.T3_BATCH_MAX_SCENES:
             raise ValueError(f'a batch holds 1..{N.T3_BATCH_MAX_SCENES} scenes')
+        if raster not in ('direct', 'binned'):
+            raise ValueError("raster must be 'direct' or 'binned'")
         self.config = dict(faces_per_item=faces_per_item, pixels_per_item=pixels_per_item,
-                           ctas_per_sm=ctas_per_sm)
+                           ctas_per_sm=ctas_per_sm, raster=raster, tile=tile, tile_threads=tile_threads,
+                           bin_capacity=bin_capacity)
         self._ws = None
         self._status = None
         self._keep = []
+
+    @staticmethod
+    def _t3_config(config):
+        c = dict(config)
+        c['raster'] = N.T3_RASTER_BINNED if c.get('raster', 'direct') == 'binned' else N.T3_RASTER_DIRECT
+        return N.t3_batch_config(**c)
 
     def _describe(self, dev):
         n = len(self.scenes)
@@ -51,24 +69,36 @@ class BatchRenderer:
             outs[i].depth_f = scene.depth_f.data_ptr()
         return descs, outs, keep
 
-    def render(self, config=None):
-        """Renders every scene of the batch (one raster launch, one shading launch)."""
+    def render(self, config=None, check_bins=True):
+        """Renders every scene of the batch (two launches over all of them).  A
+        binned batch whose bins overflowed is rendered again with bins twice
+        the automatic size, then four times (check_bins=False skips the check,
+        which reads the device status; inside a CUDA graph capture, for one)."""
         require_cuda('BatchRenderer.render')
         lib = N.load()
         dev = default_device()
         descs, outs, keep = self._describe(dev)
         n = len(self.scenes)
-        size = C.c_size_t()
-        N.check(lib.t3_batch_workspace_size(descs, n, C.byref(size)), 't3_batch_workspace_size')
-        if self._ws is None or self._ws.numel() < size.value:
-            self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
-        if self._status is None:
-            self._status = torch.zeros(1, dtype=torch.int32, device=dev)
-        cfg = N.t3_batch_config(**(config or self.config))
-        N.check(lib.t3_render_batch(descs, outs, n, C.byref(cfg), self._ws.data_ptr(),
-                                    self._ws.numel(), self._status.data_ptr(), _stream()),
-                't3_render_batch')
+        config = dict(config or self.config)
+        for attempt in range(3):
+            cfg = self._t3_config(config)
+            size = C.c_size_t()
+            N.check(lib.t3_batch_workspace_size(descs, n, C.byref(cfg), C.byref(size)),
+                    't3_batch_workspace_size')
+            if self._ws is None or self._ws.numel() < size.value:
+                self._ws = torch.empty(size.value, dtype=torch.uint8, device=dev)
+            if self._status is None:
+                self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+            N.check(lib.t3_render_batch(descs, outs, n, C.byref(cfg), self._ws.data_ptr(),
+                                        self._ws.numel(), self._status.data_ptr(), _stream()),
+                    't3_render_batch')
+            if config.get('raster') != 'binned' or not check_bins:
+                break
+            if not (self.status() & N.T3_STATUS_BIN_OVERFLOW):
+                break
+            config['bin_capacity'] = -2 * (2 ** attempt)
         self._keep = keep
+        self.last_config = config
 
     def status(self):
         lib = N.load()
@@ -84,15 +114,28 @@ class BatchRenderer:
             sig.append((tuple(s.res), int(nf)))
         return ('batch', tuple(sig))
 
-    CANDIDATES = [dict(faces_per_item=f, pixels_per_item=p, ctas_per_sm=c)
-                  for f in (256, 1024, 4096) for p in (1024, 4096, 16384) for c in (0, 2)]
+    # the direct path's work-item sizes, and the binned path's tile size x
+    # threads per tile x bin capacity (the automatic size, or twice it)
+    CANDIDATES = ([dict(raster='direct', faces_per_item=f, pixels_per_item=p, ctas_per_sm=0)
+                   for f in (256, 1024, 4096) for p in (1024, 4096, 16384)] +
+                  [dict(raster='binned', tile=t, tile_threads=th, bin_capacity=b)
+                   for t, th in ((8, 64), (16, 128), (16, 256), (32, 128), (32, 256)) for b in (0, -2)])
 
     def autotune(self, candidates=None, tuner=None, repeats=3):
         """Times each candidate configuration on this batch (CUDA events,
         median of `repeats` after one warm-up) and keeps the fastest; the
-        result is cached by the batch signature.  Returns (config, ms)."""
+        result is cached by the batch signature.  A binned candidate whose
+        bins overflow is not eligible.  Returns (config, ms)."""
         tuner = tuner or default_tuner()
-        cands = candidates or self.CANDIDATES
-        best, ms = tuner.tune(self.signature(), cands, lambda c: self.render(c), repeats=repeats)
+        cands = [dict(c) for c in (candidates or self.CANDIDATES)]
+        ok = []
+        for c in cands:
+            if c.get('raster') == 'binned':
+                self.render(c, check_bins=False)
+                if self.status() & N.T3_STATUS_BIN_OVERFLOW:
+                    continue
+            ok.append(c)
+        best, ms = tuner.tune(self.signature(), ok, lambda c: self.render(c, check_bins=False),
+                              repeats=repeats)
         self.config = dict(best)
         return self.config, ms

@@ -261,7 +261,7 @@ int max_lobes(const DevScene& sc) {
   return m;
 }
 
-static int has_points_or_lines(const t3_scene& sc) {
+int has_points_or_lines(const t3_scene& sc) {
   for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
     if (is_point_or_line(sc.objects[o].mesh) && sc.objects[o].nfaces > 0) return 1;
   return 0;
@@ -287,7 +287,7 @@ static int64_t max_object_faces(const t3_scene& sc) {
   return m;
 }
 
-static int64_t total_faces(const t3_scene& sc) {
+int64_t total_faces(const t3_scene& sc) {
   int64_t t = 0;
   for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++) t += sc.objects[o].nfaces;
   return t;
@@ -337,7 +337,7 @@ static KeyState key_state(void* ws, unsigned long long tag) {
   return ks;
 }
 
-static int64_t auto_bin_capacity(const t3_scene& sc, int tile) {
+int64_t auto_bin_capacity(const t3_scene& sc, int tile) {
   const int64_t tx = (sc.frame.width + tile - 1) / tile, ty = (sc.frame.height + tile - 1) / tile;
   const int64_t per = 8 * total_faces(sc) / (tx * ty) + 64;
   int64_t cap = per < 64 ? 64 : per > (1 << 16) ? (1 << 16) : per;

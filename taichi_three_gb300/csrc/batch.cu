@@ -224,8 +224,11 @@ using namespace t3;
 
 extern "C" {
 
-int t3_batch_workspace_size(const t3_scene* scenes, int nscenes, size_t* bytes) {
+int t3_batch_workspace_size(const t3_scene* scenes, int nscenes, const t3_batch_config* config,
+                            size_t* bytes) {
   if (!bytes) return T3_EINVAL;
+  if (config && config->raster == T3_RASTER_BINNED) return batch_binned_size(scenes, nscenes, *config, bytes);
+  if (config && config->raster != T3_RASTER_DIRECT) return T3_EINVAL;
   BatchLayout L;
   const int r = batch_layout(scenes, nscenes, L);
   if (r) return r;
@@ -237,12 +240,15 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
                     const t3_batch_config* cfg, void* workspace, size_t workspace_bytes,
                     int32_t* status, void* stream) {
   if (!scenes || !outs || !workspace || !status) return T3_EINVAL;
+  t3_batch_config c{1024, 4096, 0, T3_RASTER_DIRECT, 0, 0, 0};
+  if (cfg) c = *cfg;
+  if (c.raster == T3_RASTER_BINNED)
+    return render_batch_binned(scenes, outs, nscenes, c, workspace, workspace_bytes, status, (cudaStream_t)stream);
+  if (c.raster != T3_RASTER_DIRECT) return T3_EINVAL;
   BatchLayout L;
   int r = batch_layout(scenes, nscenes, L);
   if (r) return r;
   if (workspace_bytes < L.end) return T3_EINVAL;
-  t3_batch_config c{1024, 4096, 0, 0};
-  if (cfg) c = *cfg;
   if (c.faces_per_item <= 0) c.faces_per_item = 1024;
   if (c.pixels_per_item <= 0) c.pixels_per_item = 4096;
   if (c.faces_per_item % kBatchBlock || c.pixels_per_item % (kBatchBlock * kBatchPPT)) return T3_EINVAL;

@@ -67,19 +67,26 @@ struct GlobalKeySink {
   }
 };
 
+// `fpw` faces per warp (a power of two up to 32): lanes below fpw take one
+// face each.  Small meshes use fewer than 32 so that more warps share the
+// walk of their pixels (a mesh of a few thousand faces fills only a few SMs
+// at 32 faces per warp, and each warp's walk is a long serial chain).
 template <int BLOCK, bool COUNT>
 __global__ void __launch_bounds__(BLOCK, 6)
 k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t face_base,
-                unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold) {
+                unsigned long long* __restrict__ keys, BigQueue big, int32_t big_threshold, int fpw) {
   __shared__ __align__(16) float sv[BLOCK * 9];
   __shared__ WarpFaces wfs[BLOCK / 32];
   __shared__ WarpCols wcs[BLOCK / 32];
-  const int64_t f0 = (int64_t)blockIdx.x * BLOCK;
-  const bool staged = stage_soup<BLOCK>(mesh, nfaces, f0, sv);
-  const int64_t n = f0 + threadIdx.x;
+  const int per_block = (BLOCK / 32) * fpw;
+  const int64_t f0 = (int64_t)blockIdx.x * per_block;
+  const bool staged = stage_soup<BLOCK>(mesh, nfaces, f0, sv, per_block);
+  const int lane = threadIdx.x & 31;
+  const int slot = (threadIdx.x >> 5) * fpw + lane;  // this lane's face within the block
+  const int64_t n = f0 + slot;
   Setup s{};
   bool vis = false;
-  if (n < nfaces) {
+  if (lane < fpw && n < nfaces) {
     if (big.vndc) {
       // transformed corners from the vertex stage
       const FaceRef ref = face_ref(mesh, n);
@@ -89,7 +96,7 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
       vis = face_setup_ndc(fr, ref.flip ? c[2] : c[0], c[1], ref.flip ? c[0] : c[2], s);
     } else {
       f3 v[3];
-      load_face(mesh, n, staged, sv, v);
+      load_face(mesh, n, staged, sv, v, slot);
       vis = face_setup(fr, v, s);
     }
     vis = vis && s.botx <= s.topx && s.boty <= s.topy;
@@ -166,18 +173,23 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st) {
   if (ob.nfaces <= 0) return cudaSuccess;
   constexpr int BLOCK = 256;
-  const int64_t grid = (ob.nfaces + BLOCK - 1) / BLOCK;
+  // faces per warp: 32 once the mesh fills every SM's warps (152 SMs x 48),
+  // fewer below that, down to one face per warp
+  int fpw = 32;
+  while (fpw > 1 && ob.nfaces < (int64_t)152 * 48 * fpw) fpw >>= 1;
+  const int64_t per_block = (BLOCK / 32) * fpw;
+  const int64_t grid = (ob.nfaces + per_block - 1) / per_block;
   // big.count was zeroed at the start of the frame
   if (big.fragments) {
     k_raster_direct<BLOCK, true><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
                                                                   (uint32_t)ob.face_base, keys, big,
-                                                                  big_threshold);
+                                                                  big_threshold, fpw);
     k_raster_big<BLOCK, true><<<152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);
     return cudaGetLastError();
   }
   k_raster_direct<BLOCK, false><<<(unsigned)grid, BLOCK, 0, st>>>(fr, ob.mesh, ob.nfaces,
                                                                  (uint32_t)ob.face_base, keys, big,
-                                                                 big_threshold);
+                                                                 big_threshold, fpw);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_raster_big<BLOCK, false><<<152, BLOCK, 0, st>>>(fr, ob.mesh, (uint32_t)ob.face_base, keys, big);

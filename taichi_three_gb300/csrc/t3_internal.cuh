@@ -168,6 +168,14 @@ int fast_signature(const DevScene& sc);
 // scene when a specialised shading instance exists for them, else 0
 int lobe_signature(const DevScene& sc);
 int has_textures(const DevScene& sc);  // any Texture / ChessboardTexture node
+int has_points_or_lines(const t3_scene& sc);
+int64_t total_faces(const t3_scene& sc);
+// the binned rasteriser's automatic entries per tile bin: 8 x faces / tiles + 64
+int64_t auto_bin_capacity(const t3_scene& sc, int tile);
+// t3_render_batch's binned path (batch_binned.cu): workspace bytes, and the batch
+int batch_binned_size(const t3_scene* scenes, int n, const t3_batch_config& c, size_t* bytes);
+int render_batch_binned(const t3_scene* scenes, const t3_outputs* outs, int n, const t3_batch_config& c,
+                        void* workspace, size_t workspace_bytes, int32_t* status, cudaStream_t st);
 cudaError_t launch_bin(const t3_frame& fr, const t3_object& ob, const BinArgs& bins, cudaStream_t st);
 cudaError_t launch_tile(const DevScene* sc, const BinArgs& bins, int ntiles, const t3_outputs& out,
                         cudaStream_t st);

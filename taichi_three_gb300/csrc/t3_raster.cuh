@@ -311,9 +311,9 @@ __device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, c
 // Loads (and transforms) the corners of face n; soup positions come from the
 // block's shared-memory staging area when `staged`.
 __device__ __forceinline__ void load_face(const t3_mesh& mesh, int64_t n, bool staged,
-                                          const float* sv, f3 v[3]) {
+                                          const float* sv, f3 v[3], int slot = -1) {
   if (staged) {
-    const float* p = sv + threadIdx.x * 9;
+    const float* p = sv + (slot < 0 ? (int)threadIdx.x : slot) * 9;
     f3 t[3] = {f3{p[0], p[1], p[2]}, f3{p[3], p[4], p[5]}, f3{p[6], p[7], p[8]}};
     if (mesh.flags & T3_MESH_TRANSFORM) {
 #pragma unroll
@@ -330,11 +330,12 @@ __device__ __forceinline__ void load_face(const t3_mesh& mesh, int64_t n, bool s
 
 // Cooperative 16-byte loads of the block's face-soup positions into shared memory.
 template <int BLOCK>
-__device__ __forceinline__ bool stage_soup(const t3_mesh& mesh, int64_t nfaces, int64_t f0, float* sv) {
+__device__ __forceinline__ bool stage_soup(const t3_mesh& mesh, int64_t nfaces, int64_t f0, float* sv,
+                                           int nmax = BLOCK) {
   const bool staged = mesh.kind == T3_MESH_SOUP && !(mesh.flags & T3_MESH_NOCULL);
   if (staged) {
     const int64_t rem = nfaces - f0;
-    const int nf = rem < BLOCK ? (int)(rem > 0 ? rem : 0) : BLOCK;
+    const int nf = rem < nmax ? (int)(rem > 0 ? rem : 0) : nmax;
     const float* src = mesh.verts + f0 * 9;
     const int nflt = nf * 9;
     if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {

@@ -1,12 +1,14 @@
-"""Batched multi-view rendering (t3_render_batch, one persistent launch over a
-global work queue) against per-scene Scene.render and the oracle, plus the
-autotuner (its caching logic on the CPU, its choice on the GPU)."""
+"""Batched multi-view rendering (t3_render_batch: two launches over every
+view, direct work items or binned tiles) against per-scene Scene.render and
+the oracle, plus the autotuner (its caching logic on the CPU, its choice on
+the GPU)."""
 import json
 
 import numpy as np
 import pytest
 
 import taichi_three_gb300 as tina
+from taichi_three_gb300 import _native as N
 from taichi_three_gb300.autotune import Autotuner
 
 
@@ -57,9 +59,15 @@ def _outputs(scene):
             scene.engine.depth.cpu().numpy().copy(), scene.depth_f.cpu().numpy().copy())
 
 
+BINNED = [dict(raster='binned', tile=t, tile_threads=th) for t, th in
+          ((8, 64), (16, 128), (16, 256), (32, 128), (32, 256))]
+CONFIGS = [dict(), dict(faces_per_item=256, pixels_per_item=1024, ctas_per_sm=1),
+           dict(faces_per_item=4096, pixels_per_item=16384, ctas_per_sm=2)] + BINNED + [
+           dict(raster='binned', tile=16, tile_threads=128, ctas_per_sm=1, bin_capacity=-2)]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize('config', [dict(), dict(faces_per_item=256, pixels_per_item=1024, ctas_per_sm=1),
-                                    dict(faces_per_item=4096, pixels_per_item=16384, ctas_per_sm=2)])
+@pytest.mark.parametrize('config', CONFIGS, ids=lambda c: '-'.join(f'{k}{v}' for k, v in c.items()) or 'default')
 def test_batch_matches_single_renders(cuda, config):
     scenes = _small_batch()
     ref = []
@@ -79,9 +87,32 @@ def test_batch_matches_single_renders(cuda, config):
 
 
 @pytest.mark.gpu
-def test_batch_against_oracle(cuda, oracle_mod):
+def test_batch_binned_overflow_retries(cuda):
+    # bins of 16 entries overflow on every view with more than a few faces per
+    # tile; render() sees the status and renders again with larger bins
+    scenes = _small_batch(3)
+    ref = []
+    for s in scenes:
+        s.render()
+        ref.append(_outputs(s))
+    b = tina.BatchRenderer(scenes, raster='binned', tile=16, bin_capacity=16)
+    b.render(check_bins=False)
+    assert b.status() & N.T3_STATUS_BIN_OVERFLOW
+    b.render()
+    assert b.status() == 0 and b.last_config['bin_capacity'] < 0
+    for s, (rgb, fid, dep, dpf) in zip(scenes, ref):
+        g = _outputs(s)
+        assert np.array_equal(g[1], fid)
+        assert np.array_equal(g[2], dep)
+        assert np.abs(g[0] - rgb).max() <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('config', [dict(), dict(raster='binned', tile=32, tile_threads=256)],
+                         ids=['direct', 'binned'])
+def test_batch_against_oracle(cuda, oracle_mod, config):
     scenes = _small_batch(1)[:3]
-    tina.BatchRenderer(scenes).render()
+    tina.BatchRenderer(scenes, **config).render()
     for s in scenes:
         g = _outputs(s)
         o = oracle_mod.render(s)
@@ -95,9 +126,14 @@ def test_batch_autotune(cuda):
     scenes = _small_batch(2)
     b = tina.BatchRenderer(scenes)
     cands = [dict(faces_per_item=256, pixels_per_item=1024, ctas_per_sm=1),
-             dict(faces_per_item=1024, pixels_per_item=4096, ctas_per_sm=2)]
-    cfg, ms = b.autotune(candidates=cands, tuner=Autotuner())
-    assert cfg in cands and ms > 0
+             dict(faces_per_item=1024, pixels_per_item=4096, ctas_per_sm=2),
+             dict(raster='binned', tile=16, tile_threads=128, bin_capacity=0),
+             dict(raster='binned', tile=8, tile_threads=64, bin_capacity=4)]
+    tuner = Autotuner()
+    cfg, ms = b.autotune(candidates=cands, tuner=tuner)
+    assert cfg in cands[:3] and ms > 0
+    # the candidate whose 4-entry bins overflow is never timed
+    assert [c for c, _ in tuner.log] == cands[:3]
     b.render()
     assert b.status() == 0
 

@@ -1,9 +1,9 @@
 """Parity at the benchmark sizes: the configurations bench.py times, each
 checked against the oracle at the same size.
 
-* 64 views (20.4 M faces, 34.1 M pixels) through BatchRenderer against the
-  oracle's OpenMP mode, view by view: face id / int32 depth / float depth
-  bit-exact, scene.img within 1e-4.
+* 64 views (20.4 M faces, 34.1 M pixels) through BatchRenderer, direct and
+  binned (16- and 32-pixel tiles), against the oracle's OpenMP mode, view by
+  view: face id / int32 depth / float depth bit-exact, scene.img within 1e-4.
 * The 1080p, 1,000,000-face soup lit only by the environment with 256-sample
   Monte Carlo IBL: face id / depth bit-exact over the whole frame (against the
   oracle's raster of the same geometry), and 4,000 covered plus 500 empty
@@ -39,20 +39,31 @@ def _same_raster(g, o):
     assert np.array_equal(g['depth_f'].view(np.uint32), o['depth_f'].view(np.uint32))
 
 
-def test_batch_64_views_full_size(cuda, oracle_mod):
+@pytest.fixture(scope='module')
+def batch64(cuda):
     scenes = tina.workloads.batch_scenes(64, seed=0)
+    return scenes, {}
+
+
+@pytest.mark.parametrize('config', [dict(), dict(raster='binned', tile=16, tile_threads=128),
+                                    dict(raster='binned', tile=32, tile_threads=256)],
+                         ids=['direct', 'binned16', 'binned32'])
+def test_batch_64_views_full_size(cuda, oracle_mod, batch64, config):
+    scenes, oracle_cache = batch64
     faces = sum(next(iter(s.objects)).get_nfaces() for s in scenes)
     assert faces > 20_000_000
-    b = tina.BatchRenderer(scenes)
+    b = tina.BatchRenderer(scenes, **config)
     b.render()
     assert b.status() == 0
     worst = 0.0
-    for s in scenes:
+    for i, s in enumerate(scenes):
         g = _outputs(s)
-        o = oracle_mod.render(s, mode=1)
+        if i not in oracle_cache:
+            oracle_cache[i] = oracle_mod.render(s, mode=1)
+        o = oracle_cache[i]
         _same_raster(g, o)
         worst = max(worst, float(np.abs(g['rgb'] - o['rgb']).max()))
-    print(f'64 views: rgb max abs err {worst:.3g}')
+    print(f'64 views {config}: rgb max abs err {worst:.3g}')
     assert worst <= RGB_TOL
 
 
