@@ -303,14 +303,17 @@ int64_t total_faces(const t3_scene& sc) {
 //   rec       float4[4 * total_faces] setup records of the visible faces
 //   direct:   keys  uint64[W*H] packed (depth, id)
 //   binned:   bins  uint32[ntiles * bin_capacity]
+//   learned IBL: the network pass's rows, 96 bytes per pixel (their count is
+//             counter kMlpRowCounter)
 struct Layout {
-  size_t scene, counters, big, keys, rec, bins, vtx, end;
+  size_t scene, counters, big, keys, rec, bins, vtx, mlp, end;
   int ncounters;
   uint32_t big_capacity, bin_capacity;
   int tile, tiles_x, tiles_y;
 };
 
 constexpr size_t kStateBytes = 256;  // KeyState's tag (8 bytes) and ticket (4), padded
+constexpr int kMlpRowCounter = 62;   // counters[0..T3_MAX_OBJECTS): big faces; [63]: binned big list
 
 // The tag of a direct frame's key buffer: which workspace, layout and frame
 // size the empty keys belong to (splitmix64 finaliser over the four values).
@@ -327,6 +330,15 @@ static unsigned long long key_tag(const void* ws, size_t keys_at, int64_t npix, 
     h ^= h >> 31;
   }
   return h ? h : 1ull;
+}
+
+static MlpRows mlp_rows(uint8_t* ws, const Layout& L, uint32_t* counters) {
+  MlpRows r;
+  if (L.mlp) {
+    r.rows = reinterpret_cast<float4*>(ws + L.mlp);
+    r.count = counters + kMlpRowCounter;
+  }
+  return r;
 }
 
 static KeyState key_state(void* ws, unsigned long long tag) {
@@ -387,6 +399,10 @@ static int layout_for(const t3_scene& sc, int mode, int tile, int64_t bin_capaci
     for (int o = 0; o < sc.nobjects && o < T3_MAX_OBJECTS; o++)
       vtx += align256(16 * (size_t)mesh_vertex_rows(sc.objects[o].mesh));
     L.end += vtx;
+  }
+  if (sc.lighting.mode == T3_LIGHT_IBL_MLP) {
+    L.mlp = L.end;
+    L.end = align256(L.mlp + 96 * (size_t)sc.frame.width * (size_t)sc.frame.height);
   }
   return T3_OK;
 }
@@ -543,7 +559,8 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     }
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
-      e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st, ks);
+      e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st, ks,
+                       mlp_rows(ws, L, counters));
   } else {
     if (e == cudaSuccess)
       e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st,
@@ -584,7 +601,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
     if (e == cudaSuccess && b.keys)
-      e = launch_shade(ds, dsc, b.keys, b.rec, *out, status, st);
+      e = launch_shade(ds, dsc, b.keys, b.rec, *out, status, st, KeyState(), mlp_rows(ws, L, counters));
   }
   if (e == cudaSuccess) e = mark(3);
   return cuda_rc(e);

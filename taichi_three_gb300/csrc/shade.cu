@@ -123,7 +123,7 @@ static void launch_shade_m(const DevScene& sc, const unsigned long long* keys, c
 
 cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
                          const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st,
-                         KeyState reset) {
+                         KeyState reset, MlpRows rows) {
   const t3_frame& fr = sc_host.frame;
   const int64_t npix = (int64_t)fr.width * fr.height;
   const int max_lobes = t3::max_lobes(sc_host), light_mode = sc_host.lighting.mode;
@@ -141,7 +141,7 @@ cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const 
   else if (light_mode == T3_LIGHT_IBL_PREFILTERED)
     launch_shade_m<T3_LIGHT_IBL_PREFILTERED, false>(sc_host, keys, rec, out, npix, max_lobes, st, reset);
   else if (light_mode == T3_LIGHT_IBL_MLP)
-    return launch_shade_mlp(sc_host, keys, rec, out, status, st);
+    return launch_shade_mlp(sc_host, keys, rec, out, status, st, rows, rows.rows ? reset : KeyState());
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

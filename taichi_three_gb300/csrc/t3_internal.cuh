@@ -152,13 +152,22 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
                                  const BigQueue& big, int32_t big_threshold, cudaStream_t st);
 // the shading pass; the scene descriptor is passed to the kernels by value
 // (sc_dev, its uploaded copy, is kept for kernels that read it from memory)
-// reset (lamp and Monte Carlo lighting): the pass returns every key it reads
-// to empty and then stores reset.tag in *reset.tag_word
+// reset (lamp and Monte Carlo lighting, and the learned IBL with a row list):
+// the pass returns every key it reads to empty and then stores reset.tag in
+// *reset.tag_word
+// rows (learned IBL): the network pass's row list (96 bytes per pixel of the
+// frame) and its counter, zeroed before the pass; without it the one-kernel
+// network pass runs
+struct MlpRows {
+  float4* rows = nullptr;
+  uint32_t* count = nullptr;
+};
 cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
                          const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st,
-                         KeyState reset = KeyState());
+                         KeyState reset = KeyState(), MlpRows rows = MlpRows());
 cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys, const float4* rec,
-                             const t3_outputs& out, int32_t* status, cudaStream_t st);
+                             const t3_outputs& out, int32_t* status, cudaStream_t st,
+                             const MlpRows& rows = MlpRows(), const KeyState& reset = KeyState());
 int max_lobes(const DevScene& sc);
 // the FastMat shape of a flattened material (fast.sig = 0 when none matches)
 void find_fast_material(const DevMaterial& m, FastMat& fast);

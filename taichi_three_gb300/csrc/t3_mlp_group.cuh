@@ -1,200 +1,339 @@
 // t3_mlp_group.cuh -- the learned-IBL network on the tensor cores for the fused
-// shading kernel: several independent 128-row tiles in flight per CTA.
+// shading kernels: groups of four warps per CTA, each group's warps working
+// through a 128-row tile without group-wide barriers.
 //
-// A CTA holds the packed network once (t3_mlp_tc.cuh layout, 70,464 bytes) and
-// kMlpGroups groups of 128 threads (4 warps each).  Group g owns TMEM columns
-// [64 g, 64 g + 64) of the CTA's 512 -- every layer accumulates into the same
-// columns: the epilogue has read a layer's output into registers before the
-// next layer's MMAs are issued -- and two 8 KB A-chunk buffers, which together
-// hold the hidden operand H of the later layers once the first layer is done.
-// The first layer's A operand (128 rows x 400 features) is never materialised
-// whole: the group encodes half an input coordinate (32 features, packed
-// order of t3_mlp_tc.cuh) at a time into a chunk buffer and its elected thread
-// issues that chunk's two K = 16 MMAs; the other buffer is being encoded
-// meanwhile.  Each buffer has an mbarrier that tcgen05.commit arrives on, so a
-// buffer is rewritten only after the MMAs reading it have completed.  Small
-// per-group footprints let six groups share an SM, and groups synchronise with
-// named barriers (ids 1..kMlpGroups), so one group's gathers and encoding
-// overlap the other groups' MMA round trips.
+// A CTA holds the packed network once (t3_mlp_tc.cuh layout, 70,464 bytes).
+// Group g owns TMEM columns [64 g, 64 g + 64) and a ring of two or three 8 KB
+// A-chunk buffers; warp q of a group owns rows 32 q .. 32 q + 31 of the group's tile
+// (the TMEM lanes its quarter of the SM's lanes can read).  The group's warp 0
+// is its leader: its lane 0 issues every tcgen05.mma of the group, so each
+// layer's accumulation runs in issue order on one thread.  Per tile:
+//   layer 1  the warps encode the 400 inputs in 13 K chunks (half an input
+//            coordinate = 32 features, then the 16 tail inputs) into the ring.
+//            Warps 1-3 arrive on the buffer's `full` barrier once their 32
+//            rows are written and go on to the next chunk; the leader writes
+//            its rows, waits for `full`, issues the chunk's MMAs and commits
+//            them to the buffer's `empty` barrier, which every warp waits on
+//            before rewriting that buffer a ring later; after the last
+//            chunk it also commits to `done`.
+//   2 .. 4   after `done`, each warp reads its rows of the accumulator
+//            (tcgen05.ld), adds the bias and applies ReLU while rounding to
+//            BF16 (cvt.rn.relu.bf16x2) into its rows of H (over ring buffers 0
+//            and 1); warps 1-3 arrive on `hfull`, and the leader, after it,
+//            issues the next layer into the same columns and commits to `done`.
+// Only the leader waits for the other warps (on mbarriers, suspended, not
+// spinning); the others wait only for the MMAs whose results they read, so
+// one warp's gathers and encoding run while another's wait.  The group meets
+// at a named barrier once per tile, for the votes on whether to go on.
 //
-// Every wait is bounded; a group whose wait runs out reports false (after one
-// more bounded wait for its own MMAs) and stops.
+// Every wait is bounded.  A warp whose wait runs out records it and from then
+// on skips its waits and outputs but still makes every arrival (a leader
+// still issues and commits), so the group's other warps see the protocol
+// through; the group stops at its next votes (one on pixels left, one on
+// time-outs: every warp of the group gets the same answers, so all of them
+// leave the loop together).  Before TMEM is freed every leader waits
+// (bounded) for its own last MMAs.
 #pragma once
 
 #include "t3_mlp_tc.cuh"
 
 namespace t3 {
 
-#ifndef T3_MLP_GROUPS
-#define T3_MLP_GROUPS 6
-#endif
-constexpr int kMlpGroups = T3_MLP_GROUPS;        // up to 8 (TMEM: 64 columns each)
-constexpr uint32_t kGroupBase = 71680;           // kBlob rounded up to 1 KB
-constexpr uint32_t kChunkBytes = 128 * 32 * 2;   // 128 rows x 32 BF16
-constexpr uint32_t kGroupBytes = 2 * kChunkBytes;  // A0, A1 (together: H, 128 x 64 BF16)
-constexpr uint32_t kMlpGroupSmem = kGroupBase + kMlpGroups * kGroupBytes;
-static_assert(kMlpGroups * 64 <= 512, "TMEM holds 512 columns");
-static_assert(kMlpGroupSmem + kMlpGroups * 1040 + 64 <= 232448, "shared memory per CTA");
+constexpr int kMaxRing = 3;                        // A-chunk buffers per group, at most
+constexpr uint32_t kGroupBase = 71680;             // kBlob rounded up to 1 KB
+constexpr uint32_t kChunkBytes = 128 * 32 * 2;     // 128 rows x 32 BF16
 constexpr uint32_t kGroupTmemCols = 512;
+constexpr uint32_t kMlpWaitLimit = 1u << 24;       // try_wait rounds of one wait
 static_assert(kGroupBase >= kBlob, "packed network overlaps the group areas");
+static_assert(2 * kChunkBytes == 128 * 64 * 2, "H spans ring buffers 0 and 1");
 
-__device__ __forceinline__ void group_sync(int id) {
-  asm volatile("bar.sync %0, 128;" :: "r"(id) : "memory");
+// shared memory of a CTA of G groups with RING chunk buffers each (H, 128 x 64
+// BF16, lies over buffers 0 and 1)
+__host__ __device__ constexpr uint32_t mlp_group_smem(int G, int RING) {
+  return kGroupBase + (uint32_t)G * RING * kChunkBytes;
 }
 
-// true on every thread of the group iff v is true on every thread
-__device__ __forceinline__ bool group_and(bool v, int id) {
+// The shared-memory mbarriers of one group.
+struct GroupBars {
+  uint64_t full[kMaxRing];   // 3 arrivals (warps 1-3): chunk rows written
+  uint64_t empty[kMaxRing];  // MMA commit: the chunk's MMAs have read the buffer
+  uint64_t hfull;            // 3 arrivals (warps 1-3): H rows written (layer input)
+  uint64_t done;             // MMA commit: a layer's accumulator is complete
+};
+
+template <int G>
+struct MlpShared {
+  static_assert(G * 64 <= (int)kGroupTmemCols, "TMEM columns");
+  GroupBars g[G];
+  uint64_t cta_bar;          // the network's bulk copy
+  uint32_t tmem_slot;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+// true on every thread of the group iff v is true on any thread
+__device__ __forceinline__ bool group_any(bool v, int id) {
   uint32_t r;
   asm volatile(
       "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n"
-      " bar.red.and.pred p, %2, 128, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+      " bar.red.or.pred p, %2, 128, q;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(r) : "r"((uint32_t)v), "r"(id) : "memory");
   return r != 0;
 }
 
-struct MlpGroup {
-  unsigned char* sm;   // CTA shared memory (packed network at 0)
-  uint32_t tmem;       // TMEM address of this group's first column (lane 0)
-  uint32_t bar[3];     // shared addresses: chunk buffer 0, chunk buffer 1, layers
-  uint32_t ph[3];      // parity of each barrier's next completion
-  int id;              // named barrier id
-  int row;             // this thread's row (0..127)
-  uint32_t a[2], h;    // shared byte offsets of the chunk buffers and H
+// ---- packed FP32 pairs (f32x2 arithmetic: two lanes' worth per instruction) ----
+__device__ __forceinline__ uint64_t f2(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_split(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// BF16 pair of the packed FP32 pair, ReLU applied (low half = low lane)
+__device__ __forceinline__ uint32_t bf16x2_relu(uint64_t v) {
+  float lo, hi;
+  f2_split(v, lo, hi);
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+__device__ __forceinline__ uint32_t bf16x2(uint64_t v) {
+  float lo, hi;
+  f2_split(v, lo, hi);
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// Half h of coordinate x's Fourier features (packed order of t3_mlp_tc.cuh:
+// sines of octaves 4h..4h+3, then their cosines) as 16 BF16 pairs.  The
+// double-angle steps s' = (2 s) c, c' = (c - s)(c + s) run on two base phases
+// per f32x2 instruction and round exactly as encode_coord's scalar steps, so
+// both see the same FP32 features.  st carries the (sin, cos) pairs of the
+// base phases (j = 0,1 and 2,3) from half 0 to half 1.
+__device__ __forceinline__ void encode_half_bf16(float x, int h, uint64_t st[4], uint32_t out[16]) {
+  const float base[4] = {3.141592653589793f, 3.7360043360892607f, 4.442882938158366f, 5.283508001182123f};
+  if (h == 0) {
+    float s[4], c[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) __sincosf(x * base[j], &s[j], &c[j]);
+    st[0] = f2(s[0], s[1]);  // sines, j = 0, 1
+    st[1] = f2(c[0], c[1]);  // cosines, j = 0, 1
+    st[2] = f2(s[2], s[3]);
+    st[3] = f2(c[2], c[3]);
+  }
+  const uint64_t two = f2(2.0f, 2.0f);
+#pragma unroll
+  for (int o = 0; o < 4; o++) {
+    out[o * 2] = bf16x2(st[0]);
+    out[o * 2 + 1] = bf16x2(st[2]);
+    out[8 + o * 2] = bf16x2(st[1]);
+    out[8 + o * 2 + 1] = bf16x2(st[3]);
+#pragma unroll
+    for (int p = 0; p < 4; p += 2) {
+      const uint64_t s = st[p], c = st[p + 1];
+      st[p] = f2_mul(f2_mul(two, s), c);
+      st[p + 1] = f2_mul(f2_sub(c, s), f2_add(c, s));
+    }
+  }
+}
+
+// tcgen05.ld of 16 columns without the wait (the caller waits once for several)
+__device__ __forceinline__ void tc_ld16_async(uint32_t taddr, uint32_t r[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ---- MMA issue (the leader's lane 0) ---------------------------------------------
+// D (TMEM column col of the group) = A (ksteps x K16 of a_off) * W^T; no commit
+__device__ __forceinline__ void mma_issue(const unsigned char* sm, uint32_t tmem, uint32_t a_off,
+                                          uint32_t a_sbo, uint32_t w_off, uint32_t w_sbo, int ksteps, int N,
+                                          bool accumulate_first) {
+  const uint32_t a = smem_addr(sm + a_off), w = smem_addr(sm + w_off);
+  const uint32_t idesc = tc_idesc(128, N);
+  for (int ks = 0; ks < ksteps; ks++)
+    tc_mma(tmem, tc_desc(a + ks * 256u, 128u, a_sbo), tc_desc(w + ks * 256u, 128u, w_sbo), idesc,
+           (ks > 0 || accumulate_first) ? 1u : 0u);
+}
+
+// ---- the group's warps -------------------------------------------------------------
+struct MlpWarp {
+  unsigned char* sm;  // CTA shared memory (packed network at 0)
+  uint32_t tmem;      // the group's first column, this warp's lane quarter
+  uint32_t bars;      // shared address of the group's GroupBars
+  uint32_t area;      // shared byte offset of the group's ring (and H)
+  uint32_t chunk;     // chunks of the group issued so far (ring position)
+  uint32_t dph;       // parity of the next `done` completion
+  uint32_t hph;       // parity of the next `hfull` completion
+  int row;            // this lane's row of the tile
+  bool leader;        // warp 0 of the group: issues the group's MMAs
+  bool err;           // a wait ran out (warp-uniform)
 };
 
-// One thread polls the mbarrier; the rest of the group sleeps in the named
-// barrier that publishes the outcome (polling by every thread would spend the
-// issue slots the other groups need).
-__device__ __forceinline__ bool group_wait(MlpGroup& G, int b) {
-  bool ok = true;
-  if (G.row == 0) {
-    ok = mbar_wait_bounded(G.bar[b], G.ph[b], 1u << 24);
-    if (!ok) mbar_wait_bounded(G.bar[b], G.ph[b], 1u << 24);
-  }
-  G.ph[b] ^= 1u;
-  ok = group_and(ok, G.id);
-  tc_fence_after();
-  return ok;
+__device__ __forceinline__ uint32_t bar_full(uint32_t bars, int b) { return bars + 8u * b; }
+__device__ __forceinline__ uint32_t bar_empty(uint32_t bars, int b) { return bars + 8u * (kMaxRing + b); }
+__device__ __forceinline__ uint32_t bar_hfull(uint32_t bars) { return bars + 8u * (2 * kMaxRing); }
+__device__ __forceinline__ uint32_t bar_done(uint32_t bars) { return bars + 8u * (2 * kMaxRing + 1); }
+
+__device__ __forceinline__ void warp_wait(MlpWarp& W, uint32_t bar, uint32_t parity) {
+  if (W.err) return;
+  const bool ok = mbar_wait_bounded(bar, parity, kMlpWaitLimit);
+  W.err = !__all_sync(0xFFFFFFFFu, ok);
 }
 
-// Issue (by the group's first thread, after a group barrier): D += A_chunk * W^T
-__device__ __forceinline__ void group_issue(const MlpGroup& G, uint32_t a_off, uint32_t a_sbo,
-                                            uint32_t w_off, uint32_t w_sbo, int ksteps, int N,
-                                            uint32_t col, bool accumulate_first, int commit_bar) {
-  const uint32_t a = smem_addr(G.sm + a_off), w = smem_addr(G.sm + w_off);
-  const uint32_t idesc = tc_idesc(128, N);
-  for (int ks = 0; ks < ksteps; ks++) {
-    tc_mma(G.tmem + col, tc_desc(a + ks * 256u, 128u, a_sbo), tc_desc(w + ks * 256u, 128u, w_sbo), idesc,
-           (ks > 0 || accumulate_first) ? 1u : 0u);
+// The warp's rows are written (shared memory for the MMAs, TMEM reads done).
+// Warps 1-3 arrive on `bar`; the leader waits for their three arrivals
+// (phase `parity`) and then its lane 0 runs issue().
+template <typename Issue>
+__device__ __forceinline__ void warp_handoff(MlpWarp& W, uint32_t bar, uint32_t parity, Issue issue) {
+  fence_async_smem();
+  tc_fence_before();
+  __syncwarp();
+  if (!W.leader) {
+    if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
+    return;
   }
-  tc_commit(G.bar[commit_bar]);
+  warp_wait(W, bar, parity);
+  if ((threadIdx.x & 31) == 0) {
+    tc_fence_after();
+    issue();
+  }
+  __syncwarp();
 }
 
-// bias + ReLU of this thread's row of the 64 columns at `col`, written as BF16 into H
-__device__ __forceinline__ void group_epilogue(const MlpGroup& G, uint32_t col, uint32_t b_off) {
-  const uint32_t lane_base = (uint32_t)((threadIdx.x & 96) << 16);  // warp's TMEM lane quarter
-  const float4* bias = reinterpret_cast<const float4*>(G.sm + b_off);  // 16-byte aligned
+// Layer-1 K chunk k (0..12) of this warp's rows into the next ring buffer.
+template <int RING>
+__device__ __forceinline__ void warp_chunk(MlpWarp& W, int k, const float in[6], float rough, float metal,
+                                           uint64_t st[4]) {
+  const uint32_t c = W.chunk++;
+  const int b = (int)(c % RING);
+  if (c >= (uint32_t)RING) warp_wait(W, bar_empty(W.bars, b), (c / RING - 1) & 1u);
+  unsigned char* A = W.sm + W.area + (uint32_t)b * kChunkBytes;
+  if (k < 12) {
+    uint32_t f[16];
+    encode_half_bf16(in[k >> 1], k & 1, st, f);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      *reinterpret_cast<uint4*>(A + tc_chunk_off(W.row, 8 * q, 32)) = make_uint4(f[4 * q], f[4 * q + 1],
+                                                                                 f[4 * q + 2], f[4 * q + 3]);
+  } else {
+    // roughness, metallic, zero padding (K = 16 layout)
+    float t[8] = {rough, metal, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    *reinterpret_cast<uint4*>(A + tc_chunk_off(W.row, 0, 16)) = pack8_bf16(t);
+    *reinterpret_cast<uint4*>(A + tc_chunk_off(W.row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  const uint32_t bars = W.bars, tmem = W.tmem & 0xFFFFu, a_off = W.area + (uint32_t)b * kChunkBytes;
+  const unsigned char* sm = W.sm;
+  warp_handoff(W, bar_full(bars, b), (c / RING) & 1u, [&] {
+    if (k < 12) mma_issue(sm, tmem, a_off, 512u, kW1 + (uint32_t)k * 512u, 6400u, 2, 64, k > 0);
+    else mma_issue(sm, tmem, a_off, 256u, kW1 + 6144u, 6400u, 1, 64, true);
+    tc_commit(bar_empty(bars, b));
+    if (k == 12) tc_commit(bar_done(bars));
+  });
+}
+
+// bias + ReLU of this warp's rows of the layer output, as BF16 into H
+__device__ __forceinline__ void warp_epilogue(MlpWarp& W, uint32_t b_off) {
+  const uint64_t* bias = reinterpret_cast<const uint64_t*>(W.sm + b_off);  // FP32 pairs
+  unsigned char* Hm = W.sm + W.area;
 #pragma unroll
   for (int c = 0; c < 64; c += 16) {
-    float v[16];
-    tc_ld16(G.tmem + lane_base + col + c, v);
+    uint32_t r[16];
+    tc_ld16_async(W.tmem + c, r);
+    tc_wait_ld();
+    uint32_t h[8];
 #pragma unroll
-    for (int i = 0; i < 16; i += 4) {
-      const float4 b = bias[(c + i) >> 2];
-      v[i] = fmaxf(v[i] + b.x, 0.0f);
-      v[i + 1] = fmaxf(v[i + 1] + b.y, 0.0f);
-      v[i + 2] = fmaxf(v[i + 2] + b.z, 0.0f);
-      v[i + 3] = fmaxf(v[i + 3] + b.w, 0.0f);
-    }
-    *reinterpret_cast<uint4*>(G.sm + G.h + tc_chunk_off(G.row, c, 64)) = pack8_bf16(v);
-    *reinterpret_cast<uint4*>(G.sm + G.h + tc_chunk_off(G.row, c + 8, 64)) = pack8_bf16(v + 8);
+    for (int i = 0; i < 8; i++)
+      h[i] = bf16x2_relu(f2_add(f2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1])), bias[(c >> 1) + i]));
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+      *reinterpret_cast<uint4*>(Hm + tc_chunk_off(W.row, c + 8 * q, 64)) =
+          make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
   }
 }
 
-// Half h of the row's coordinate x as 32 BF16 features in chunk buffer b (K = 32 layout)
-__device__ __forceinline__ void group_encode_half(const MlpGroup& G, int b, float x, int h, float st[8]) {
-  float f[32];
-  encode_half(x, h, st, f);
-  unsigned char* A = G.sm + G.a[b];
+// The network for the warp's rows of one tile: in = the row's six direction
+// coordinates (already mirrored), rough, metal; rows whose lane has no pixel
+// run on whatever they hold.  out[16]: the row's output.  False when a wait
+// ran out (now or earlier): the output is then not to be used.
+template <int RING>
+__device__ __forceinline__ bool warp_network(MlpWarp& W, const float in[6], float rough, float metal,
+                                             float out[16]) {
+  uint64_t st[4];
 #pragma unroll
-  for (int q = 0; q < 4; q++)
-    *reinterpret_cast<uint4*>(A + tc_chunk_off(G.row, 8 * q, 32)) = pack8_bf16(f + 8 * q);
-}
-
-// The last 16 inputs (roughness, metallic, zero padding) in chunk buffer b (K = 16 layout)
-__device__ __forceinline__ void group_encode_tail(const MlpGroup& G, int b, float rough, float metal) {
-  unsigned char* A = G.sm + G.a[b];
-  float t[8] = {rough, metal, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  *reinterpret_cast<uint4*>(A + tc_chunk_off(G.row, 0, 16)) = pack8_bf16(t);
-  t[0] = t[1] = 0.0f;
-  *reinterpret_cast<uint4*>(A + tc_chunk_off(G.row, 8, 16)) = pack8_bf16(t);
-}
-
-// The whole network for the group's tile.  `in` = this row's six direction
-// coordinates (already mirrored), rough, metal; rows of threads with
-// `valid == false` are computed on whatever their buffers hold and ignored.
-// out[16] receives the row's output.  Returns false on a timed-out wait.
-__device__ __forceinline__ bool group_tile(MlpGroup& G, const float in[6], float rough, float metal,
-                                           float out[16]) {
-  const bool leader = G.row == 0;
-  // layer 1: thirteen K chunks (6 coordinates x 2 halves x 32 features, then
-  // the 16 tail inputs), chunk k in buffer k & 1, all into the group's columns
-  float st[8];
-  for (int k = 0; k < 13; k++) {
-    const int b = k & 1;
-    if (k >= 2 && !group_wait(G, b)) return false;  // chunk k - 2 has left buffer b
-    if (k < 12) group_encode_half(G, b, in[k >> 1], k & 1, st);
-    else group_encode_tail(G, b, rough, metal);
-    fence_async_smem();
-    tc_fence_before();
-    group_sync(G.id);
-    if (leader) {
-      tc_fence_after();
-      if (k < 12) group_issue(G, G.a[b], 512u, kW1 + (uint32_t)k * 512u, 6400u, 2, 64, 0, k > 0, b);
-      else group_issue(G, G.a[b], 256u, kW1 + 6144u, 6400u, 1, 64, 0, true, b);
-    }
-  }
-  if (!group_wait(G, 1)) return false;  // chunk 11
-  if (!group_wait(G, 0)) return false;  // chunk 12: layer 1 complete
-  // layers 2-4 read the previous output back (bias + ReLU into H) and overwrite
-  // the same columns: each epilogue's TMEM loads complete (tcgen05.wait::ld)
-  // before the group barrier that precedes the next issue
-  const uint32_t w[3] = {kW2, kW3, kW4};
+  for (int k = 0; k < 13; k++) warp_chunk<RING>(W, k, in, rough, metal, st);
   const uint32_t bias_in[3] = {kB1, kB2, kB3};
+  const uint32_t w_next[3] = {kW2, kW3, kW4};
   for (int l = 0; l < 3; l++) {
-    group_epilogue(G, 0, bias_in[l]);
-    fence_async_smem();
-    tc_fence_before();
-    group_sync(G.id);
-    if (leader) {
-      tc_fence_after();
-      group_issue(G, G.h, 1024u, w[l], 1024u, 4, l == 2 ? 16 : 64, 0, false, 2);
-    }
-    if (!group_wait(G, 2)) return false;
+    warp_wait(W, bar_done(W.bars), W.dph);
+    W.dph ^= 1u;
+    tc_fence_after();
+    if (!W.err) warp_epilogue(W, bias_in[l]);
+    const uint32_t bars = W.bars, tmem = W.tmem & 0xFFFFu, area = W.area, w = w_next[l];
+    const unsigned char* sm = W.sm;
+    warp_handoff(W, bar_hfull(bars), W.hph, [&] {
+      mma_issue(sm, tmem, area, 1024u, w, 1024u, 4, l == 2 ? 16 : 64, false);
+      tc_commit(bar_done(bars));
+    });
+    W.hph ^= 1u;
   }
-  const uint32_t lane_base = (uint32_t)((threadIdx.x & 96) << 16);
-  tc_ld16(G.tmem + lane_base, out);
-  const float* b4 = reinterpret_cast<const float*>(G.sm + kB4);
+  warp_wait(W, bar_done(W.bars), W.dph);
+  W.dph ^= 1u;
+  tc_fence_after();
+  if (W.err) return false;
+  uint32_t r[16];
+  tc_ld16_async(W.tmem, r);
+  tc_wait_ld();
+  const float* b4 = reinterpret_cast<const float*>(W.sm + kB4);
 #pragma unroll
-  for (int i = 0; i < 16; i++) out[i] += b4[i];
-  tc_fence_before();
+  for (int i = 0; i < 16; i++) out[i] = __uint_as_float(r[i]) + b4[i];
   return true;
 }
 
 // CTA prologue: barriers, TMEM (512 columns, warp 0), bulk copy of the packed
 // network.  Returns false (on every thread) if the copy's wait ran out.
-__device__ __forceinline__ bool group_cta_begin(unsigned char* sm, uint64_t* cta_bar, uint64_t (*gbar)[3],
-                                                uint32_t* tmem_slot, const void* blob) {
-  const uint32_t cb = smem_addr(cta_bar);
+template <int G>
+__device__ __forceinline__ bool mlp_cta_begin(unsigned char* sm, MlpShared<G>& S, const void* blob) {
+  const uint32_t cb = smem_addr(&S.cta_bar);
   if (threadIdx.x == 0) {
     mbar_init(cb, 1);
-    for (int g = 0; g < kMlpGroups; g++)
-      for (int k = 0; k < 3; k++) mbar_init(smem_addr(&gbar[g][k]), 1);
+    for (int g = 0; g < G; g++) {
+      const uint32_t bars = smem_addr(&S.g[g]);
+      for (int b = 0; b < kMaxRing; b++) {
+        mbar_init(bar_full(bars, b), 3);
+        mbar_init(bar_empty(bars, b), 1);
+      }
+      mbar_init(bar_hfull(bars), 3);
+      mbar_init(bar_done(bars), 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 :: "r"(smem_addr(tmem_slot)), "r"(kGroupTmemCols) : "memory");
+                 :: "r"(smem_addr(&S.tmem_slot)), "r"(kGroupTmemCols) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
@@ -206,30 +345,41 @@ __device__ __forceinline__ bool group_cta_begin(unsigned char* sm, uint64_t* cta
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
         :: "r"(smem_addr(sm)), "l"(blob), "r"(kBlob), "r"(cb) : "memory");
   }
-  bool ok = mbar_wait_bounded(cb, 0, 1u << 24);
-  if (!ok) mbar_wait_bounded(cb, 0, 1u << 24);
+  bool ok = mbar_wait_bounded(cb, 0, kMlpWaitLimit);
+  if (!ok) mbar_wait_bounded(cb, 0, kMlpWaitLimit);
   return __syncthreads_and(ok) != 0;
 }
 
-__device__ __forceinline__ MlpGroup group_init(unsigned char* sm, uint64_t (*gbar)[3], uint32_t tmem_base) {
-  MlpGroup G;
-  const int g = threadIdx.x >> 7;
-  G.sm = sm;
-  G.tmem = tmem_base + (uint32_t)g * 64u;
-  for (int k = 0; k < 3; k++) {
-    G.bar[k] = smem_addr(&gbar[g][k]);
-    G.ph[k] = 0;
-  }
-  G.id = 1 + g;
-  G.row = threadIdx.x & 127;
-  const uint32_t base = kGroupBase + (uint32_t)g * kGroupBytes;
-  G.a[0] = base;
-  G.a[1] = base + kChunkBytes;
-  G.h = base;  // both chunk buffers are free once the first layer has completed
-  return G;
+template <int G, int RING>
+__device__ __forceinline__ MlpWarp mlp_warp_init(unsigned char* sm, MlpShared<G>& S, uint32_t tmem_base) {
+  MlpWarp W;
+  const int warp = threadIdx.x >> 5, g = warp >> 2, q = warp & 3;
+  W.sm = sm;
+  W.tmem = tmem_base + (uint32_t)g * 64u + ((uint32_t)(q * 32) << 16);
+  W.bars = smem_addr(&S.g[g]);
+  W.area = kGroupBase + (uint32_t)g * RING * kChunkBytes;
+  W.chunk = 0;
+  W.dph = 0;
+  W.hph = 0;
+  W.row = q * 32 + (threadIdx.x & 31);
+  W.leader = q == 0;
+  W.err = false;
+  return W;
 }
 
-__device__ __forceinline__ void group_cta_end(uint32_t tmem_base) {
+// A leader's last act: commit (tracking every MMA it issued) and wait for it,
+// so no MMA of the group is running when TMEM is freed.  False if that wait
+// ran out.
+__device__ __forceinline__ bool warp_drain(MlpWarp& W) {
+  if (!W.leader) return true;
+  if ((threadIdx.x & 31) == 0) tc_commit(bar_done(W.bars));
+  __syncwarp();
+  const bool ok = __all_sync(0xFFFFFFFFu, mbar_wait_bounded(bar_done(W.bars), W.dph, kMlpWaitLimit));
+  W.dph ^= 1u;
+  return ok;
+}
+
+__device__ __forceinline__ void mlp_cta_end(uint32_t tmem_base) {
   tc_fence_before();
   __syncthreads();
   if (threadIdx.x < 32) {
