@@ -238,28 +238,32 @@ def direct_launches(scene):
     return n + 1
 
 
-def stage_times(scene, reps=10):
-    """Median ms of the three stages of t3_render_staged for the scene's
-    current state (upload+clear | raster | shade)."""
+def stage_times(scene, reps=10, split_shade=False):
+    """Median ms of the stages of t3_render_staged_n for the scene's current
+    state (upload+clear | raster | shade); split_shade (learned IBL) also
+    times the shading's row prepass and network kernel apart."""
     from taichi_three_gb300 import _native as N
     lib = N.load()
     scene.render()
     sc, keep = scene.describe()
     outs = N.t3_outputs(scene.image.data_ptr(), scene.face_id.data_ptr(),
                         scene.engine.depth.data_ptr(), scene.depth_f.data_ptr())
-    evs = [C.c_void_p() for _ in range(4)]
+    evs = [C.c_void_p() for _ in range(5)]
     for e in evs:
         N.check(lib.t3_event_create(C.byref(e)), "t3_event_create")
-    arr = (C.c_void_p * 4)(*[e.value for e in evs])
-    st = {k: [] for k in ("clear", "raster", "shade")}
+    arr = (C.c_void_p * 5)(*[e.value for e in evs])
+    spans = {"clear": (0, 1), "raster": (1, 2), "shade": (2, 4)}
+    if split_shade:
+        spans.update({"shade_rows": (2, 3), "shade_net": (3, 4)})
+    st = {k: [] for k in spans}
     mode = N.T3_RASTER_DIRECT if scene.raster_mode == "direct" else N.T3_RASTER_BINNED
     for _ in range(reps):
-        N.check(lib.t3_render_staged(C.byref(sc), mode, scene.tile, scene.bin_capacity,
-                                     scene._ws.data_ptr(), scene._ws.numel(),
-                                     scene._status.data_ptr(), C.byref(outs),
-                                     torch.cuda.current_stream().cuda_stream, arr), "staged")
+        N.check(lib.t3_render_staged_n(C.byref(sc), mode, scene.tile, scene.bin_capacity,
+                                       scene._ws.data_ptr(), scene._ws.numel(),
+                                       scene._status.data_ptr(), C.byref(outs),
+                                       torch.cuda.current_stream().cuda_stream, arr, 5), "staged")
         ms = C.c_float()
-        for name, (a, b) in zip(st, ((0, 1), (1, 2), (2, 3))):
+        for name, (a, b) in spans.items():
             N.check(lib.t3_event_elapsed_ms(evs[a], evs[b], C.byref(ms)), "elapsed")
             st[name].append(ms.value)
     for e in evs:
@@ -288,7 +292,7 @@ def bench_learned_ibl(flush, tc_peak):
         scene, _ = tina.workloads.ibl_soup_scene(skybox=sky, mode=mode, spp=spp, mlp=net)
         g = graph_of(scene.render)
         ms = time_graph(g, 20 if mode == "mlp" else 5, flush)
-        stages = stage_times(scene, 5)
+        stages = stage_times(scene, 5, split_shade=mode == "mlp")
         res[key] = (ms, scene.img.cpu().numpy().reshape(-1, 3), scene, stages)
     scene = res["mlp"][2]
     fid = scene.face_id.cpu().numpy().ravel()
@@ -297,6 +301,7 @@ def bench_learned_ibl(flush, tc_peak):
     _, truth = oracle.pixels_f64(scene, pick, spp=4096, seed=12345)
     de = {k: float(tina.colour.delta_e2000(v[1][pick], truth).mean()) for k, v in res.items()}
     shade_ms = res["mlp"][3]["shade"]
+    net_ms = res["mlp"][3]["shade_net"]
     flop = MLP_FLOP_PER_PIXEL * len(cov)
     return {"workload": "1920x1080 soup, 1,000,000 faces, PBR per-face, lit only by a 1024x512 "
                         "FP16 procedural sky (gradient + 12 Gaussian lobes)",
@@ -306,11 +311,14 @@ def bench_learned_ibl(flush, tc_peak):
             "dE2000_mean_mlp": de["mlp"], "dE2000_mean_mc256": de["mc256"],
             "dE2000_reference": "FP64 oracle, 4096 samples/pixel, 4000 random covered pixels",
             "train_s": train_s, "train": "16M samples, 4096-sample MC targets, 12000 Adam steps of 32768",
-            "mlp_shade_kernel_ms": shade_ms,
-            "roofline_mlp": {"bound": "tensor", "achieved": flop / (shade_ms / 1e3) / 1e12,
+            "mlp_shade_ms": shade_ms, "mlp_net_kernel_ms": net_ms,
+            "roofline_mlp": {"bound": "tensor", "kernel": "k_mlp_net", "achieved": flop / (net_ms / 1e3) / 1e12,
                              "peak": tc_peak, "unit": "TFLOP/s",
-                             "frac": flop / (shade_ms / 1e3) / 1e12 / tc_peak,
+                             "frac": flop / (net_ms / 1e3) / 1e12 / tc_peak,
                              "flop_per_pixel": MLP_FLOP_PER_PIXEL, "pixels": int(len(cov))},
+            "roofline_mlp_shading": {"bound": "tensor", "kernels": "k_mlp_rows + k_mlp_net",
+                                     "achieved": flop / (shade_ms / 1e3) / 1e12, "peak": tc_peak,
+                                     "unit": "TFLOP/s", "frac": flop / (shade_ms / 1e3) / 1e12 / tc_peak},
             "stages_ms": {k: v[3] for k, v in res.items()}}, sky, net
 
 

@@ -369,6 +369,13 @@ int t3_tonemap(float* rgb, int64_t n, void* stream);
 int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
                      void* workspace, size_t workspace_bytes, int32_t* status,
                      const t3_outputs* out, void* stream, void* const* stage_events);
+/* The same with nevents = 4 or 5 events; with 5, event [3] is recorded between
+ * the learned-IBL shading's two kernels (after the row prepass, before the
+ * network kernel) -- for other lighting together with [4] -- and [4] after
+ * shading. */
+int t3_render_staged_n(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
+                       void* workspace, size_t workspace_bytes, int32_t* status,
+                       const t3_outputs* out, void* stream, void* const* stage_events, int nevents);
 
 /* Timing-event helpers for callers without their own CUDA runtime binding. */
 int t3_event_create(void** event);

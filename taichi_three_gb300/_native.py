@@ -165,6 +165,8 @@ SIGNATURES = {
     "t3_accumulate": (C.c_int, [_VP, _VP, _I64, C.c_int, _VP]),
     "t3_render_staged": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,
                                    C.POINTER(t3_outputs), _VP, C.POINTER(C.c_void_p)]),
+    "t3_render_staged_n": (C.c_int, [C.POINTER(t3_scene), C.c_int, C.c_int, _I64, _VP, _SZ, _VP,
+                                     C.POINTER(t3_outputs), _VP, C.POINTER(C.c_void_p), C.c_int]),
     "t3_render_noalloc": (C.c_int, [C.POINTER(t3_scene), _VP, C.POINTER(t3_outputs), _VP]),
     "t3_raster_fragments": (C.c_int, [C.POINTER(t3_scene), _VP, _SZ, C.POINTER(C.c_int64), _VP]),
     "t3_red_min_rate": (C.c_int, [_VP, _I64, C.c_int, _VP]),

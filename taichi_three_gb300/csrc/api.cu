@@ -509,7 +509,15 @@ int t3_render(const t3_scene* scene, int mode, int tile, int64_t bin_capacity, v
 int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
                      void* workspace, size_t workspace_bytes, int32_t* status,
                      const t3_outputs* out, void* stream, void* const* stage_events) {
+  return t3_render_staged_n(scene, mode, tile, bin_capacity, workspace, workspace_bytes, status, out, stream,
+                            stage_events, 4);
+}
+
+int t3_render_staged_n(const t3_scene* scene, int mode, int tile, int64_t bin_capacity,
+                       void* workspace, size_t workspace_bytes, int32_t* status,
+                       const t3_outputs* out, void* stream, void* const* stage_events, int nevents) {
   if (!scene || !workspace || !status || !out || !out->rgb) return T3_EINVAL;
+  if (stage_events && nevents != 4 && nevents != 5) return T3_EINVAL;
   static thread_local DevScene ds;
   int r = make_dev_scene(*scene, ds);
   if (r) return r;
@@ -524,6 +532,13 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
   auto mark = [&](int k) -> cudaError_t {
     if (!stage_events || !stage_events[k]) return cudaSuccess;
     return cudaEventRecord((cudaEvent_t)stage_events[k], st);
+  };
+  // with five events: [3] between the learned-IBL shading's two kernels
+  const int last = stage_events && nevents == 5 ? 4 : 3;
+  auto rows_of = [&]() {
+    MlpRows r = mlp_rows(ws, L, counters);
+    if (last == 4) r.split = (cudaEvent_t)stage_events[3];
+    return r;
   };
   cudaError_t e = mark(0);
   if (mode == T3_RASTER_DIRECT) {
@@ -560,7 +575,7 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess)
       e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st, ks,
-                       mlp_rows(ws, L, counters));
+                       rows_of());
   } else {
     if (e == cudaSuccess)
       e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st,
@@ -601,9 +616,10 @@ int t3_render_staged(const t3_scene* scene, int mode, int tile, int64_t bin_capa
     if (e == cudaSuccess) e = mark(2);
     if (e == cudaSuccess) e = launch_tile(dsc, b, L.tiles_x * L.tiles_y, *out, st);
     if (e == cudaSuccess && b.keys)
-      e = launch_shade(ds, dsc, b.keys, b.rec, *out, status, st, KeyState(), mlp_rows(ws, L, counters));
+      e = launch_shade(ds, dsc, b.keys, b.rec, *out, status, st, KeyState(), rows_of());
   }
-  if (e == cudaSuccess) e = mark(3);
+  if (e == cudaSuccess && last == 4 && !(ds.lighting.mode == T3_LIGHT_IBL_MLP && L.mlp)) e = mark(3);
+  if (e == cudaSuccess) e = mark(last);
   return cuda_rc(e);
 }
 

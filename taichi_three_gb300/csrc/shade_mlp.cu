@@ -42,10 +42,24 @@ struct MlpCoeffs {
 // lobe weights of one fragment (materials of Lambert, CookTorrance and
 // Emission leaves with at most one CookTorrance; checked on the host)
 template <int NL, bool TEX, int SIG>
-__device__ __forceinline__ void eval_mlp_coeffs(const DevMaterial& mat, const Frag& fg, MlpCoeffs& q) {
+__device__ __forceinline__ void eval_mlp_coeffs(const DevObject& ob, const Frag& fg, MlpCoeffs& q) {
+  const DevMaterial& mat = ob.mat;
   q.cd = q.c1 = q.c2 = q.base = v3(0.f, 0.f, 0.f);
   q.rough = 1.0f;
   q.metal = 0.0f;
+  if constexpr ((SIG & T3_SIG_FAST) != 0) {
+    // the PBR shape Mix(Lambert * C, CookTorrance(f0 = F), F) (FastMat): the
+    // weights (1 - F) C and F with each parameter evaluated once -- the same
+    // products as the loop below forms (1 x a = a, 0 + a = a exactly)
+    const V3 c = eval_basic(mat.nodes[ob.fast.node[0]], fg);
+    const V3 f = eval_value<false>(mat, ob.fast.node[1], fg);
+    q.cd = one_minus(f) * c;
+    q.c1 = f * f;
+    q.c2 = f * one_minus(f);
+    q.rough = eval_basic(mat.nodes[ob.fast.node[2]], fg).x;
+    q.metal = fminf(1.0f, fmaxf(0.0f, (f.x + f.y + f.z) * (1.0f / 3.0f)));
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < NL; k++) {
     if (k >= mat.nlobes) continue;
@@ -158,11 +172,12 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
           store_rgb(fr, out, pix, pg.fg.color);  // a line pixel
         } else if (hit) {
           mine = true;
-          eval_mlp_coeffs<NL, TEX, SIG>(pg.ob->mat, pg.fg, q);
+          eval_mlp_coeffs<NL, TEX, SIG>(*pg.ob, pg.fg, q);
           if (lt.nlights > 0) {
             LobeState<NL> L;
             V3 amb, emi;
-            eval_material<NL, TEX, SIG>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
+            if constexpr ((SIG & T3_SIG_FAST) != 0) eval_material_fast<NL, SIG>(*pg.ob, pg.fg, pg.vdir, L, amb, emi);
+            else eval_material<NL, TEX, SIG>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
             q.base = q.base + lamps_term<NL, SIG>(lt, L, pg.fg, pg.vdir);
           }
           const float nv[6] = {pg.fg.normal.x, pg.fg.normal.y, pg.fg.normal.z, pg.vdir.x, pg.vdir.y, pg.vdir.z};
@@ -259,11 +274,12 @@ k_mlp_rows(const __grid_constant__ DevScene scene, const unsigned long long* __r
         store_rgb(fr, out, pix, pg.fg.color);  // a line pixel
       } else if (hit) {
         have = true;
-        eval_mlp_coeffs<NL, TEX, SIG>(pg.ob->mat, pg.fg, q);
+        eval_mlp_coeffs<NL, TEX, SIG>(*pg.ob, pg.fg, q);
         if (lt.nlights > 0) {
           LobeState<NL> L;
           V3 amb, emi;
-          eval_material<NL, TEX, SIG>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
+          if constexpr ((SIG & T3_SIG_FAST) != 0) eval_material_fast<NL, SIG>(*pg.ob, pg.fg, pg.vdir, L, amb, emi);
+          else eval_material<NL, TEX, SIG>(pg.ob->mat, pg.fg, pg.vdir, L, amb, emi);
           q.base = q.base + lamps_term<NL, SIG>(lt, L, pg.fg, pg.vdir);
         }
         const float nv[6] = {pg.fg.normal.x, pg.fg.normal.y, pg.fg.normal.z, pg.vdir.x, pg.vdir.y, pg.vdir.z};
@@ -316,6 +332,9 @@ k_mlp_net(const __grid_constant__ DevScene scene, const float4* __restrict__ row
       const float4 a = valid ? __ldg(r) : make_float4(0.f, 0.f, 0.f, 0.f);
       const float4 b = valid ? __ldg(r + 1) : make_float4(0.f, 0.f, 1.f, 0.f);
       const float in[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+      // the row of the group's next tile, on its way while this one runs
+      const int64_t next = (t + (int64_t)gridDim.x * kNetGroups) * 128 + W.row;
+      if (next < (int64_t)n) asm volatile("prefetch.global.L1 [%0];" :: "l"(rows + next * kRowVec));
       float y[16];
       const bool was_ok = !W.err;
       if (!warp_network<kNetRing>(W, in, b.z, b.w, y)) {
@@ -359,6 +378,7 @@ static cudaError_t launch_shade_mlp_t(const DevScene& sc, const unsigned long lo
     k_mlp_rows<BLOCK, PPT, NL, TEX, SIG><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix, rows.rows,
                                                                          rows.count, reset);
     e = cudaGetLastError();
+    if (e == cudaSuccess && rows.split) e = cudaEventRecord(rows.split, st);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_mlp_net, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmem);
     if (e != cudaSuccess) return e;
@@ -380,7 +400,12 @@ cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys,
                              const t3_outputs& out, int32_t* status, cudaStream_t st, const MlpRows& rows,
                              const KeyState& reset) {
   const int64_t npix = (int64_t)sc.frame.width * sc.frame.height;
-  // untextured PBR scenes take the instance with the lobe kinds as constants
+  // untextured PBR scenes take the instance with the lobe kinds as constants,
+  // and with each material parameter evaluated once when every object has the
+  // PBR material shape
+  if (!has_textures(sc) && fast_signature(sc) == T3_SIG_PBR)
+    return launch_shade_mlp_t<2, false, T3_SIG_PBR | T3_SIG_FAST>(sc, keys, rec, out, npix, status, st, rows,
+                                                                  reset);
   if (!has_textures(sc) && lobe_signature(sc) == T3_SIG_PBR)
     return launch_shade_mlp_t<2, false, T3_SIG_PBR>(sc, keys, rec, out, npix, status, st, rows, reset);
   if (max_lobes(sc) <= 2) return launch_shade_mlp_t<2, true, 0>(sc, keys, rec, out, npix, status, st, rows, reset);

@@ -161,6 +161,7 @@ cudaError_t launch_raster_direct(const t3_frame& fr, const t3_object& ob, unsign
 struct MlpRows {
   float4* rows = nullptr;
   uint32_t* count = nullptr;
+  cudaEvent_t split = nullptr;  // recorded between the two kernels (timing)
 };
 cudaError_t launch_shade(const DevScene& sc_host, const DevScene* sc_dev, const unsigned long long* keys,
                          const float4* rec, const t3_outputs& out, int32_t* status, cudaStream_t st,
