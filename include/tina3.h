@@ -60,6 +60,11 @@ extern "C" {
  * every tile then gives up, writes background and sets T3_STATUS_TIMEOUT.  No
  * copy is in flight, so nothing is drained; the next frame is unaffected. */
 #define T3_STARVE_BIN_COPY 512
+/* The same for the learned-IBL network pass: its leader warps issue no
+ * tensor-core operation, so every wait on one (wait_limit polls each) runs
+ * out; the pass stops, leaves its covered pixels' colour unwritten and sets
+ * T3_STATUS_TIMEOUT.  Nothing was issued, so nothing is drained. */
+#define T3_STARVE_NETWORK 1024
 
 typedef struct t3_frame {
   int32_t width, height; /* Engine.res                                      */
@@ -71,9 +76,10 @@ typedef struct t3_frame {
   float bgcolor[3];      /* Scene(bgcolor=...) image.fill value             */
   float linecolor[3];    /* WireframeRaster(linecolor=...), wireframe.py:6-20 */
   int32_t wait_limit;    /* polls of the binned tiles' first bounded wait on
-                            their bin copy (0: the default, 1 << 22); the
-                            second wait, which lets an issued copy land, keeps
-                            the default                                     */
+                            their bin copy (0: the default, 1 << 22) and of
+                            each wait of the learned-IBL network pass on the
+                            tensor cores (0: 1 << 24); the waits that let an
+                            issued copy or MMA land keep the defaults       */
   int32_t _pad;          /* 184 bytes: keeps t3_scene.lighting.lights 16-byte aligned */
 } t3_frame;
 

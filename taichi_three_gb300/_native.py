@@ -34,6 +34,7 @@ T3_CULLING, T3_CLIPPING, T3_SMOOTHING, T3_TEXTURING, T3_TONEMAP = 1, 2, 4, 8, 16
 T3_WIRE_CLIPPING = 32
 T3_SHADE_OWNED, T3_SHADE_EMPTY = 128, 256
 T3_STARVE_BIN_COPY = 512
+T3_STARVE_NETWORK = 1024
 T3_MESH_SOUP, T3_MESH_GRID, T3_MESH_INDEXED, T3_MESH_PARTICLES, T3_MESH_LINES = 0, 1, 2, 3, 4
 T3_MESH_TRANSFORM, T3_MESH_NOCULL, T3_MESH_FLIP_ORDER, T3_MESH_FLIP_NORMAL, T3_MESH_FLAT_NORMAL = \
     1, 2, 4, 8, 16

@@ -118,7 +118,7 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
     const Env env{lt.env, lt.env_w, lt.env_h, lt.env_half};
     const int H = fr.height;
     const int g = warp >> 2;
-    MlpWarp W = mlp_warp_init<kFusedGroups, kFusedRing>(sm, S, tmem_base);
+    MlpWarp W = mlp_warp_init<kFusedGroups, kFusedRing>(sm, S, tmem_base, fr);
     int* list = s_list[warp];
     // this warp's stream: 32-pixel chunks, strided over every warp of the grid
     const int64_t nchunks = (npix + 31) / 32;
@@ -321,7 +321,7 @@ k_mlp_net(const __grid_constant__ DevScene scene, const float4* __restrict__ row
   if (ok) {
     const t3_frame& fr = scene.frame;
     const int g = threadIdx.x >> 7;
-    MlpWarp W = mlp_warp_init<kNetGroups, kNetRing>(sm, S, tmem_base);
+    MlpWarp W = mlp_warp_init<kNetGroups, kNetRing>(sm, S, tmem_base, fr);
     const uint32_t n = *nrows;  // written by k_mlp_rows, the previous kernel
     const int64_t ntiles = ((int64_t)n + 127) / 128;
     // every warp of a group walks the same tiles: no vote is needed

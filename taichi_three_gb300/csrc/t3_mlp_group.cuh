@@ -59,6 +59,7 @@ struct GroupBars {
   uint64_t empty[kMaxRing];  // MMA commit: the chunk's MMAs have read the buffer
   uint64_t hfull;            // 3 arrivals (warps 1-3): H rows written (layer input)
   uint64_t done;             // MMA commit: a layer's accumulator is complete
+  uint64_t drain;            // the leader's last commit (used once)
 };
 
 template <int G>
@@ -188,8 +189,10 @@ struct MlpWarp {
   uint32_t chunk;     // chunks of the group issued so far (ring position)
   uint32_t dph;       // parity of the next `done` completion
   uint32_t hph;       // parity of the next `hfull` completion
+  uint32_t limit;     // polls of one wait
   int row;            // this lane's row of the tile
   bool leader;        // warp 0 of the group: issues the group's MMAs
+  bool starve;        // issue nothing (tests of the timeout path)
   bool err;           // a wait ran out (warp-uniform)
 };
 
@@ -197,10 +200,11 @@ __device__ __forceinline__ uint32_t bar_full(uint32_t bars, int b) { return bars
 __device__ __forceinline__ uint32_t bar_empty(uint32_t bars, int b) { return bars + 8u * (kMaxRing + b); }
 __device__ __forceinline__ uint32_t bar_hfull(uint32_t bars) { return bars + 8u * (2 * kMaxRing); }
 __device__ __forceinline__ uint32_t bar_done(uint32_t bars) { return bars + 8u * (2 * kMaxRing + 1); }
+__device__ __forceinline__ uint32_t bar_drain(uint32_t bars) { return bars + 8u * (2 * kMaxRing + 2); }
 
 __device__ __forceinline__ void warp_wait(MlpWarp& W, uint32_t bar, uint32_t parity) {
   if (W.err) return;
-  const bool ok = mbar_wait_bounded(bar, parity, kMlpWaitLimit);
+  const bool ok = mbar_wait_bounded(bar, parity, W.limit);
   W.err = !__all_sync(0xFFFFFFFFu, ok);
 }
 
@@ -217,7 +221,7 @@ __device__ __forceinline__ void warp_handoff(MlpWarp& W, uint32_t bar, uint32_t 
     return;
   }
   warp_wait(W, bar, parity);
-  if ((threadIdx.x & 31) == 0) {
+  if ((threadIdx.x & 31) == 0 && !W.starve) {
     tc_fence_after();
     issue();
   }
@@ -328,6 +332,7 @@ __device__ __forceinline__ bool mlp_cta_begin(unsigned char* sm, MlpShared<G>& S
       }
       mbar_init(bar_hfull(bars), 3);
       mbar_init(bar_done(bars), 1);
+      mbar_init(bar_drain(bars), 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -351,7 +356,8 @@ __device__ __forceinline__ bool mlp_cta_begin(unsigned char* sm, MlpShared<G>& S
 }
 
 template <int G, int RING>
-__device__ __forceinline__ MlpWarp mlp_warp_init(unsigned char* sm, MlpShared<G>& S, uint32_t tmem_base) {
+__device__ __forceinline__ MlpWarp mlp_warp_init(unsigned char* sm, MlpShared<G>& S, uint32_t tmem_base,
+                                                 const t3_frame& fr) {
   MlpWarp W;
   const int warp = threadIdx.x >> 5, g = warp >> 2, q = warp & 3;
   W.sm = sm;
@@ -361,8 +367,10 @@ __device__ __forceinline__ MlpWarp mlp_warp_init(unsigned char* sm, MlpShared<G>
   W.chunk = 0;
   W.dph = 0;
   W.hph = 0;
+  W.limit = fr.wait_limit > 0 ? (uint32_t)fr.wait_limit : kMlpWaitLimit;
   W.row = q * 32 + (threadIdx.x & 31);
   W.leader = q == 0;
+  W.starve = (fr.flags & T3_STARVE_NETWORK) != 0;
   W.err = false;
   return W;
 }
@@ -372,11 +380,9 @@ __device__ __forceinline__ MlpWarp mlp_warp_init(unsigned char* sm, MlpShared<G>
 // ran out.
 __device__ __forceinline__ bool warp_drain(MlpWarp& W) {
   if (!W.leader) return true;
-  if ((threadIdx.x & 31) == 0) tc_commit(bar_done(W.bars));
+  if ((threadIdx.x & 31) == 0) tc_commit(bar_drain(W.bars));
   __syncwarp();
-  const bool ok = __all_sync(0xFFFFFFFFu, mbar_wait_bounded(bar_done(W.bars), W.dph, kMlpWaitLimit));
-  W.dph ^= 1u;
-  return ok;
+  return __all_sync(0xFFFFFFFFu, mbar_wait_bounded(bar_drain(W.bars), 0, kMlpWaitLimit));
 }
 
 __device__ __forceinline__ void mlp_cta_end(uint32_t tmem_base) {
