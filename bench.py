@@ -315,7 +315,8 @@ def bench_learned_ibl(flush, tc_peak):
             "roofline_mlp": {"bound": "tensor", "kernel": "k_mlp_net", "achieved": flop / (net_ms / 1e3) / 1e12,
                              "peak": tc_peak, "unit": "TFLOP/s",
                              "frac": flop / (net_ms / 1e3) / 1e12 / tc_peak,
-                             "flop_per_pixel": MLP_FLOP_PER_PIXEL, "pixels": int(len(cov))},
+                             "flop_per_pixel": MLP_FLOP_PER_PIXEL, "pixels": int(len(cov)),
+                             "traffic": traffic_of("ibl1080", "mlp_net")},
             "roofline_mlp_shading": {"bound": "tensor", "kernels": "k_mlp_rows + k_mlp_net",
                                      "achieved": flop / (shade_ms / 1e3) / 1e12, "peak": tc_peak,
                                      "unit": "TFLOP/s", "frac": flop / (shade_ms / 1e3) / 1e12 / tc_peak},
