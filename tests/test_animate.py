@@ -10,8 +10,8 @@ import taichi_three_gb300 as tina
 pytestmark = pytest.mark.gpu
 
 
-def _grid_scene():
-    scene = tina.Scene(128, 96, smoothing=True)
+def _grid_scene(raster='direct'):
+    scene = tina.Scene(128, 96, smoothing=True, raster=raster)
     grid = tina.MeshGrid(64)
     scene.add_object(grid, tina.PBR(basecolor=(0.75, 0.62, 0.5), metallic=0.3, roughness=0.35))
     scene.lighting.clear_lights()
@@ -21,9 +21,10 @@ def _grid_scene():
     return scene, grid
 
 
-def test_frame_graph_equals_eager_frames(cuda, oracle_mod):
+@pytest.mark.parametrize('raster', ['direct', 'binned'])
+def test_frame_graph_equals_eager_frames(cuda, oracle_mod, raster):
     frames = 5
-    scene, grid = _grid_scene()
+    scene, grid = _grid_scene(raster)
     eager = []
     for k in range(frames):
         grid.displace_wave(0.25 * k)
