@@ -8,6 +8,7 @@
 // No entry point allocates device memory; every buffer is caller-owned.
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "t3_internal.cuh"
 
@@ -349,6 +350,40 @@ static KeyState key_state(void* ws, unsigned long long tag) {
   return ks;
 }
 
+// Host-side record of the workspaces whose last direct frame (issued by this
+// process) ended with a shading pass that empties the keys, with that frame's
+// tag.  It only picks the size of the next frame's clear; the clear itself
+// checks the tag on the device, so a stale entry (a graph replayed out of
+// order, a workspace freed and reused) costs time, never correctness.
+struct KeyHint {
+  const void* ws;
+  unsigned long long tag;
+};
+static std::mutex g_hint_mu;
+static KeyHint g_hints[32];
+static int g_hint_next;
+
+static bool hint_empty(const void* ws, unsigned long long tag) {
+  std::lock_guard<std::mutex> lock(g_hint_mu);
+  for (const KeyHint& h : g_hints)
+    if (h.ws == ws) return h.tag == tag;
+  return false;
+}
+
+// tag 0 forgets the workspace
+static void hint_set(const void* ws, unsigned long long tag) {
+  std::lock_guard<std::mutex> lock(g_hint_mu);
+  for (KeyHint& h : g_hints) {
+    if (h.ws == ws) {
+      h.tag = tag;
+      return;
+    }
+  }
+  if (!tag) return;
+  g_hints[g_hint_next] = KeyHint{ws, tag};
+  g_hint_next = (g_hint_next + 1) % 32;
+}
+
 int64_t auto_bin_capacity(const t3_scene& sc, int tile) {
   const int64_t tx = (sc.frame.width + tile - 1) / tile, ty = (sc.frame.height + tile - 1) / tile;
   const int64_t per = 8 * total_faces(sc) / (tx * ty) + 64;
@@ -548,7 +583,9 @@ int t3_render_staged_n(const t3_scene* scene, int mode, int tile, int64_t bin_ca
     const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
     // the keys a previous frame's shading emptied are not cleared again; the
     // lamp and Monte Carlo shading passes empty them for the next frame
-    const KeyState ks = key_state(ws, key_tag(ws, L.keys, npix, L.end));
+    KeyState ks = key_state(ws, key_tag(ws, L.keys, npix, L.end));
+    ks.likely_empty = hint_empty(ws, ks.tag);
+    hint_set(ws, 0ull);
     if (e == cudaSuccess) e = launch_clear(keys, npix, st, counters, L.ncounters, status, ks);
     if (e == cudaSuccess) e = mark(1);
     size_t vtx = L.vtx;
@@ -576,7 +613,10 @@ int t3_render_staged_n(const t3_scene* scene, int mode, int tile, int64_t bin_ca
     if (e == cudaSuccess)
       e = launch_shade(ds, dsc, keys, reinterpret_cast<const float4*>(ws + L.rec), *out, status, st, ks,
                        rows_of());
+    // every shading pass of a direct frame returns the keys to empty
+    if (e == cudaSuccess) hint_set(ws, ks.tag);
   } else {
+    hint_set(ws, 0ull);
     if (e == cudaSuccess)
       e = launch_upload_scene(ds, dsc, counters, L.ncounters, status, st,
                               reinterpret_cast<unsigned long long*>(ws));
@@ -640,6 +680,7 @@ int t3_raster_fragments(const t3_scene* scene, void* workspace, size_t workspace
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(ws + L.keys);
   const int64_t npix = (int64_t)scene->frame.width * scene->frame.height;
   // a full clear (tag 0), which also marks the keys as not known to be empty
+  hint_set(ws, 0ull);
   cudaError_t e = launch_clear(keys, npix, st, counters, L.ncounters, nullptr, key_state(ws, 0ull));
   for (int o = 0; o < scene->nobjects && e == cudaSuccess; o++) {
     BigQueue big;

@@ -160,8 +160,9 @@ cudaError_t launch_clear(unsigned long long* keys, int64_t n, cudaStream_t st, u
   const int block = 256;
   int64_t want = ((n >> 1) + block - 1) / block;
   // with a key state, a grid that exits quickly when the keys are already
-  // empty (four CTAs per SM stride over the buffer when they are not)
-  const int64_t cap = ks.tag_word ? 4 * 152 : 4 * 152 * 8;
+  // empty (four CTAs per SM stride over the buffer when they are not); one
+  // block when the host expects them to be empty
+  const int64_t cap = ks.tag_word ? (ks.likely_empty ? 1 : 4 * 152) : 4 * 152 * 8;
   int64_t grid = want < cap ? want : cap;
   if (grid * block < ncounters) grid = (ncounters + block - 1) / block;
   if (grid < 1) grid = 1;

@@ -117,6 +117,10 @@ struct KeyState {
   unsigned long long* tag_word = nullptr;  // nullptr: no state kept (always clear)
   uint32_t* ticket = nullptr;              // blocks of the clear that have read the tag
   unsigned long long tag = 0;              // this frame's tag (0: never skip the clear)
+  // the host expects the tag to match (the previous frame through this
+  // workspace emptied the keys): the clear runs as one block, which still
+  // clears every key, slowly, if the tag turns out not to match
+  bool likely_empty = false;
 };
 
 int flatten_material(const t3_material& in, DevMaterial& out);

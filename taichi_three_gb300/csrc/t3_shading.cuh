@@ -21,6 +21,22 @@ __device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y *
 __device__ __forceinline__ V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
 __device__ __forceinline__ float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 __device__ __forceinline__ V3 normalized(V3 a) { return rsqrtf(dot(a, a)) * a; }
+// Approximate reciprocal, reciprocal square root and quotient for the
+// shading-only arithmetic (lamp terms, BRDF lobes, view ray, ACES), whose
+// inputs are normal numbers: the hardware approximations in their
+// flush-to-zero form, without the denormal handling of rsqrtf / __fdividef.
+__device__ __forceinline__ float rsqrt_fast(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_fast(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float div_fast(float a, float b) { return a * rcp_fast(b); }
+__device__ __forceinline__ V3 normalized_fast(V3 a) { return rsqrt_fast(dot(a, a)) * a; }
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
   return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
@@ -28,7 +44,7 @@ __device__ __forceinline__ V3 one_minus(V3 a) { return v3(1.0f - a.x, 1.0f - a.y
 __device__ __forceinline__ V3 tov(f3 a) { return v3(a.x, a.y, a.z); }
 
 __device__ __forceinline__ float aces(float c) {
-  return __fdividef(c * (2.51f * c + 0.03f), c * (2.43f * c + 0.59f) + 0.14f);
+  return div_fast(c * (2.51f * c + 0.03f), c * (2.43f * c + 0.59f) + 0.14f);
 }
 
 __device__ __forceinline__ float ipowf(float x, int n) {
@@ -178,7 +194,7 @@ __device__ __forceinline__ void eval_material(const DevMaterial& mat, const Frag
       const float kk = a2 * 0.5f;
       L.a2[k] = a2;
       L.k[k] = kk;
-      L.gnorm[k] = __fdividef(1.0f, ((NoV * kk + 1.0f) - kk) * (1.0f * (1.0f - a2) + 12.566370614359172f * a2));
+      L.gnorm[k] = div_fast(1.0f, ((NoV * kk + 1.0f) - kk) * (1.0f * (1.0f - a2) + 12.566370614359172f * a2));
       L.oma2[k] = 1.0f - a2;
       L.f0[k] = eval_value<TEX>(mat, lb.p1, fg);
     } else if (kind == T3_OP_PHONG) {
@@ -218,7 +234,7 @@ __device__ __forceinline__ void eval_material_fast(const DevObject& ob, const Fr
       const float kk = a2 * 0.5f;
       L.a2[1] = a2;
       L.k[1] = kk;
-      L.gnorm[1] = __fdividef(1.0f, ((NoV * kk + 1.0f) - kk) * (1.0f * (1.0f - a2) + 12.566370614359172f * a2));
+      L.gnorm[1] = div_fast(1.0f, ((NoV * kk + 1.0f) - kk) * (1.0f * (1.0f - a2) + 12.566370614359172f * a2));
       L.oma2[1] = 1.0f - a2;
       L.f0[1] = f;
     } else {
@@ -238,14 +254,14 @@ __device__ __forceinline__ V3 eval_brdf(const LobeState<NL>& L, V3 n, V3 ldir, V
     if (kind == T3_OP_LAMBERT) {
       acc = acc + 0.31830988618379067f * L.w[k];
     } else if (kind == T3_OP_COOK) {
-      const V3 half = normalized(ldir + vdir);
+      const V3 half = normalized_fast(ldir + vdir);
       const float NoH = fmaxf(1e-10f, dot(half, n));
       const float NoL = fmaxf(1e-10f, dot(ldir, n));
       const float VoH = fminf(1.0f, fmaxf(1e-10f, dot(half, vdir)));
       const float a2 = L.a2[k];
       const float denom = 1.0f - (NoH * NoH) * L.oma2[k];
-      const float ndf = __fdividef(a2, denom * denom);
-      const float vdf = __fdividef(L.gnorm[k], (NoL * L.k[k] + 1.0f) - L.k[k]);
+      const float ndf = div_fast(a2, denom * denom);
+      const float vdf = div_fast(L.gnorm[k], (NoL * L.k[k] + 1.0f) - L.k[k]);
       const float om = 1.0f - VoH;
       const float om2 = om * om;
       const float p5 = om * (om2 * om2);
@@ -293,15 +309,15 @@ namespace t3 {
 // calc_view_ray (shader.py:82-87): the ray through pixel centre (px, py),
 // normalize(mapply_pos(V2W, (u, +1)) - mapply_pos(V2W, (u, -1)))
 __device__ __forceinline__ V3 view_ray(const t3_frame& fr, float px, float py) {
-  const float ux = __fdividef(px, (float)fr.width) * 2.0f - 1.0f;
-  const float uy = __fdividef(py, (float)fr.height) * 2.0f - 1.0f;
+  const float ux = div_fast(px, (float)fr.width) * 2.0f - 1.0f;
+  const float uy = div_fast(py, (float)fr.height) * 2.0f - 1.0f;
   const float* M = fr.V2W;
   const float bx = M[3] + M[0] * ux + M[1] * uy, by = M[7] + M[4] * ux + M[5] * uy;
   const float bz = M[11] + M[8] * ux + M[9] * uy, bw = M[15] + M[12] * ux + M[13] * uy;
-  const float w0 = __fdividef(1.0f, bw - M[14]), w1 = __fdividef(1.0f, bw + M[14]);
+  const float w0 = rcp_fast(bw - M[14]), w1 = rcp_fast(bw + M[14]);
   const V3 ro = v3((bx - M[2]) * w0, (by - M[6]) * w0, (bz - M[10]) * w0);
   const V3 ro1 = v3((bx + M[2]) * w1, (by + M[6]) * w1, (bz + M[10]) * w1);
-  return normalized(ro1 - ro);
+  return normalized_fast(ro1 - ro);
 }
 
 // the object owning the key's face id (-1: empty pixel, or an id no object owns)
@@ -462,7 +478,7 @@ __device__ __forceinline__ V3 lamps_term(const t3_lighting& lt, const LobeState<
     const float4 ld = *reinterpret_cast<const float4*>(lt.lights[l].dir);
     V3 ldir = v3(ld.x - fg.pos.x * ld.w, ld.y - fg.pos.y * ld.w, ld.z - fg.pos.z * ld.w);
     const float d2 = dot(ldir, ldir);
-    const float inv_d = rsqrtf(d2);
+    const float inv_d = rsqrt_fast(d2);
     ldir = inv_d * ldir;
     const float cos_i = dot(fg.normal, ldir);
     if (cos_i > 0.0f) {
@@ -563,6 +579,95 @@ __device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const
   store_rgb(fr, out, g.i, color);
 }
 
+// Lamp-lit frames: this thread's four consecutive pixels [base + local0, +4).
+// Their keys are read as two 16-byte loads; four empty pixels are written as
+// background with 16-byte stores (three for the RGB triples, one each for id,
+// depth and float depth) when the output buffers allow it; the covered pixels
+// are appended to the block's list in pixel order (one shared atomic per warp).
+template <bool COHERENT>
+__device__ __forceinline__ void list_quad(const t3_frame& fr, const unsigned long long* __restrict__ keys,
+                                          const t3_outputs& out, int64_t npix, int64_t base, int local0,
+                                          V3 bg, int* s_list, int* s_count, unsigned long long* s_key,
+                                          unsigned long long* reset_keys) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i0 = base + local0;
+  unsigned long long kk[4];
+  unsigned valid = 0u;  // pixels inside the frame
+  if (i0 + 3 < npix && (reinterpret_cast<uintptr_t>(keys + i0) & 15) == 0) {
+    const ulonglong2* k2 = reinterpret_cast<const ulonglong2*>(keys + i0);
+    const ulonglong2 a = COHERENT ? __ldcg(k2) : k2[0];
+    const ulonglong2 b = COHERENT ? __ldcg(k2 + 1) : k2[1];
+    kk[0] = a.x; kk[1] = a.y; kk[2] = b.x; kk[3] = b.y;
+    valid = 15u;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      kk[j] = T3_EMPTY_KEY;
+      if (i0 + j < npix) {
+        kk[j] = COHERENT ? __ldcg(keys + i0 + j) : keys[i0 + j];
+        valid |= 1u << j;
+      }
+    }
+  }
+  unsigned covered = 0u;
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    if (kk[j] != T3_EMPTY_KEY) covered |= 1u << j;
+  // protocol frames that select pixels write empty ones only with T3_SHADE_EMPTY
+  if (!(fr.flags & T3_SHADE_OWNED) || (fr.flags & T3_SHADE_EMPTY)) {
+    const uintptr_t align = reinterpret_cast<uintptr_t>(out.rgb) | reinterpret_cast<uintptr_t>(out.face_id) |
+                            reinterpret_cast<uintptr_t>(out.depth) | reinterpret_cast<uintptr_t>(out.depth_f);
+    if (covered == 0u && valid == 15u && (align & 15) == 0) {
+      if (out.rgb) {
+        float4* r4 = reinterpret_cast<float4*>(out.rgb + 3 * i0);
+        r4[0] = make_float4(bg.x, bg.y, bg.z, bg.x);
+        r4[1] = make_float4(bg.y, bg.z, bg.x, bg.y);
+        r4[2] = make_float4(bg.z, bg.x, bg.y, bg.z);
+      }
+      if (out.face_id) *reinterpret_cast<int4*>(out.face_id + i0) = make_int4(-1, -1, -1, -1);
+      if (out.depth) {
+        const int32_t d = fr.maxdepth;
+        *reinterpret_cast<int4*>(out.depth + i0) = make_int4(d, d, d, d);
+      }
+      if (out.depth_f) {
+        const float inf = __int_as_float(0x7f800000);
+        *reinterpret_cast<float4*>(out.depth_f + i0) = make_float4(inf, inf, inf, inf);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if ((valid >> j & 1u) && !(covered >> j & 1u)) write_empty(fr, out, i0 + j, bg);
+    }
+  }
+  if (reset_keys && covered) {
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (covered >> j & 1u) reset_keys[i0 + j] = T3_EMPTY_KEY;
+  }
+  // the warp's covered pixels, in pixel order, after one shared atomic
+  const int cnt = __popc(covered);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  if (total == 0) return;
+  int slot = 0;
+  if (lane == 31) slot = atomicAdd(s_count, total);
+  slot = __shfl_sync(0xFFFFFFFFu, slot, 31);
+  int at = slot + incl - cnt;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    if (covered >> j & 1u) {
+      s_list[at] = local0 + j;
+      s_key[at] = kk[j];
+      at++;
+    }
+  }
+}
+
 // One block's share of the shading pass: pixels [base, base + BLOCK * PPT) of
 // the frame.  Empty pixels are written as background at once; covered ones are
 // compacted into a shared list (warp ballot + one shared atomic per warp), with
@@ -581,32 +686,39 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
   const int H = fr.height;
   const V3 bg = background(fr);
   const int lane = threadIdx.x & 31;
+  if constexpr (MODE == T3_LIGHT_LAMPS && PPT % 4 == 0) {
 #pragma unroll
-  for (int k = 0; k < PPT; k++) {
-    const int local = k * BLOCK + threadIdx.x;
-    const int64_t i = base + local;
-    bool covered = false;
-    unsigned long long key = T3_EMPTY_KEY;
-    if (i < npix) {
-      // with IBL, empty pixels show the sky and go through the shading list too
-      key = COHERENT ? __ldcg(keys + i) : keys[i];
-      if (MODE == T3_LIGHT_LAMPS && key == T3_EMPTY_KEY) {
-        // protocol frames that select pixels write empty ones only with T3_SHADE_EMPTY
-        if (!(fr.flags & T3_SHADE_OWNED) || (fr.flags & T3_SHADE_EMPTY)) write_empty(fr, out, i, bg);
-      } else {
-        covered = true;
+    for (int k = 0; k < PPT / 4; k++)
+      list_quad<COHERENT>(fr, keys, out, npix, base, 4 * (k * BLOCK + threadIdx.x), bg, s_list, s_count,
+                          s_key, reset_keys);
+  } else {
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const int local = k * BLOCK + threadIdx.x;
+      const int64_t i = base + local;
+      bool covered = false;
+      unsigned long long key = T3_EMPTY_KEY;
+      if (i < npix) {
+        // with IBL, empty pixels show the sky and go through the shading list too
+        key = COHERENT ? __ldcg(keys + i) : keys[i];
+        if (MODE == T3_LIGHT_LAMPS && key == T3_EMPTY_KEY) {
+          // protocol frames that select pixels write empty ones only with T3_SHADE_EMPTY
+          if (!(fr.flags & T3_SHADE_OWNED) || (fr.flags & T3_SHADE_EMPTY)) write_empty(fr, out, i, bg);
+        } else {
+          covered = true;
+        }
+        if (key != T3_EMPTY_KEY && reset_keys) reset_keys[i] = T3_EMPTY_KEY;
       }
-      if (key != T3_EMPTY_KEY && reset_keys) reset_keys[i] = T3_EMPTY_KEY;
-    }
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
-    if (m) {
-      int slot = 0;
-      if (lane == 0) slot = atomicAdd(s_count, __popc(m));
-      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-      if (covered) {
-        const int at = slot + __popc(m & ((1u << lane) - 1u));
-        s_list[at] = local;
-        s_key[at] = key;
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, covered);
+      if (m) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(s_count, __popc(m));
+        slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+        if (covered) {
+          const int at = slot + __popc(m & ((1u << lane) - 1u));
+          s_list[at] = local;
+          s_key[at] = key;
+        }
       }
     }
   }
