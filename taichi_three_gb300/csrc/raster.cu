@@ -116,41 +116,66 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
                     fr.width - 1, 0, fr.height - 1, fr, sink);
 }
 
-// Large faces: every CTA walks a slice of every queued face's bbox.
+// Large faces: every CTA walks a slice of every queued face's bbox.  The
+// queued faces' setups are read 32 at a time into shared memory (one round
+// of loads for the chunk instead of a dependent load chain per face).
 template <int BLOCK, bool COUNT>
 __global__ void __launch_bounds__(BLOCK)
 k_raster_big(const t3_frame fr, const t3_mesh mesh, uint32_t face_base,
              unsigned long long* __restrict__ keys, BigQueue big) {
+  constexpr int kChunk = 32;
+  __shared__ Setup s_face[kChunk];
+  __shared__ uint32_t s_id[kChunk];
   const uint32_t count = min(*big.count, big.capacity);
   const float maxd = (float)fr.maxdepth;
   GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
   const int64_t stride = (int64_t)gridDim.x * BLOCK;
-  for (uint32_t e = 0; e < count; e++) {
-    const uint32_t n = big.items[e];
-    Setup s;
-    if (big.rec) {
-      // the setup record k_raster_direct stored for the face
-      load_record(big.rec, face_base + n, s);
-    } else {
-      f3 v[3];
-      face_verts(mesh, face_ref(mesh, n), v);
-      if (!face_setup(fr, v, s)) continue;
+  for (uint32_t e0 = 0; e0 < count; e0 += kChunk) {
+    const uint32_t m = min((uint32_t)kChunk, count - e0);
+    __syncthreads();  // the previous chunk's faces are walked
+    if (threadIdx.x < m) {
+      const uint32_t n = big.items[e0 + threadIdx.x];
+      Setup s;
+      if (big.rec) {
+        // the setup record k_raster_direct stored for the face
+        load_record(big.rec, face_base + n, s);
+      } else {
+        f3 v[3];
+        face_verts(mesh, face_ref(mesh, n), v);
+        if (!face_setup(fr, v, s)) s.topx = s.botx - 1;  // nothing to walk
+      }
+      s_face[threadIdx.x] = s;
+      s_id[threadIdx.x] = face_base + n;
     }
-    const int32_t h = s.topy - s.boty + 1;
-    const int64_t area = (int64_t)(s.topx - s.botx + 1) * h;
-    const uint32_t id = face_base + n;
-    for (int64_t k = (int64_t)blockIdx.x * BLOCK + threadIdx.x; k < area; k += stride) {
-      const int32_t x = s.botx + (int32_t)(k / h);
-      const int32_t y = s.boty + (int32_t)(k - (k / h) * h);
-      const float px = xadd((float)x, fr.bias[0]);
-      const float py = xadd((float)y, fr.bias[1]);
-      float wx, wy, wz, sum;
-      face_raw_weights(s, px, py, wx, wy, wz, sum);
-      f3 wei;
-      if (!face_inside(wx, wy, wz, sum, wei)) continue;
-      const int32_t d = trunc_i32(xmul(face_depth(s, wei), maxd));
-      if (d >= fr.maxdepth) continue;
-      sink(x, y, pack_key(d, id));
+    __syncthreads();
+    for (uint32_t e = 0; e < m; e++) {
+      const Setup& s = s_face[e];
+      if (s.topx < s.botx || s.topy < s.boty) continue;
+      const int32_t h = s.topy - s.boty + 1;
+      const int64_t area = (int64_t)(s.topx - s.botx + 1) * h;
+      const uint32_t id = s_id[e];
+      for (int64_t k = (int64_t)blockIdx.x * BLOCK + threadIdx.x; k < area; k += stride) {
+        // bboxes are clamped to the frame (at most 65535 rows), so the
+        // column / row split fits 32-bit arithmetic when the area does
+        int32_t q, r;
+        if (area <= INT32_MAX) {
+          q = (int32_t)k / h;
+          r = (int32_t)k - q * h;
+        } else {
+          q = (int32_t)(k / h);
+          r = (int32_t)(k - (int64_t)q * h);
+        }
+        const int32_t x = s.botx + q, y = s.boty + r;
+        const float px = xadd((float)x, fr.bias[0]);
+        const float py = xadd((float)y, fr.bias[1]);
+        float wx, wy, wz, sum;
+        face_raw_weights(s, px, py, wx, wy, wz, sum);
+        f3 wei;
+        if (!face_inside(wx, wy, wz, sum, wei)) continue;
+        const int32_t d = trunc_i32(xmul(face_depth(s, wei), maxd));
+        if (d >= fr.maxdepth) continue;
+        sink(x, y, pack_key(d, id));
+      }
     }
   }
 }
