@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_batch_raster(const __grid_co
   }
 }
 
-template <int NL, bool TEX, int SIG>
+template <int NL, bool TEX, int SIG, bool PLAIN = false>
 __global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_constant__ BatchArgs a) {
   __shared__ int s_list[kBatchBlock * kBatchPPT];
   __shared__ unsigned long long s_key[kBatchBlock * kBatchPPT];
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_batch_shade(const __grid_con
     const BatchView& v = a.v[s];
     const int64_t base = (int64_t)(gs - v.shade_item0) * a.pixels_per_item;
     for (int64_t p0 = base; p0 < base + a.pixels_per_item && p0 < v.npix; p0 += kBatchBlock * kBatchPPT) {
-      shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS, false, TEX, SIG>(v.sc, v.keys, v.rec, v.out,
+      shade_block<kBatchBlock, kBatchPPT, NL, T3_LIGHT_LAMPS, false, TEX, SIG, PLAIN>(v.sc, v.keys, v.rec, v.out,
                                                                                 v.npix, p0, s_list, &s_count,
                                                                                 s_key);
       __syncthreads();
@@ -264,7 +264,7 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   a.pixels_per_item = c.pixels_per_item;
   a.queue = reinterpret_cast<uint32_t*>(ws + L.counters);
   int nl = 1, sig = -1, fsig = -1;
-  bool textured = false;
+  bool textured = false, plain = true;
   uint32_t item = 0;
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < nscenes && e == cudaSuccess; s++) {
@@ -278,6 +278,7 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
     sig = sig < 0 || sig == ssig ? ssig : 0;
     const int sfast = fast_signature(ds);
     fsig = fsig < 0 || fsig == sfast ? sfast : 0;
+    plain = plain && plain_soups(ds);
     DevScene* dst = reinterpret_cast<DevScene*>(ws + L.scenes + align256b(sizeof(DevScene)) * (size_t)s);
     // the first upload also zeroes the queue counters and the status
     e = launch_upload_scene(ds, dst, s == 0 ? a.queue : nullptr, s == 0 ? 2 : 0, s == 0 ? status : nullptr,
@@ -324,9 +325,15 @@ int t3_render_batch(const t3_scene* scenes, const t3_outputs* outs, int nscenes,
   // untextured signature, texture nodes compiled in only when a view has one
   const void* shade_fn;
   constexpr int F = T3_SIG_FAST;
-  if (!textured && fsig == T3_SIG_PBR) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_PBR | F>;
-  else if (!textured && fsig == T3_SIG_CLASSIC) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC | F>;
-  else if (!textured && fsig == T3_SIG_DIFFUSE) shade_fn = (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE | F>;
+  if (!textured && fsig == T3_SIG_PBR)
+    shade_fn = plain ? (const void*)k_batch_shade<2, false, T3_SIG_PBR | F, true>
+                     : (const void*)k_batch_shade<2, false, T3_SIG_PBR | F>;
+  else if (!textured && fsig == T3_SIG_CLASSIC)
+    shade_fn = plain ? (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC | F, true>
+                     : (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC | F>;
+  else if (!textured && fsig == T3_SIG_DIFFUSE)
+    shade_fn = plain ? (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE | F, true>
+                     : (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE | F>;
   else if (!textured && sig == T3_SIG_PBR) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_PBR>;
   else if (!textured && sig == T3_SIG_CLASSIC) shade_fn = (const void*)k_batch_shade<2, false, T3_SIG_CLASSIC>;
   else if (!textured && sig == T3_SIG_DIFFUSE) shade_fn = (const void*)k_batch_shade<1, false, T3_SIG_DIFFUSE>;

@@ -43,7 +43,7 @@ cudaError_t launch_upload_scene(const DevScene& sc, DevScene* dst, uint32_t* cou
 // descriptor is a __grid_constant__ kernel parameter: lamps, materials and
 // camera are read through the constant cache (warp-uniform broadcasts), not
 // as per-pixel global loads.
-template <int BLOCK, int PPT, int NL, int MODE, bool TEX, int SIG>
+template <int BLOCK, int PPT, int NL, int MODE, bool TEX, int SIG, bool PLAIN = false>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_shade(const __grid_constant__ DevScene sc, const unsigned long long* __restrict__ keys,
         const float4* __restrict__ rec, t3_outputs out, int64_t npix, KeyState reset) {
@@ -54,7 +54,7 @@ k_shade(const __grid_constant__ DevScene sc, const unsigned long long* __restric
   // the keys are empty once every block has run: mark them so for the next frame
   if (reset.tag_word && blockIdx.x == 0 && threadIdx.x == 0) *reset.tag_word = reset.tag;
   __syncthreads();
-  shade_block<BLOCK, PPT, NL, MODE, false, TEX, SIG>(
+  shade_block<BLOCK, PPT, NL, MODE, false, TEX, SIG, PLAIN>(
       &sc, keys, rec, out, npix, (int64_t)blockIdx.x * BLOCK * PPT, s_list, &s_count, s_key,
       reset.tag_word ? const_cast<unsigned long long*>(keys) : nullptr);
 }
@@ -75,6 +75,17 @@ int lobe_signature(const DevScene& sc) {
   return sig == T3_SIG_PBR || sig == T3_SIG_CLASSIC || sig == T3_SIG_DIFFUSE ? sig : 0;
 }
 
+bool plain_soups(const DevScene& sc) {
+  constexpr uint32_t edits = T3_MESH_TRANSFORM | T3_MESH_NOCULL | T3_MESH_FLIP_ORDER | T3_MESH_FLIP_NORMAL |
+                             T3_MESH_FLAT_NORMAL | T3_MESH_WIREFRAME | T3_MESH_QUADS;
+  for (int o = 0; o < sc.nobjects; o++) {
+    const t3_mesh& m = sc.obj[o].mesh;
+    if (m.kind != T3_MESH_SOUP || (m.flags & edits)) return false;
+    if ((sc.frame.flags & T3_SMOOTHING) && !m.norms) return false;
+  }
+  return sc.nobjects > 0;
+}
+
 int fast_signature(const DevScene& sc) {
   int sig = -1;
   for (int o = 0; o < sc.nobjects; o++) {
@@ -86,22 +97,30 @@ int fast_signature(const DevScene& sc) {
   return sig > 0 ? sig : 0;
 }
 
-template <int NL, int MODE, bool TEX, int SIG = 0>
+template <int NL, int MODE, bool TEX, int SIG = 0, bool PLAIN = false>
 static void launch_shade_t(const DevScene& sc, const unsigned long long* keys, const float4* rec,
                            const t3_outputs& out, int64_t npix, cudaStream_t st, const KeyState& ks) {
   constexpr int BLOCK = 256, PPT = 4;
   const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
   if constexpr (MODE == T3_LIGHT_LAMPS && !TEX && SIG == 0) {
-    // untextured lamp scenes with one common material shape, or else one
+    // untextured lamp scenes with one common material shape (on plain soups,
+    // an instance whose geometry path is compiled for them), or else one
     // common lobe signature
     const int fsig = fast_signature(sc);
+    const bool plain = plain_soups(sc);
     constexpr int F = T3_SIG_FAST;
-    if (NL == 2 && fsig == T3_SIG_PBR)
+    if (NL == 2 && fsig == T3_SIG_PBR) {
+      if (plain) return launch_shade_t<2, MODE, TEX, T3_SIG_PBR | F, true>(sc, keys, rec, out, npix, st, ks);
       return launch_shade_t<2, MODE, TEX, T3_SIG_PBR | F>(sc, keys, rec, out, npix, st, ks);
-    if (NL == 2 && fsig == T3_SIG_CLASSIC)
+    }
+    if (NL == 2 && fsig == T3_SIG_CLASSIC) {
+      if (plain) return launch_shade_t<2, MODE, TEX, T3_SIG_CLASSIC | F, true>(sc, keys, rec, out, npix, st, ks);
       return launch_shade_t<2, MODE, TEX, T3_SIG_CLASSIC | F>(sc, keys, rec, out, npix, st, ks);
-    if (NL == 1 && fsig == T3_SIG_DIFFUSE)
+    }
+    if (NL == 1 && fsig == T3_SIG_DIFFUSE) {
+      if (plain) return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE | F, true>(sc, keys, rec, out, npix, st, ks);
       return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE | F>(sc, keys, rec, out, npix, st, ks);
+    }
     const int sig = lobe_signature(sc);
     if (NL == 2 && sig == T3_SIG_PBR) return launch_shade_t<2, MODE, TEX, T3_SIG_PBR>(sc, keys, rec, out, npix, st, ks);
     if (NL == 2 && sig == T3_SIG_CLASSIC)
@@ -109,7 +128,7 @@ static void launch_shade_t(const DevScene& sc, const unsigned long long* keys, c
     if (NL == 1 && sig == T3_SIG_DIFFUSE)
       return launch_shade_t<1, MODE, TEX, T3_SIG_DIFFUSE>(sc, keys, rec, out, npix, st, ks);
   }
-  k_shade<BLOCK, PPT, NL, MODE, TEX, SIG><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix, ks);
+  k_shade<BLOCK, PPT, NL, MODE, TEX, SIG, PLAIN><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix, ks);
 }
 
 template <int MODE, bool TEX>

@@ -127,6 +127,13 @@ __device__ __forceinline__ FaceRef face_ref(const t3_mesh& d, int64_t n) {
   return r;
 }
 
+// the three corners of face n of a face soup's position or normal array
+__device__ __forceinline__ void soup_corners(const float* arr, int64_t n, f3 v[3]) {
+  const float* p = arr + n * 9;
+#pragma unroll
+  for (int k = 0; k < 3; k++) v[k] = ld3(p + 3 * k);
+}
+
 __device__ __forceinline__ void base_verts(const t3_mesh& d, int64_t f, f3 v[3]) {
 #pragma unroll
   for (int k = 0; k < 3; k++) {

@@ -178,6 +178,9 @@ int max_lobes(const DevScene& sc);
 void find_fast_material(const DevMaterial& m, FastMat& fast);
 // the shape shared by every shaded object of the scene, or 0
 int fast_signature(const DevScene& sc);
+// every object is a face soup without mesh edits (and with normals when the
+// frame smooths): the shading instances that compile the other geometry out
+bool plain_soups(const DevScene& sc);
 // the lobe kinds (one byte per slot) shared by every shaded object of the
 // scene when a specialised shading instance exists for them, else 0
 int lobe_signature(const DevScene& sc);

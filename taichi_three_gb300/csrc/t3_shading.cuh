@@ -348,8 +348,11 @@ struct PixelGeom {
 // an empty pixel.  `rec` (nullable) holds the rasteriser's setup records
 // (64 bytes per face id); without it the face setup is recomputed,
 // bit-identically.  COHERENT_REC: the records were written by the same kernel
-// launch (read through L2, not the read-only path).
-template <bool COHERENT_REC = false>
+// launch (read through L2, not the read-only path).  PLAIN: every object of
+// the frame is a face soup without mesh edits (plain_soups), so the line,
+// particle, transform and corner-order paths are compiled out (fewer
+// registers and instructions, the same values).
+template <bool COHERENT_REC = false, bool PLAIN = false>
 __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
                                                const float4* __restrict__ rec,
                                                unsigned long long key, int x, int y,
@@ -371,7 +374,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   g.ob = &ob;
   const t3_mesh& mesh = ob.mesh;
   const int64_t n = (int64_t)gid - ob.face_base;
-  if (is_wire(mesh)) {
+  if (!PLAIN && is_wire(mesh)) {
     // WireframeRaster: the raster's line colour, blended with factor 1 by
     // Shader.blend_color (wireframe.py:93-97, shader.py:133-135)
     const int32_t d = (int32_t)((uint32_t)(key >> 32) ^ 0x80000000u);
@@ -382,7 +385,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
     g.fg.color = v3(fr.linecolor[0], fr.linecolor[1], fr.linecolor[2]);
     return true;
   }
-  if (mesh.kind == T3_MESH_PARTICLES) {
+  if (!PLAIN && mesh.kind == T3_MESH_PARTICLES) {
     // ParticleRaster.render_color (particle.py:116-146)
     const f3 A = ld3(mesh.verts + n * 3);
     const float Rl = __ldg(mesh.coors + n);
@@ -406,7 +409,7 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
     g.vdir = v3(-rd.x, -rd.y, -rd.z);
     return true;
   }
-  const FaceRef ref = face_ref(mesh, n);
+  const FaceRef ref = PLAIN ? FaceRef{n, false, false} : face_ref(mesh, n);
   // start every gather of this face now: normals and material attributes are
   // needed only after the weights, but their DRAM latency overlaps from here
   if ((fr.flags & T3_SMOOTHING) && mesh.norms && !(mesh.flags & T3_MESH_FLAT_NORMAL)) {
@@ -417,7 +420,8 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   if (mesh.face_attr)
     asm volatile("prefetch.global.L1 [%0];" :: "l"(mesh.face_attr + ref.f * mesh.attr_stride));
   f3 v[3];
-  face_verts(mesh, ref, v);
+  if constexpr (PLAIN) soup_corners(mesh.verts, n, v);
+  else face_verts(mesh, ref, v);
   Setup s;
   if (rec) {
     const float4* r = rec + (size_t)gid * 4;
@@ -448,7 +452,8 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   V3 nrm;
   if (fr.flags & T3_SMOOTHING) {
     f3 nn[3];
-    face_norms(mesh, ref, nn);
+    if constexpr (PLAIN) soup_corners(mesh.norms, n, nn);
+    else face_norms(mesh, ref, nn);
     nrm = (wei.x * tov(nn[0]) + wei.y * tov(nn[1])) + wei.z * tov(nn[2]);
   } else {
     nrm = cross(B - A, C - A);
@@ -507,7 +512,7 @@ __device__ __forceinline__ void shade_lit(const DevScene* __restrict__ sc, const
 
 // Shades pixel (x, y) from its packed (depth, id) key and writes every output.
 // MODE is the lighting (T3_LIGHT_LAMPS or T3_LIGHT_IBL_MC).
-template <int NL, int MODE, bool COHERENT_REC = false, bool TEX = true, int SIG = 0>
+template <int NL, int MODE, bool COHERENT_REC = false, bool TEX = true, int SIG = 0, bool PLAIN = false>
 __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict__ sc,
                                                      const float4* __restrict__ rec,
                                                      unsigned long long key, int x, int y,
@@ -520,7 +525,7 @@ __device__ __forceinline__ void shade_pixel_from_key(const DevScene* __restrict_
     const bool empty = key == T3_EMPTY_KEY;
     if (empty ? !(sel & T3_SHADE_EMPTY) : (!(sel & T3_SHADE_OWNED) || key_owner(sc, key) < 0)) return;
   }
-  if (!pixel_geometry<COHERENT_REC>(sc, rec, key, x, y, out, g)) {
+  if (!pixel_geometry<COHERENT_REC, PLAIN>(sc, rec, key, x, y, out, g)) {
     V3 bg = v3(fr.bgcolor[0], fr.bgcolor[1], fr.bgcolor[2]);
     if (MODE != T3_LIGHT_LAMPS) {
       // Engine.render_background (engine.py:42-49): the sky along the view ray
@@ -675,7 +680,8 @@ __device__ __forceinline__ void list_quad(const t3_frame& fr, const unsigned lon
 // BLOCK * PPT entries; s_count must be zero on entry and is left non-zero
 // (callers reset it after a barrier).  reset_keys (nullable): the frame's key
 // buffer, whose keys this block returns to empty as it reads them.
-template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false, bool TEX = true, int SIG = 0>
+template <int BLOCK, int PPT, int NL, int MODE, bool COHERENT = false, bool TEX = true, int SIG = 0,
+          bool PLAIN = false>
 __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
                                             const unsigned long long* __restrict__ keys,
                                             const float4* __restrict__ rec, const t3_outputs& out,
@@ -727,7 +733,7 @@ __device__ __forceinline__ void shade_block(const DevScene* __restrict__ sc,
   for (int j = threadIdx.x; j < n; j += BLOCK) {
     const int64_t i = base + s_list[j];
     const int x = (int)(i / H), y = (int)(i - (int64_t)x * H);
-    shade_pixel_from_key<NL, MODE, COHERENT, TEX, SIG>(sc, rec, s_key[j], x, y, out);
+    shade_pixel_from_key<NL, MODE, COHERENT, TEX, SIG, PLAIN>(sc, rec, s_key[j], x, y, out);
   }
 }
 
