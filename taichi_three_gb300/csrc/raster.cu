@@ -111,9 +111,14 @@ k_raster_direct(const t3_frame fr, const t3_mesh mesh, int64_t nfaces, uint32_t 
       vis = false;
     }
   }
+  // the staged positions are read: each warp's 1,152 bytes of them hold its
+  // faces' column constants from here on
+  static_assert(sizeof(ColConsts) * 32 <= 32 * 9 * sizeof(float), "column constants outgrow the staging area");
+  __syncthreads();
+  ColConsts* cc = reinterpret_cast<ColConsts*>(sv + (threadIdx.x >> 5) * 32 * 9);
   GlobalKeySink<COUNT> sink{keys, fr.height, big.fragments};
   warp_raster_spans(wfs[threadIdx.x >> 5], wcs[threadIdx.x >> 5], s, vis, face_base + (uint32_t)n, 0,
-                    fr.width - 1, 0, fr.height - 1, fr, sink);
+                    fr.width - 1, 0, fr.height - 1, fr, sink, cc);
 }
 
 // Large faces: every CTA walks a slice of every queued face's bbox.  The

@@ -191,12 +191,78 @@ __device__ __forceinline__ void column_rows(const Setup& t, int x, int y0, int y
   }
 }
 
+// column_rows split in two: the per-face part (column_consts, once by the
+// face's own lane) and the per-column part (column_rows_c), with the same
+// bounds up to the order of N's sum and the approximate reciprocal of the
+// edge slopes, both far inside the margin's 2^-18 factor.
+struct ColConsts {
+  float4 a;  // S (NaN: the face's columns get no bounds), H = hb + hc + |by| + |cy| + 2,
+             // by * bcnx, cy * canx
+  float4 b;  // 1 / k of the edges bc, ca, ab (0: the edge gives no bound), unused
+};
+
+__device__ __forceinline__ ColConsts column_consts(const Setup& t, int y0, int y1, float biasy) {
+  const bool ok = t.wsa > 0.0f && t.wsb > 0.0f && t.wsc > 0.0f && t.wsa < INFINITY && t.wsb < INFINITY &&
+                  t.wsc < INFINITY;
+  float S = fabsf(t.bcnx) + fabsf(t.bcny) + fabsf(t.canx) + fabsf(t.cany);
+  if (!ok || !(S < INFINITY)) S = __int_as_float(0x7fffffff);
+  const float ya = (float)y0 + biasy, yb = (float)y1 + biasy;
+  const float hb = fmaxf(fabsf(ya - t.by), fabsf(yb - t.by)), hc = fmaxf(fabsf(ya - t.cy), fabsf(yb - t.cy));
+  const float ks[3] = {-t.bcnx, -t.canx, t.bcnx + t.canx};
+  float ik[3];
+#pragma unroll
+  for (int e = 0; e < 3; e++)  // a slope nearly constant along the column gives no bound
+    ik[e] = fabsf(ks[e]) * 1048576.0f > S ? __fdividef(1.0f, ks[e]) : 0.0f;
+  ColConsts c;
+  c.a = make_float4(S, hb + hc + fabsf(t.by) + fabsf(t.cy) + 2.0f, t.by * t.bcnx, t.cy * t.canx);
+  c.b = make_float4(ik[0], ik[1], ik[2], 0.0f);
+  return c;
+}
+
+// column_rows from the face's corners b, c, its coefficients bcn.y and can.y
+// and its column_consts
+__device__ __forceinline__ void column_rows_c(float bx, float cx, float bcny, float cany, const ColConsts& c,
+                                              int x, int y0, int y1, float biasx, float biasy, int& lo,
+                                              int& hi) {
+  lo = y0;
+  hi = y1;
+  const float S = c.a.x;
+  if (!(S < INFINITY)) return;  // also NaN
+  const float px = xadd((float)x, biasx);
+  const float dbx = fabsf(px - bx), dcx = fabsf(px - cx);
+  const float N = 2.0f * ((dbx + dcx) + c.a.y) * S + 4.0f;
+  const float A1 = (px - bx) * bcny + c.a.z;
+  const float A2 = (px - cx) * cany + c.a.w;
+  const float A3 = 1.0f - A1 - A2;
+  const float As[3] = {A1, A2, A3}, iks[3] = {c.b.x, c.b.y, c.b.z};
+  const float flo = (float)y0 - 1.0f, fhi = (float)y1 + 1.0f;
+#pragma unroll
+  for (int e = 0; e < 3; e++) {
+    const float ik = iks[e];
+    if (ik == 0.0f) continue;
+    const float B = -As[e] * ik;
+    const float m = 3.814697265625e-06f * (N * fabsf(ik) + fabsf(B)) + 9.5367431640625e-07f;
+    if (!(fabsf(B) < 1e30f) || !(m < 1e30f)) continue;
+    if (ik > 0.0f) {
+      const float b = fminf(fmaxf(B - m - biasy, flo), fhi);
+      const int r = (int)ceilf(b);
+      lo = r > lo ? r : lo;
+    } else {
+      const float b = fminf(fmaxf(B + m - biasy, flo), fhi);
+      const int r = (int)floorf(b);
+      hi = r < hi ? r : hi;
+    }
+  }
+}
+
 // warp_raster over column spans: same interface and result; warps whose faces
 // have more than kMaxWarpCols columns in total take the bbox walk.
+// cc (nullable, 32 entries, the warp's own): the faces' column_consts are
+// stored there once and the columns read them instead of recomputing them.
 template <class Sink>
 __device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, const Setup& s, bool active,
                                                   uint32_t id, int cx0, int cx1, int cy0, int cy1,
-                                                  const t3_frame& fr, Sink sink) {
+                                                  const t3_frame& fr, Sink sink, ColConsts* cc = nullptr) {
   const unsigned FULL = 0xFFFFFFFFu;
   const int lane = threadIdx.x & 31;
   const int x0 = max(s.botx, cx0), x1 = min(s.topx, cx1);
@@ -229,6 +295,7 @@ __device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, c
     wf.rec[r][3] = make_float4(s.Bz, s.Cz, __int_as_float(x0 | (y0 << 16)), __uint_as_float(id));
     wf.h[r] = y1 - y0 + 1;
     wf.start[r] = first;
+    if (cc) cc[r] = column_consts(s, y0, y1, fr.bias[1]);
   }
   const unsigned upto = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
   const unsigned below = (1u << lane) - 1u;
@@ -244,16 +311,21 @@ __device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, c
     int cnt = 0, rlo = 0, x = 0, j = 0;
     if (ci < total) {
       j = before + __popc(starts & upto) - 1;
-      const float4 r0 = wf.rec[j][0], r1 = wf.rec[j][1], r2 = wf.rec[j][2];
       const int xy = __float_as_int(wf.rec[j][3].z);
-      Setup t;
-      t.bx = r0.x; t.by = r0.y; t.cx = r0.z; t.cy = r0.w;
-      t.bcnx = r1.x; t.bcny = r1.y; t.canx = r1.z; t.cany = r1.w;
-      t.wsa = r2.x; t.wsb = r2.y; t.wsc = r2.z;
       x = (xy & 0xFFFF) + (ci - wf.start[j]);
       const int fy0 = xy >> 16;
       int rhi;
-      column_rows(t, x, fy0, fy0 + wf.h[j] - 1, biasx, biasy, rlo, rhi);
+      if (cc) {
+        const float4 r0 = wf.rec[j][0], r1 = wf.rec[j][1];
+        column_rows_c(r0.x, r0.z, r1.y, r1.w, cc[j], x, fy0, fy0 + wf.h[j] - 1, biasx, biasy, rlo, rhi);
+      } else {
+        const float4 r0 = wf.rec[j][0], r1 = wf.rec[j][1], r2 = wf.rec[j][2];
+        Setup t;
+        t.bx = r0.x; t.by = r0.y; t.cx = r0.z; t.cy = r0.w;
+        t.bcnx = r1.x; t.bcny = r1.y; t.canx = r1.z; t.cany = r1.w;
+        t.wsa = r2.x; t.wsb = r2.y; t.wsc = r2.z;
+        column_rows(t, x, fy0, fy0 + wf.h[j] - 1, biasx, biasy, rlo, rhi);
+      }
       cnt = rhi >= rlo ? rhi - rlo + 1 : 0;
     }
     const unsigned m = __ballot_sync(FULL, cnt > 0);

@@ -199,8 +199,9 @@ def _trimmed(lo, hi, T):
 
 
 def _column_rows(t, x, y0, y1):
-    """Candidate rows [lo, hi] of column x (t3_raster.cuh column_rows) in
-    float32, with exact divisions where the kernel divides approximately (the
+    """Candidate rows [lo, hi] of column x (t3_raster.cuh column_consts and
+    column_rows_c, as k_raster_direct runs them) in float32, with exact
+    divisions where the kernel divides or takes reciprocals approximately (the
     margin's 2^-18 |B| term covers the difference)."""
     f32 = np.float32
     lo, hi = y0, y1
@@ -213,7 +214,8 @@ def _column_rows(t, x, y0, y1):
     dbx, dcx = abs(f32(px - t['bx'])), abs(f32(px - t['cx']))
     hb = max(abs(f32(ya - t['by'])), abs(f32(yb - t['by'])))
     hc = max(abs(f32(ya - t['cy'])), abs(f32(yb - t['cy'])))
-    N = f32(f32(2) * f32(dbx + dcx + hb + hc + abs(t['by']) + abs(t['cy']) + f32(2)) * S + f32(4))
+    H = f32(hb + hc + abs(t['by']) + abs(t['cy']) + f32(2))
+    N = f32(f32(f32(2) * f32(f32(dbx + dcx) + H)) * S + f32(4))
     A1 = f32(f32(f32(px - t['bx']) * t['bcny']) + f32(t['by'] * t['bcnx']))
     A2 = f32(f32(f32(px - t['cx']) * t['cany']) + f32(t['cy'] * t['canx']))
     A3 = f32(f32(f32(1) - A1) - A2)
