@@ -212,7 +212,7 @@ k_shade_mlp(const __grid_constant__ DevScene scene, const unsigned long long* __
 //   [4] c2.z base.xyz   [5] pixel index (int bits), 0, 0, 0
 constexpr int kRowVec = 6;
 
-template <int BLOCK, int PPT, int NL, bool TEX, int SIG, bool PLAIN = false>
+template <int BLOCK, int PPT, int NL, bool TEX, int SIG>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_mlp_rows(const __grid_constant__ DevScene scene, const unsigned long long* __restrict__ keys,
            const float4* __restrict__ rec, t3_outputs out, int64_t npix, float4* __restrict__ rows,
@@ -269,7 +269,7 @@ k_mlp_rows(const __grid_constant__ DevScene scene, const unsigned long long* __r
       pix = base + s_list[j];
       const int x = (int)(pix / H), y = (int)(pix - (int64_t)x * H);
       PixelGeom pg;
-      const bool hit = pixel_geometry<false, PLAIN>(sc, rec, s_key[j], x, y, out, pg);
+      const bool hit = pixel_geometry(sc, rec, s_key[j], x, y, out, pg);
       if (hit && pg.flat) {
         store_rgb(fr, out, pix, pg.fg.color);  // a line pixel
       } else if (hit) {
@@ -363,7 +363,7 @@ static cudaError_t sm_count(int& nsm) {
   return e;
 }
 
-template <int NL, bool TEX, int SIG, bool PLAIN = false>
+template <int NL, bool TEX, int SIG>
 static cudaError_t launch_shade_mlp_t(const DevScene& sc, const unsigned long long* keys,
                                       const float4* rec, const t3_outputs& out, int64_t npix,
                                       int32_t* status, cudaStream_t st, const MlpRows& rows,
@@ -375,8 +375,8 @@ static cudaError_t launch_shade_mlp_t(const DevScene& sc, const unsigned long lo
     constexpr int BLOCK = 256, PPT = 4;
     const int64_t grid = (npix + BLOCK * PPT - 1) / (BLOCK * PPT);
     if (grid <= 0) return cudaSuccess;
-    k_mlp_rows<BLOCK, PPT, NL, TEX, SIG, PLAIN><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix,
-                                                                                rows.rows, rows.count, reset);
+    k_mlp_rows<BLOCK, PPT, NL, TEX, SIG><<<(unsigned)grid, BLOCK, 0, st>>>(sc, keys, rec, out, npix, rows.rows,
+                                                                         rows.count, reset);
     e = cudaGetLastError();
     if (e == cudaSuccess && rows.split) e = cudaEventRecord(rows.split, st);
     if (e == cudaSuccess)
@@ -402,15 +402,12 @@ cudaError_t launch_shade_mlp(const DevScene& sc, const unsigned long long* keys,
   const int64_t npix = (int64_t)sc.frame.width * sc.frame.height;
   // untextured PBR scenes take the instance with the lobe kinds as constants,
   // and with each material parameter evaluated once when every object has the
-  // PBR material shape (its row prepass compiled for plain face soups when
-  // the frame has only those)
-  if (!has_textures(sc) && fast_signature(sc) == T3_SIG_PBR) {
-    if (plain_soups(sc))
-      return launch_shade_mlp_t<2, false, T3_SIG_PBR | T3_SIG_FAST, true>(sc, keys, rec, out, npix, status, st,
-                                                                          rows, reset);
+  // PBR material shape.  (A row prepass compiled for plain face soups, as the
+  // lamp pass has, rounds some network inputs differently from the one-kernel
+  // pass of the allocation-free frame, whose pixels must stay equal to these.)
+  if (!has_textures(sc) && fast_signature(sc) == T3_SIG_PBR)
     return launch_shade_mlp_t<2, false, T3_SIG_PBR | T3_SIG_FAST>(sc, keys, rec, out, npix, status, st, rows,
                                                                   reset);
-  }
   if (!has_textures(sc) && lobe_signature(sc) == T3_SIG_PBR)
     return launch_shade_mlp_t<2, false, T3_SIG_PBR>(sc, keys, rec, out, npix, status, st, rows, reset);
   if (max_lobes(sc) <= 2) return launch_shade_mlp_t<2, true, 0>(sc, keys, rec, out, npix, status, st, rows, reset);

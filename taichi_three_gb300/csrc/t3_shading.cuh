@@ -19,7 +19,17 @@ __device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y +
 __device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
 __device__ __forceinline__ V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
-__device__ __forceinline__ float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+// The products and sums of dot and lerp3 are written as explicit FMAs, so every
+// kernel instance that interpolates a fragment gets the same bits (left to the
+// compiler, the contraction of a sum of products can differ between instances
+// with different surrounding code, and the network's Fourier features of the
+// normal can then round to different BF16 values).
+__device__ __forceinline__ float dot(V3 a, V3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+// wa A + wb B + wc C, summed in that order
+__device__ __forceinline__ V3 lerp3(float wa, float wb, float wc, V3 A, V3 B, V3 C) {
+  return v3(fmaf(wc, C.x, fmaf(wb, B.x, wa * A.x)), fmaf(wc, C.y, fmaf(wb, B.y, wa * A.y)),
+            fmaf(wc, C.z, fmaf(wb, B.z, wa * A.z)));
+}
 __device__ __forceinline__ V3 normalized(V3 a) { return rsqrtf(dot(a, a)) * a; }
 // Approximate reciprocal, reciprocal square root and quotient for the
 // shading-only arithmetic (lamp terms, BRDF lobes, view ray, ACES), whose
@@ -38,7 +48,7 @@ __device__ __forceinline__ float rcp_fast(float x) {
 __device__ __forceinline__ float div_fast(float a, float b) { return a * rcp_fast(b); }
 __device__ __forceinline__ V3 normalized_fast(V3 a) { return rsqrt_fast(dot(a, a)) * a; }
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
-  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+  return v3(fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x)));
 }
 __device__ __forceinline__ V3 one_minus(V3 a) { return v3(1.0f - a.x, 1.0f - a.y, 1.0f - a.z); }
 __device__ __forceinline__ V3 tov(f3 a) { return v3(a.x, a.y, a.z); }
@@ -448,13 +458,13 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   // interpolate (triangle.py:32-49)
   Frag& fg = g.fg;
   const V3 A = tov(v[0]), B = tov(v[1]), C = tov(v[2]);
-  fg.pos = (wei.x * A + wei.y * B) + wei.z * C;
+  fg.pos = lerp3(wei.x, wei.y, wei.z, A, B, C);
   V3 nrm;
   if (fr.flags & T3_SMOOTHING) {
     f3 nn[3];
     if constexpr (PLAIN) soup_corners(mesh.norms, n, nn);
     else face_norms(mesh, ref, nn);
-    nrm = (wei.x * tov(nn[0]) + wei.y * tov(nn[1])) + wei.z * tov(nn[2]);
+    nrm = lerp3(wei.x, wei.y, wei.z, tov(nn[0]), tov(nn[1]), tov(nn[2]));
   } else {
     nrm = cross(B - A, C - A);
   }
@@ -463,8 +473,8 @@ __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
   if (fr.flags & T3_TEXTURING) {
     f2 t[3];
     face_coors(mesh, ref, t);
-    fg.tex = f2{(wei.x * t[0].x + wei.y * t[1].x) + wei.z * t[2].x,
-                (wei.x * t[0].y + wei.y * t[1].y) + wei.z * t[2].y};
+    fg.tex = f2{fmaf(wei.z, t[2].x, fmaf(wei.y, t[1].x, wei.x * t[0].x)),
+                fmaf(wei.z, t[2].y, fmaf(wei.y, t[1].y, wei.x * t[0].y))};
   }
   fg.attr = mesh.face_attr ? mesh.face_attr + ref.f * mesh.attr_stride : nullptr;
   fg.color = v3(1.f, 1.f, 1.f);
