@@ -71,3 +71,52 @@ def test_outputs_at_unaligned_addresses(cuda, oracle_mod):
          'depth_f': bufs['depth_f'][1:].view(W, H).cpu().numpy()}
     _assert_matches(g, o)
     assert bufs['face_id'][0].item() == -7 and bufs['rgb'][0].item() == -7.0
+
+
+def test_one_block_clear_when_the_hint_is_stale(cuda, oracle_mod):
+    """The host remembers that a workspace's last direct frame emptied the keys
+    and launches the next frame's clear as one block.  A CUDA graph captured
+    then and replayed after a binned frame has scribbled over the workspace
+    (and reset its key tag) must still give the oracle's frame: the one block
+    finds the tag changed and clears every key."""
+    W, H = 128, 96
+    scene, _ = random_soup_scene(33, ntri=2000, res=(W, H), nlights=3)
+    o = oracle_mod.render(scene)
+    lib = N.load()
+    sc, keep = scene.describe(cuda)
+    sizes = []
+    for mode in (N.T3_RASTER_DIRECT, N.T3_RASTER_BINNED):
+        n = C.c_size_t()
+        assert lib.t3_workspace_size(C.byref(sc), mode, 16, 0, C.byref(n)) == N.T3_OK
+        sizes.append(n.value)
+    ws = torch.zeros(max(sizes), dtype=torch.uint8, device=cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    bufs = {'rgb': torch.empty((W, H, 3), device=cuda), 'face_id': torch.empty((W, H), dtype=torch.int32, device=cuda),
+            'depth': torch.empty((W, H), dtype=torch.int32, device=cuda), 'depth_f': torch.empty((W, H), device=cuda)}
+    outs = N.t3_outputs(bufs['rgb'].data_ptr(), bufs['face_id'].data_ptr(), bufs['depth'].data_ptr(),
+                        bufs['depth_f'].data_ptr())
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+
+    def frame(mode, stream):
+        rc = lib.t3_render(C.byref(sc), mode, 16, 0, ws.data_ptr(), ws.numel(), status.data_ptr(),
+                           C.byref(outs), stream.cuda_stream)
+        assert rc == N.T3_OK
+
+    with torch.cuda.stream(side):
+        frame(N.T3_RASTER_DIRECT, side)
+        frame(N.T3_RASTER_DIRECT, side)  # the keys are now empty, and the host knows it
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            frame(N.T3_RASTER_DIRECT, side)  # captured with the one-block clear
+    torch.cuda.synchronize()
+    frame(N.T3_RASTER_BINNED, torch.cuda.current_stream())  # another layout over the same bytes
+    torch.cuda.synchronize()
+    for f in ('rgb', 'face_id', 'depth', 'depth_f'):
+        bufs[f].fill_(-7)
+    g.replay()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    g_out = {k: v.cpu().numpy() for k, v in bufs.items()}
+    _assert_matches(g_out, o)
