@@ -619,7 +619,8 @@ def main():
     for e in evs:
         lib.t3_event_destroy(e)
 
-    # algorithmic bytes per launch ("Roofline accounting")
+    # algorithmic bytes per launch: every input byte the stage must read and
+    # every output byte it must write once, nothing for re-reads
     P = W * H
     fid = scene.face_id
     visible = int(torch.unique(fid[fid >= 0]).numel())
