@@ -358,8 +358,11 @@ __device__ __forceinline__ void warp_raster_spans(WarpFaces& wf, WarpCols& wc, c
   for (int base = 0; base < npix; base += 32) {
     unsigned bits = 0u;
 #pragma unroll
-    for (int q = 0; q < kMaxWarpCols / 32; q++)
-      if (cst[q] >= base && cst[q] < base + 32) bits |= 1u << (cst[q] - base);
+    for (int q = 0; q < kMaxWarpCols / 32; q++) {
+      if (32 * q >= ncand) break;  // warp-uniform: no column starts in the registers from here on
+      const unsigned d = (unsigned)(cst[q] - base);
+      if (d < 32u) bits |= 1u << d;
+    }
     const unsigned starts = __reduce_or_sync(FULL, bits);
     const int idx = base + lane;
     if (idx < npix) {
