@@ -361,7 +361,9 @@ struct PixelGeom {
 // launch (read through L2, not the read-only path).  PLAIN: every object of
 // the frame is a face soup without mesh edits (plain_soups), so the line,
 // particle, transform and corner-order paths are compiled out (fewer
-// registers and instructions, the same values).
+// registers and instructions; the raster outputs are the same bits, the
+// shading arithmetic may round differently in its last bit where the
+// compiler contracts it differently, well inside the RGB tolerance).
 template <bool COHERENT_REC = false, bool PLAIN = false>
 __device__ __forceinline__ bool pixel_geometry(const DevScene* __restrict__ sc,
                                                const float4* __restrict__ rec,
